@@ -1,0 +1,192 @@
+"""Synthetic inputs for the second-order solve path (host side, numpy).
+
+Builds the structured meshes and seeded initial states that the solver is run
+on.  The meshes follow the reference's generators:
+
+* ``cuboid_tet4``: the structured cell grid of
+  ``symx/src/solver/mesh_generation.cpp:38-91`` (vertex index
+  ``i*(ny+1)*(nz+1) + j*(nz+1) + k``, every cell split into the same 6 tets
+  around the v0-v6 diagonal, :76-83).
+* ``cuboid_hex8``: ``mesh_generation.cpp:161-206`` (node order
+  ``(-,-,-),(+,-,-),(+,+,-),(-,+,-)`` then the same at z+).
+
+Two deliberate differences, both pure relabelings/translations that leave the
+physics unchanged: the reference's reverse Cuthill-McKee renumbering
+(``mesh_generation.cpp:89``) is not applied (the lexicographic numbering of a
+structured grid is already banded), and the box is translated from
+``[-L/2, L/2]`` to ``[0, L]`` so that the clamped face is ``x = 0``.
+
+Random numbers come from a splitmix64 stream with a Box-Muller transform,
+written out here so that the same seed gives the same inputs on every numpy
+version and machine.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n consecutive outputs of the splitmix64 generator started at ``seed``."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, n + 1, dtype=np.uint64)
+        z = (np.uint64(seed) + idx * np.uint64(0x9E3779B97F4A7C15)) & _M64
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed: int, n: int) -> np.ndarray:
+    """n doubles in (0, 1) from the top 53 bits of splitmix64."""
+    z = splitmix64(seed, n)
+    return ((z >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def normal(seed: int, n: int, mean: float = 0.0, std: float = 1.0) -> np.ndarray:
+    """n standard-normal samples (Box-Muller over pairs of uniforms)."""
+    m = (n + 1) // 2
+    u = uniform01(seed, 2 * m)
+    u1, u2 = u[0::2], u[1::2]
+    r = np.sqrt(-2.0 * np.log(u1))
+    z = np.empty(2 * m)
+    z[0::2] = r * np.cos(2.0 * np.pi * u2)
+    z[1::2] = r * np.sin(2.0 * np.pi * u2)
+    return mean + std * z[:n]
+
+
+def _grid_vertices(nx, ny, nz, size):
+    size = np.asarray(size, dtype=np.float64)
+    delta = size / np.array([nx, ny, nz], dtype=np.float64)
+    i, j, k = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    ijk = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float64)
+    return ijk * delta
+
+
+def _cell_corners(nx, ny, nz):
+    def index(i, j, k):
+        return i * (ny + 1) * (nz + 1) + j * (nz + 1) + k
+
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    v = [index(i, j, k), index(i + 1, j, k), index(i + 1, j + 1, k), index(i, j + 1, k),
+         index(i, j, k + 1), index(i + 1, j, k + 1), index(i + 1, j + 1, k + 1), index(i, j + 1, k + 1)]
+    return [a.astype(np.int32) for a in v]
+
+
+def cuboid_tet4(nx: int, ny: int, nz: int, size):
+    """Structured Tet4 box on [0, size]: (vertices (nv,3) f64, tets (6*cells,4) i32)."""
+    X = _grid_vertices(nx, ny, nz, size)
+    v0, v1, v2, v3, v4, v5, v6, v7 = _cell_corners(nx, ny, nz)
+    tets = np.stack([
+        np.stack([v0, v1, v6, v5], 1), np.stack([v0, v1, v2, v6], 1),
+        np.stack([v0, v2, v3, v6], 1), np.stack([v0, v5, v6, v4], 1),
+        np.stack([v0, v6, v3, v7], 1), np.stack([v0, v6, v7, v4], 1)], axis=1)
+    return X, tets.reshape(-1, 4).astype(np.int32)
+
+
+def cuboid_hex8(nx: int, ny: int, nz: int, size):
+    """Structured Hex8 box on [0, size]: (vertices (nv,3) f64, hexes (cells,8) i32)."""
+    X = _grid_vertices(nx, ny, nz, size)
+    hexes = np.stack(_cell_corners(nx, ny, nz), axis=1)
+    return X, hexes.astype(np.int32)
+
+
+def lame(youngs, poisson):
+    """(mu, lambda) from Young's modulus and Poisson ratio (examples/NeoHookean.cpp:71-72)."""
+    youngs = np.asarray(youngs, dtype=np.float64)
+    mu = youngs / (2.0 * (1.0 + poisson))
+    lam = youngs * poisson / ((1.0 + poisson) * (1.0 - 2.0 * poisson))
+    return mu, lam
+
+
+_HEX8_SIGNS = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                        [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], dtype=np.float64)
+
+
+def element_volumes(X, conn):
+    """Rest volume of each element (Tet4: |det|/6; Hex8: 2x2x2 Gauss sum of det J)."""
+    if conn.shape[1] == 4:
+        P = X[conn]
+        D = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=2)
+        return np.abs(np.linalg.det(D)) / 6.0
+    P = X[conn]  # (ne, 8, 3)
+    g = 1.0 / np.sqrt(3.0)
+    vol = np.zeros(conn.shape[0])
+    for q in _HEX8_SIGNS * g:
+        dN = np.empty((8, 3))
+        for a, s in enumerate(_HEX8_SIGNS):
+            f = 0.5 * (1.0 + s * q)
+            dN[a] = [0.5 * s[0] * f[1] * f[2], 0.5 * s[1] * f[0] * f[2], 0.5 * s[2] * f[0] * f[1]]
+        J = np.einsum("eai,aj->eij", P, dN)
+        vol += np.linalg.det(J)
+    return vol
+
+
+def lumped_mass(X, conn, density):
+    """Per-vertex lumped mass: each element gives density*volume/nodes to each node
+    (examples/dynamic_elasticity_with_contact.cpp:66-79)."""
+    vol = element_volumes(X, conn)
+    m = np.zeros(X.shape[0])
+    share = density * vol / conn.shape[1]
+    for a in range(conn.shape[1]):
+        np.add.at(m, conn[:, a], share)
+    return m
+
+
+# Named workloads.  `cells` per axis, spacing h, and the seeds used for each random field.
+CONFIGS = {
+    # Plain FP64 Neo-Hookean Tet4 implicit-Euler step: 10^3 cells, 1,331 vertices, 6,000 tets.
+    "tet4_10": dict(kind="tet4", cells=(10, 10, 10), h=0.01, perturb=0.0, seed=0),
+    # Scaled-up step: 64^3 cells, 274,625 vertices, 1,572,864 tets, 5% spacing perturbation.
+    "tet4_64": dict(kind="tet4", cells=(64, 64, 64), h=0.01, perturb=0.05, seed=1),
+    # Hex8 slab, 128x128x32 cells, log-normal Young's modulus per element.
+    "hex8_128x128x32": dict(kind="hex8", cells=(128, 128, 32), h=0.01, perturb=0.0, seed=2,
+                            youngs_lognormal_sigma=0.5),
+    # Smaller cases used by parity tests.
+    "tet4_3": dict(kind="tet4", cells=(3, 3, 3), h=0.01, perturb=0.0, seed=10),
+    "tet4_6p": dict(kind="tet4", cells=(6, 5, 4), h=0.01, perturb=0.05, seed=11),
+    "hex8_3": dict(kind="hex8", cells=(3, 3, 2), h=0.01, perturb=0.0, seed=12,
+                   youngs_lognormal_sigma=0.5),
+    "tet4_32": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.0, seed=3),
+    "tet4_40": dict(kind="tet4", cells=(40, 40, 40), h=0.01, perturb=0.0, seed=4),
+}
+
+
+def step_problem(name_or_cfg, *, youngs=1e5, poisson=0.3, density=1000.0, dt=1.0 / 60.0,
+                 gravity=(0.0, -9.81, 0.0), v_std=0.5, k_bc=1e8):
+    """One implicit-Euler step of a clamped Neo-Hookean box.
+
+    Returns a dict of numpy arrays: X (rest), x0 (previous positions), v0, x_init
+    (initial Newton guess = x0), mass, conn, mu, lam (per element), bc_idx (vertices
+    with x == 0), bc_target (their rest positions), and scalars dt, gravity, k_bc.
+    """
+    cfg = CONFIGS[name_or_cfg] if isinstance(name_or_cfg, str) else dict(name_or_cfg)
+    nx, ny, nz = cfg["cells"]
+    h = cfg["h"]
+    size = (nx * h, ny * h, nz * h)
+    if cfg["kind"] == "tet4":
+        X, conn = cuboid_tet4(nx, ny, nz, size)
+    else:
+        X, conn = cuboid_hex8(nx, ny, nz, size)
+    nv, ne = X.shape[0], conn.shape[0]
+    seed = int(cfg["seed"])
+    sigma = cfg.get("youngs_lognormal_sigma", 0.0)
+    if sigma > 0.0:
+        E = np.exp(normal(seed * 1000 + 3, ne, mean=np.log(youngs), std=sigma))
+    else:
+        E = np.full(ne, youngs)
+    mu, lam = lame(E, poisson)
+    mass = lumped_mass(X, conn, density)
+    v0 = normal(seed * 1000 + 1, nv * 3, std=v_std).reshape(nv, 3)
+    x0 = X.copy()
+    if cfg.get("perturb", 0.0) > 0.0:
+        x0 = x0 + (cfg["perturb"] * h) * (2.0 * uniform01(seed * 1000 + 2, nv * 3) - 1.0).reshape(nv, 3)
+    bc_idx = np.nonzero(X[:, 0] <= 1e-12)[0].astype(np.int32)
+    return dict(
+        name=cfg.get("name", name_or_cfg if isinstance(name_or_cfg, str) else "custom"),
+        X=X, x0=x0, v0=v0, x_init=x0.copy(), mass=mass, conn=conn, mu=mu, lam=lam,
+        bc_idx=bc_idx, bc_target=X[bc_idx].copy(), dt=float(dt),
+        gravity=np.asarray(gravity, dtype=np.float64), k_bc=float(k_bc),
+    )

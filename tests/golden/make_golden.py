@@ -1,0 +1,199 @@
+"""Regenerate the golden fixtures in tests/golden/ from the reference SymX itself.
+
+Test infrastructure.  Runs oracle/_ref/symx_ref_harness (the unmodified reference,
+compiled from its own sources by ``make -f oracle/Makefile.ref``) on seeded inputs
+and stores its outputs as small .npz files.  Only this script needs the reference;
+the tests read the committed .npz files.
+
+    make -f oracle/Makefile.ref -j8 && python tests/golden/make_golden.py
+
+Fixtures:
+  elem_nh_tet4.npz     per-element NH Tet4 [E, g(12), H(144)] via Compiled<double>
+                        (value_gradient_hessian, diff.cpp:209-214), 64 seeded elements
+  project12.npz        project_to_PD_inplace (project_to_PD.cpp:12-32) on 48 12x12 matrices
+  project24.npz        same on 12 24x24 matrices (the reference's dynamic-size path)
+  doc_hessian_kat.npz  the 12x12 NH Hessian printed in docs/source/compilation.md:269-281
+  <case>_eval.npz      E, gradient, element Hessians, BCSR triplets at the initial state
+  <case>_solve.npz     final positions and iteration counts of NewtonsMethod::solve
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from symx_gb300 import problems  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "symx_ref_harness")
+REF_DOC = "/root/reference/docs/source/compilation.md"
+
+
+def run(*args):
+    subprocess.run([HARNESS, *map(str, args)], check=True, stdout=subprocess.DEVNULL)
+
+
+def write_problem(path, p):
+    nv, ne, nn = p["X"].shape[0], p["conn"].shape[0], p["conn"].shape[1]
+    with open(path, "wb") as f:
+        np.array([nv, ne, p["bc_idx"].size, nn], dtype=np.int64).tofile(f)
+        np.array([p["dt"], *p["gravity"], p["k_bc"]], dtype=np.float64).tofile(f)
+        for k in ("X", "x0", "v0", "x_init"):
+            np.ascontiguousarray(p[k], dtype=np.float64).tofile(f)
+        np.ascontiguousarray(p["mass"], dtype=np.float64).tofile(f)
+        np.ascontiguousarray(p["conn"], dtype=np.int32).tofile(f)
+        np.ascontiguousarray(p["mu"], dtype=np.float64).tofile(f)
+        np.ascontiguousarray(p["lam"], dtype=np.float64).tofile(f)
+        np.ascontiguousarray(p["bc_idx"], dtype=np.int32).tofile(f)
+        np.ascontiguousarray(p["bc_target"], dtype=np.float64).tofile(f)
+
+
+def random_tets(seed, n):
+    """Seeded Tet4 inputs: rest shapes around a regular tet, deformations from mild to
+    strong compression, a few nearly inverted."""
+    rows = np.empty((n, 26))
+    base = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    u = problems.uniform01(seed, n * 40).reshape(n, 40)
+    for e in range(n):
+        Xr = 0.01 * (base + 0.2 * (u[e, 0:12].reshape(4, 3) - 0.5))
+        strength = [0.05, 0.3, 0.8][e % 3]
+        x = Xr + 0.01 * strength * (u[e, 12:24].reshape(4, 3) - 0.5)
+        x += u[e, 24:27] * 0.1  # rigid translation
+        mu, lam = problems.lame(1e5 * (0.5 + u[e, 27]), 0.3 + 0.15 * u[e, 28])
+        rows[e, 0:12] = x.ravel()
+        rows[e, 12:24] = Xr.ravel()
+        rows[e, 24], rows[e, 25] = mu, lam
+    return rows
+
+
+def make_elem(tmp):
+    n = 64
+    rows = random_tets(7, n)
+    fin = os.path.join(tmp, "elem_in.bin")
+    fout = os.path.join(tmp, "elem_out.bin")
+    with open(fin, "wb") as f:
+        np.array([n], dtype=np.int64).tofile(f)
+        rows.tofile(f)
+    run("elem", fin, fout)
+    out = np.fromfile(fout, dtype=np.float64).reshape(n, 157)
+    np.savez_compressed(os.path.join(HERE, "elem_nh_tet4.npz"), inputs=rows, outputs=out)
+    return rows, out
+
+
+def make_project(tmp, elem_out):
+    # 12x12: real NH element Hessians (always indefinite or singular: rigid modes) and
+    # seeded symmetric random matrices with a spread of negative eigenvalues.
+    mats = [elem_out[i, 13:].reshape(12, 12) for i in range(32)]
+    z = problems.normal(21, 16 * 144).reshape(16, 12, 12)
+    for i in range(16):
+        a = z[i] + z[i].T
+        a += np.eye(12) * (1.0 * (i % 4) - 1.0)
+        mats.append(a * 10.0 ** (i % 5 - 2))
+    fixtures = {}
+    for n, mlist, name in ((12, mats, "project12"), (24, None, "project24")):
+        if mlist is None:
+            z = problems.normal(22, 12 * 576).reshape(12, 24, 24)
+            mlist = [(z[i] + z[i].T) * 10.0 ** (i % 4) + np.eye(24) * (i % 3 - 1.0) for i in range(12)]
+        arr = np.stack(mlist).astype(np.float64)
+        fin = os.path.join(tmp, f"{name}_in.bin")
+        fout = os.path.join(tmp, f"{name}_out.bin")
+        with open(fin, "wb") as f:
+            np.array([arr.shape[0], n], dtype=np.int64).tofile(f)
+            arr.tofile(f)
+        run("project", fin, fout)
+        out = np.fromfile(fout, dtype=np.float64).reshape(arr.shape)
+        changed = np.fromfile(fout + ".changed", dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), inputs=arr, outputs=out, changed=changed)
+        fixtures[name] = out
+    return fixtures
+
+
+def make_doc_kat():
+    text = open(REF_DOC).read()
+    m = re.search(r"Hessian = \n(.*?)```", text, re.S)
+    rows = [list(map(float, line.split())) for line in m.group(1).strip().splitlines()]
+    H = np.array(rows)
+    assert H.shape == (12, 12)
+    x = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    X = np.array([[0, 0, 0], [0.9, 0, 0], [0, 0.8, 0], [0, 0, 0.7]], dtype=np.float64)
+    mu, lam = problems.lame(1e6, 0.3)
+    np.savez_compressed(os.path.join(HERE, "doc_hessian_kat.npz"), H=H, x=x, X=X, mu=mu, lam=lam,
+                        source="docs/source/compilation.md:269-281 (printed to 6 significant digits)")
+
+
+def make_case(tmp, case, solve_iters=(1, -1), keep_triplets=True):
+    p = problems.step_problem(case)
+    pfile = os.path.join(tmp, f"{case}.bin")
+    write_problem(pfile, p)
+    ev = os.path.join(tmp, f"{case}_eval")
+    os.makedirs(ev, exist_ok=True)
+    run("eval", pfile, ev, 1)
+    rd = lambda name, dt: np.fromfile(os.path.join(ev, name), dtype=dt)  # noqa: E731
+    E = rd("E.bin", np.float64)[0]
+    grad = rd("grad.bin", np.float64)
+    sizes = rd("hess_elem_size.bin", np.int32)
+    hv = rd("hess_elem.bin", np.float64)
+    hp = rd("hess_elem_projected.bin", np.float64)
+    ti = rd("bcsr_triplet_idx.bin", np.int32).reshape(-1, 2)
+    tv = rd("bcsr_triplet_val.bin", np.float64)
+    ne = p["conn"].shape[0]
+    n_el = 3 * p["conn"].shape[1]
+    # element Hessians of the elastic potential come first (definition order)
+    assert np.all(sizes[:ne] == n_el)
+    H_el = hv[: ne * n_el * n_el].reshape(ne, n_el, n_el)
+    H_el_p = hp[: ne * n_el * n_el].reshape(ne, n_el, n_el)
+    ndof = grad.size
+    out = dict(E=E, E_only=rd("E_only.bin", np.float64)[0], grad=grad, ndof=ndof)
+    sample = np.unique(np.linspace(0, ne - 1, min(ne, 48)).astype(np.int64))
+    out.update(hess_sample_idx=sample, hess_sample=H_el[sample], hess_sample_projected=H_el_p[sample])
+    # the assembled projected matrix: exact triplets for small cases, products with seeded
+    # vectors (a size-independent fingerprint) for all cases
+    import scipy.sparse as sp
+    A = sp.coo_matrix((tv, (ti[:, 0], ti[:, 1])), shape=(ndof, ndof)).tocsr()
+    V = problems.normal(99, 2 * ndof).reshape(2, ndof)
+    out.update(probe_vectors=V, probe_products=np.stack([A @ v for v in V]),
+               diag=A.diagonal(), nnz=A.nnz)
+    if keep_triplets:
+        out.update(triplet_idx=ti, triplet_val=tv)
+    np.savez_compressed(os.path.join(HERE, f"{case}_eval.npz"), **out)
+
+    sol = {}
+    for iters in solve_iters:
+        sd = os.path.join(tmp, f"{case}_solve_{iters}")
+        os.makedirs(sd, exist_ok=True)
+        subprocess.run([HARNESS, "solve", pfile, sd, "1", str(iters), "1e-3"],
+                       check=False, stdout=open(os.path.join(sd, "log.txt"), "w"))
+        stats = json.load(open(os.path.join(sd, "stats.json")))
+        tag = "full" if iters < 0 else f"it{iters}"
+        sol[f"x_{tag}"] = np.fromfile(os.path.join(sd, "x_final.bin"), dtype=np.float64).reshape(-1, 3)
+        for k in ("return", "newton_iterations", "cg_iterations", "ls_bt_iterations"):
+            sol[f"{k}_{tag}"] = stats[k]
+        sol[f"log_{tag}"] = open(os.path.join(sd, "log.txt")).read()
+    np.savez_compressed(os.path.join(HERE, f"{case}_solve.npz"), **sol)
+    return out, sol
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference first: make -f oracle/Makefile.ref -j8")
+    with tempfile.TemporaryDirectory() as tmp:
+        rows, out = make_elem(tmp)
+        make_project(tmp, out)
+        make_doc_kat()
+        make_case(tmp, "tet4_3")
+        make_case(tmp, "tet4_6p")
+        make_case(tmp, "hex8_3")
+        make_case(tmp, "tet4_10", keep_triplets=False)
+    for f in sorted(os.listdir(HERE)):
+        print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
