@@ -1,0 +1,342 @@
+"""Benchmark: Newton step time of SymX's second-order solve path on one GB300.
+
+Workload (the metric's configuration): one implicit-Euler step of a clamped Neo-Hookean
+Tet4 cube, 64^3 cells = 274,625 vertices and 1,572,864 tets, dt = 1/60, E = 1e5 Pa,
+nu = 0.3, seeded 5%-of-spacing perturbation of the initial positions, solved by projected
+Newton (eps 1e-10, block-Jacobi PCG to relative 1e-3, Armijo c = 1e-4) to
+max |grad E| < 1e-6.  Synthetic, seeded inputs (symx_gb300.problems, "tet4_64").
+
+A bench step is one complete implicit-Euler step solve from the same initial state.
+`value` is the Newton step time: device ms of that solve divided by its Newton
+iterations, in mixed precision; the all-FP64 GPU form of the same solve is timed in the
+same run (`fp64`).  Inputs stay resident in HBM for `value`; `e2e` times the same solve
+through the C ABI with host arrays (state upload + solve + position download each step).
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference] [--config tet4_64]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton step time at 1.57M tets: mixed-precision vs FP64 GPU, 1e-6 rel residual"
+UNIT = "ms"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while a region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def spmv_roofline(solver, torch, sg, n_rep=30):
+    """Time the BCSR SpMV kernel (the PCG's dominant HBM-bound kernel) on the assembled
+    mixed-precision Hessian of the workload, with CUDA events on its stream."""
+    rp, cols, vals = solver.assembled_hessian(project=True)
+    dev = torch.device("cuda")
+    rp_t = torch.tensor(rp, device=dev)
+    cols_t = torch.tensor(cols, device=dev)
+    vals_t = torch.tensor(vals, dtype=torch.float32, device=dev)
+    n = 3 * (rp.size - 1)
+    x = torch.randn(n, dtype=torch.float32, device=dev)
+    y = torch.zeros_like(x)
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        sg.bcsr_spmv(rp_t, cols_t, vals_t, x, y)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2
+    times = []
+    for _ in range(n_rep):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        sg.bcsr_spmv(rp_t, cols_t, vals_t, x, y)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b) * 1e-3)
+    nnzb, nb = cols.size, rp.size - 1
+    algo_bytes = nnzb * (9 * 4 + 4) + (nb + 1) * 4 + n * 4 + n * 4
+    t = statistics.median(times)
+    return {"nnzb": int(nnzb), "n_block_rows": int(nb), "algorithmic_bytes": int(algo_bytes), "seconds": t}
+
+
+def run_ours(args):
+    import torch
+
+    import symx_gb300 as sg
+    from symx_gb300 import problems
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    p = problems.step_problem(args.config)
+    solver = sg.ElasticSolver(p)
+    solver.set_settings(cg_rel_tolerance=1e-3, precision="mixed")
+
+    def device_solve(precision):
+        solver.set_settings(precision=precision)
+        solver.set_state(p["x_init"], p["x0"], p["v0"])
+        solver.upload()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        st = solver.solve_device()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), st
+
+    # warm-up (also compiles / loads the generated kernels)
+    for _ in range(args.warmup):
+        device_solve("mixed")
+    lc0 = sg.load().symxg_launch_count()
+    ms, stats = [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t, st = device_solve("mixed")
+            ms.append(t)
+            stats.append(st)
+    lc1 = sg.load().symxg_launch_count()
+    st = stats[-1]
+    assert st["solver_return"] == 0 and st["final_residual"] < 1e-6, st
+    solver.download()
+    x_mixed = solver.get_positions()
+    newton_its = st["newton_iterations"]
+    ms_step = statistics.mean(ms)
+
+    # all-FP64 GPU form of the same solve
+    fp64_ms, fp64_st = [], None
+    for i in range(max(1, args.fp64_steps) + 1):
+        t, s64 = device_solve("fp64")
+        if i > 0:
+            fp64_ms.append(t)
+        fp64_st = s64
+    solver.download()
+    x_fp64 = solver.get_positions()
+
+    # end to end through the C ABI with host arrays
+    solver.set_settings(precision="mixed")
+    e2e_ms, e2e_st = [], None
+    for i in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.set_state(p["x_init"], p["x0"], p["v0"])
+        e2e_st = solver.solve()
+        x_host = solver.get_positions()
+        t1 = time.perf_counter()
+        if i > 0:
+            e2e_ms.append((t1 - t0) * 1e3)
+
+    # max over ranks (replicas)
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([ms_step], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    if rank != 0:
+        return None
+
+    peak, peak_kind = measured_peaks()
+    rf = spmv_roofline(solver, torch, sg)
+    achieved = rf["algorithmic_bytes"] / rf["seconds"] / 1e9
+    rel_vs_fp64 = float(np.linalg.norm(x_mixed - x_fp64) / np.linalg.norm(x_fp64))
+    out = {
+        "metric": METRIC,
+        "value": round(ms_step / newton_its, 4),
+        "unit": UNIT + " per Newton step",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 Hessian/PCG, f64 energy/gradient/line search",
+        "data": "synthetic (seeded 64^3 Tet4 cube)",
+        "config": {"workload": "Neo-Hookean Tet4 implicit-Euler step, 64^3 cells (274,625 vertices, 1,572,864 tets)",
+                   "name": args.config, "precision": "mixed", "newton_iterations": newton_its,
+                   "cg_iterations": st["cg_iterations"], "final_residual": st["final_residual"],
+                   "l2": "working set > L2 (element Hessians 0.9 GB, BCSR 0.16 GB)",
+                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "stage_seconds": {k: round(st[k], 6) for k in st if k.startswith("t_")},
+        "fp64": {"ms_per_step": round(statistics.mean(fp64_ms), 3),
+                 "ms_per_newton_step": round(statistics.mean(fp64_ms) / fp64_st["newton_iterations"], 4),
+                 "newton_iterations": fp64_st["newton_iterations"], "cg_iterations": fp64_st["cg_iterations"],
+                 "stage_seconds": {k: round(fp64_st[k], 6) for k in fp64_st if k.startswith("t_")}},
+        "mixed_vs_fp64_step_speedup": round(statistics.mean(fp64_ms) / ms_step, 3),
+        "mixed_vs_fp64_position_rel_err": rel_vs_fp64,
+        "e2e": {"value": round(statistics.mean(e2e_ms) / e2e_st["newton_iterations"], 4),
+                "unit": UNIT + " per Newton step", "ms_per_step": round(statistics.mean(e2e_ms), 3),
+                "h2d_bytes_per_step": int(e2e_st["h2d_bytes"]), "d2h_bytes_per_step": int(e2e_st["d2h_bytes"])},
+        "gpu_launches": int((lc1 - lc0) / max(1, args.steps)),
+        "gpu_launches_total": int(lc1 - lc0),
+        "roofline": {"kernel": "k_bcsr_spmv<float> (PCG SpMV, standalone launch on the assembled Hessian)",
+                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "algorithmic_bytes": rf["algorithmic_bytes"], "launch_seconds": rf["seconds"], "traffic": None},
+        "clocks": clocks.summary(),
+    }
+    if args.cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(p, args)
+    return out
+
+
+def cpu_baseline(p, args):
+    """The oracle restatement of the reference's CPU path on this host's cores, on a bounded
+    sample of the same workload: the first `n` Newton iterations of the same solve."""
+    from oracle import oracle as O
+
+    n = args.cpu_newton_iterations
+    P = O.Problem(p, 0)
+    threads = O.lib().oracle_num_threads()
+    P.set_x(p["x_init"])
+    st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, max_iterations=n, max_iterations_as_success=1))
+    its = max(1, st["newton_iterations"])
+    return {"value": round(st["t_total"] * 1e3 / its, 3), "unit": UNIT + " per Newton step", "cores": threads,
+            "kind": "port",
+            "sample": f"first {its} Newton iterations of the same tet4_64 solve (oracle port, OpenMP), "
+                      f"{st['t_total']:.1f} s; cg {st['cg_iterations']}",
+            "stage_seconds": {k: round(st[k], 3) for k in ("t_eval", "t_project", "t_assembly", "t_linear_solve",
+                                                            "t_line_search")}}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    from symx_gb300 import problems
+
+    p = problems.step_problem(args.config)
+    P = O.Problem(p, 0)
+    threads = O.lib().oracle_num_threads()
+    n = args.cpu_newton_iterations
+    per_step = []
+    for i in range(args.warmup + args.steps):
+        P.set_x(p["x_init"])
+        st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, max_iterations=n, max_iterations_as_success=1))
+        if i >= args.warmup:
+            per_step.append(st["t_total"] * 1e3 / max(1, st["newton_iterations"]))
+    v = statistics.mean(per_step)
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT + " per Newton step",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v * n, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 64^3 Tet4 cube)",
+        "config": {"workload": "Neo-Hookean Tet4 implicit-Euler step, 64^3 cells (274,625 vertices, 1,572,864 tets)",
+                   "name": args.config},
+        "cpu_baseline": {"value": round(v, 3), "unit": UNIT + " per Newton step", "cores": threads, "kind": "port",
+                         "sample": f"each step: the first {n} Newton iterations of the same solve, from the same state"},
+        "e2e": {"value": round(v, 3), "unit": UNIT + " per Newton step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="tet4_64")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-newton-iterations", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    rank, world, _ = dist_env()
+    if world > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(dist_env()[2])
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        out = run_reference(args)
+    else:
+        if world > 1 and rank != 0:
+            args.cpu_baseline = False
+        out = run_ours(args)
+    if out is not None and rank == 0:
+        print(json.dumps(out))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,175 @@
+/*
+ * symx_gb300 C ABI: the GPU second-order solve path of SymX behind plain C types.
+ *
+ * The reference (InteractiveComputerGraphics/SymX) is a C++ library whose solve path is
+ * reached through GlobalPotential::add_potential + NewtonsMethod::solve
+ * (symx/src/solver/GlobalPotential.h:37-76, symx/src/solver/NewtonsMethod.h:83-87) and whose
+ * generated kernels sit behind a dlopen'ed plugin ABI `void f(T* in, T* out)` with
+ * get_n_inputs/get_n_outputs (symx/src/compile/Compilation.cpp:292-323).  This header is
+ * the C boundary of the GPU implementation: opaque handles, host or device pointers and
+ * sizes, int status codes (0 = success), never exit() or a trap.  The C++ API
+ * (include/symx) is the drop-in for C++ users; this ABI is what an FFI binds.
+ *
+ * Threading: one handle must not be used from two threads at once; separate handles are
+ * independent.  All work of a handle runs on its own CUDA stream on the current device.
+ */
+#ifndef SYMX_GB300_H
+#define SYMX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SYMXG_ABI_VERSION 1
+
+/* status codes */
+#define SYMXG_OK 0
+#define SYMXG_ERR_INVALID_ARGUMENT 1
+#define SYMXG_ERR_RUNTIME 2 /* CUDA, NVRTC or internal failure; see symxg_last_error() */
+
+/* arithmetic of the Hessian path */
+#define SYMXG_PRECISION_FP64 0
+#define SYMXG_PRECISION_MIXED 1 /* FP32 element Hessians, projection, BCSR and PCG vectors;
+                                   FP64 energy, gradient, residual, line search, dot sums */
+
+/* solver return codes: same values and meaning as symx::SolverReturn
+   (symx/src/solver/solver_utils.h:15-26) */
+#define SYMXG_SOLVER_SUCCESSFUL 0
+#define SYMXG_SOLVER_TOO_MANY_ITERATIONS 3
+#define SYMXG_SOLVER_TOO_MANY_ARMIJO_ITERATIONS 4
+#define SYMXG_SOLVER_LINEAR_SYSTEM_SOLVE_FAILURE 5
+#define SYMXG_SOLVER_STEP_DOES_NOT_DESCEND 7
+
+typedef struct symxg_solver symxg_solver;
+
+/* One implicit-Euler step (or a quasistatic solve when mass == NULL) of a clamped
+ * Neo-Hookean solid, written with the reference's own idioms: classic Neo-Hookean density
+ * (examples/elasticity_potentials.h:7-13) integrated with the FEM rule of the element type
+ * (symx/src/solver/fem_integrators.cpp:52-133), backward-Euler inertia
+ * 1/2 m |x - (x0 + dt v0 + dt^2 g)|^2 / dt^2 (examples/dynamic_elasticity_with_contact.cpp:86-103)
+ * and penalty Dirichlet 1/2 k |x - target|^2 (examples/rubber_extrusion.cpp:94-107).
+ * All arrays are copied at creation. */
+typedef struct symxg_elastic_problem {
+    int32_t n_vertices;
+    int32_t n_elements;
+    int32_t nodes_per_element;     /* 4 (Tet4) or 8 (Hex8) */
+    const int32_t* connectivity;   /* n_elements * nodes_per_element */
+    const double* rest_positions;  /* n_vertices * 3 */
+    const double* mu;              /* n_elements Lame mu */
+    const double* lambda;          /* n_elements Lame lambda */
+    const double* mass;            /* n_vertices lumped masses, or NULL (no inertia term) */
+    double dt;
+    double gravity[3];
+    int32_t n_bc;
+    const int32_t* bc_vertices;    /* n_bc */
+    const double* bc_targets;      /* n_bc * 3 */
+    double bc_stiffness;
+} symxg_elastic_problem;
+
+/* Mirror of symx::NewtonSettings (symx/src/solver/solver_utils.h:272-358) for the fields
+ * the GPU path implements, plus the precision. */
+typedef struct symxg_newton_settings {
+    int32_t max_iterations;
+    int32_t min_iterations;
+    double residual_tolerance_abs;
+    double residual_tolerance_rel;
+    double step_tolerance;
+    int32_t max_iterations_as_success;
+    double step_cap;
+    int32_t enable_armijo_backtracking;
+    double line_search_armijo_beta;
+    int32_t max_backtracking_armijo_iterations;
+    int32_t project_to_pd;           /* 1 ProjectedNewton (default), 0 plain Newton */
+    double projection_eps;
+    int32_t project_to_pd_use_mirroring;
+    int32_t cg_max_iterations;
+    double cg_abs_tolerance;
+    double cg_rel_tolerance;
+    double bailout_residual;
+    int32_t precision;               /* SYMXG_PRECISION_* */
+} symxg_newton_settings;
+
+typedef struct symxg_solve_stats {
+    int32_t solver_return;
+    int32_t newton_iterations;
+    int32_t cg_iterations;
+    int32_t ls_bt_iterations;
+    double final_residual;           /* max |grad| at the last evaluation */
+    double final_energy;
+    int32_t projection_not_converged;
+    double t_evaluate_P_grad_hess;   /* device seconds per stage (CUDA events) */
+    double t_project_to_PD;
+    double t_assembly;
+    double t_linear_system_solve;
+    double t_evaluate_P;
+    int64_t h2d_bytes;               /* host->device bytes of the last upload */
+    int64_t d2h_bytes;               /* device->host bytes of the last download */
+} symxg_solve_stats;
+
+/* message of the last failing call on this thread ("" if none) */
+const char* symxg_last_error(void);
+int symxg_abi_version(void);
+void symxg_default_settings(symxg_newton_settings* settings);
+
+/* Build the potentials, differentiate, generate and compile (NVRTC, cached in cache_dir or
+ * the default cache when NULL) the element kernels, and build the BCSR sparsity. */
+int symxg_elastic_create(const symxg_elastic_problem* problem, const char* cache_dir, symxg_solver** out);
+int symxg_destroy(symxg_solver* solver);
+int symxg_set_settings(symxg_solver* solver, const symxg_newton_settings* settings);
+
+/* Host state: positions x (the DoFs, also the Newton initial guess), previous positions
+ * x0 and velocities v0 (each n_vertices*3; x0/v0 may be NULL to keep the current ones). */
+int symxg_set_state(symxg_solver* solver, const double* x, const double* x0, const double* v0);
+int symxg_get_positions(symxg_solver* solver, double* x);
+
+/* NewtonsMethod::solve(): upload the host state, run the Newton loop on the device,
+ * download the positions.  solver_return receives a SYMXG_SOLVER_* code. */
+int symxg_solve(symxg_solver* solver, int32_t* solver_return, symxg_solve_stats* stats);
+
+/* Device-resident pieces of symxg_solve for callers that keep the state on the GPU. */
+int symxg_upload(symxg_solver* solver);
+int symxg_solve_device(symxg_solver* solver, int32_t* solver_return, symxg_solve_stats* stats);
+int symxg_download(symxg_solver* solver);
+
+/* Energy and gradient (n_vertices*3, may be NULL) at the host state. */
+int symxg_evaluate(symxg_solver* solver, double* energy, double* grad);
+/* Energy only, at the host state (line-search kernel). */
+int symxg_evaluate_energy(symxg_solver* solver, double* energy);
+/* Assembled Hessian at the host state in the current precision, projected or not.
+ * Call with vals == NULL to get n_blocks and nnzb; then row_ptr (n_blocks+1), cols (nnzb)
+ * and vals (nnzb*9, row-major 3x3 blocks, as double). */
+int symxg_assembled_hessian(symxg_solver* solver, int32_t project, int32_t* n_blocks, int64_t* nnzb,
+                            int32_t* row_ptr, int32_t* cols, double* vals);
+/* Element outputs of potential `potential` (0 elastic, 1 inertia, 2 boundary) at the host
+ * state: E (n), g (n*m), H (n*m*m row-major, optionally projected), m = 3 * nodes. */
+int symxg_element_outputs(symxg_solver* solver, int32_t potential, int32_t project, double* E, double* g, double* H);
+/* Number of scalar operations in the generated code of a potential: E+g, H, E-only. */
+int symxg_op_counts(symxg_solver* solver, int32_t potential, int64_t counts[3]);
+
+/* Number of CUDA kernels this library has launched since it was loaded (all handles). */
+int64_t symxg_launch_count(void);
+
+/* ---- stand-alone kernels on caller-owned DEVICE memory (stream: a cudaStream_t or NULL) ---- */
+
+/* Project `count` symmetric n x n matrices (n = 3k <= 24), stored block-major (3x3 block
+ * (a,b) at offset (a*k+b)*9, row-major inside), in place.  not_converged: device int set
+ * to 1 if a Jacobi sweep cap was hit.  Replaces project_to_PD_inplace
+ * (symx/src/solver/second_order/project_to_PD.cpp:12-81). */
+int symxg_project_pd_f32(float* matrices, int32_t n, int64_t count, float eps, int32_t mirroring,
+                         int32_t* not_converged, void* stream);
+int symxg_project_pd_f64(double* matrices, int32_t n, int64_t count, double eps, int32_t mirroring,
+                         int32_t* not_converged, void* stream);
+/* y = A x for a 3x3-block CSR matrix (row_ptr n_blocks+1, cols nnzb, vals nnzb*9 row-major
+ * blocks).  Replaces BlockedSparseMatrix::spmxv_from_ptr (BlockedSparseMatrix.h:986-1138). */
+int symxg_bcsr_spmv_f32(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
+                        const float* x, float* y, void* stream);
+int symxg_bcsr_spmv_f64(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                        const double* x, double* y, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SYMX_GB300_H */

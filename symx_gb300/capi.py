@@ -1,0 +1,126 @@
+"""ctypes declarations of the C ABI in include/symx_gb300.h.
+
+`load()` opens the in-tree libsymxg.so and fails loudly if it has not been built: there
+is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsymxg.so")
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+SOLVER_RETURN = {
+    0: "Successful", 1: "Running", 2: "InvalidInitialState", 3: "TooManyIterations",
+    4: "TooManyArmijoIterations", 5: "LinearSystemSolveFailure",
+    6: "TooManyInvalidIntermediateIterations", 7: "StepDoesNotDescend", 8: "InvalidConvergedState",
+}
+
+# Every symbol include/symx_gb300.h declares (checked by the CPU tests).
+EXPORTS = [
+    "symxg_last_error", "symxg_abi_version", "symxg_default_settings", "symxg_elastic_create",
+    "symxg_destroy", "symxg_set_settings", "symxg_set_state", "symxg_get_positions", "symxg_solve",
+    "symxg_upload", "symxg_solve_device", "symxg_download", "symxg_evaluate", "symxg_evaluate_energy",
+    "symxg_assembled_hessian", "symxg_element_outputs", "symxg_op_counts", "symxg_project_pd_f32",
+    "symxg_project_pd_f64", "symxg_bcsr_spmv_f32", "symxg_bcsr_spmv_f64", "symxg_launch_count",
+]
+
+
+class ElasticProblem(C.Structure):
+    _fields_ = [
+        ("n_vertices", C.c_int32), ("n_elements", C.c_int32), ("nodes_per_element", C.c_int32),
+        ("connectivity", C.c_void_p), ("rest_positions", C.c_void_p), ("mu", C.c_void_p),
+        ("lam", C.c_void_p), ("mass", C.c_void_p), ("dt", C.c_double), ("gravity", C.c_double * 3),
+        ("n_bc", C.c_int32), ("bc_vertices", C.c_void_p), ("bc_targets", C.c_void_p),
+        ("bc_stiffness", C.c_double),
+    ]
+
+
+class NewtonSettings(C.Structure):
+    _fields_ = [
+        ("max_iterations", C.c_int32), ("min_iterations", C.c_int32),
+        ("residual_tolerance_abs", C.c_double), ("residual_tolerance_rel", C.c_double),
+        ("step_tolerance", C.c_double), ("max_iterations_as_success", C.c_int32),
+        ("step_cap", C.c_double), ("enable_armijo_backtracking", C.c_int32),
+        ("line_search_armijo_beta", C.c_double), ("max_backtracking_armijo_iterations", C.c_int32),
+        ("project_to_pd", C.c_int32), ("projection_eps", C.c_double),
+        ("project_to_pd_use_mirroring", C.c_int32), ("cg_max_iterations", C.c_int32),
+        ("cg_abs_tolerance", C.c_double), ("cg_rel_tolerance", C.c_double),
+        ("bailout_residual", C.c_double), ("precision", C.c_int32),
+    ]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [
+        ("solver_return", C.c_int32), ("newton_iterations", C.c_int32), ("cg_iterations", C.c_int32),
+        ("ls_bt_iterations", C.c_int32), ("final_residual", C.c_double), ("final_energy", C.c_double),
+        ("projection_not_converged", C.c_int32), ("t_evaluate_P_grad_hess", C.c_double),
+        ("t_project_to_PD", C.c_double), ("t_assembly", C.c_double),
+        ("t_linear_system_solve", C.c_double), ("t_evaluate_P", C.c_double),
+        ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+    ]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["solver_return_name"] = SOLVER_RETURN.get(self.solver_return, str(self.solver_return))
+        return d
+
+
+_lib = None
+
+
+class SymxgError(RuntimeError):
+    pass
+
+
+def load(path: str | None = None):
+    """Open libsymxg.so (built by symx_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise SymxgError(f"{p} is missing: build the CUDA library first (python -m symx_gb300.build)")
+    L = C.CDLL(p)
+    P = C.c_void_p
+    I32, I64, D = C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "symxg_last_error": ([], C.c_char_p),
+        "symxg_abi_version": ([], C.c_int),
+        "symxg_launch_count": ([], C.c_int64),
+        "symxg_default_settings": ([C.POINTER(NewtonSettings)], None),
+        "symxg_elastic_create": ([C.POINTER(ElasticProblem), C.c_char_p, C.POINTER(P)], C.c_int),
+        "symxg_destroy": ([P], C.c_int),
+        "symxg_set_settings": ([P, C.POINTER(NewtonSettings)], C.c_int),
+        "symxg_set_state": ([P, P, P, P], C.c_int),
+        "symxg_get_positions": ([P, P], C.c_int),
+        "symxg_solve": ([P, C.POINTER(I32), C.POINTER(SolveStats)], C.c_int),
+        "symxg_upload": ([P], C.c_int),
+        "symxg_solve_device": ([P, C.POINTER(I32), C.POINTER(SolveStats)], C.c_int),
+        "symxg_download": ([P], C.c_int),
+        "symxg_evaluate": ([P, P, P], C.c_int),
+        "symxg_evaluate_energy": ([P, P], C.c_int),
+        "symxg_assembled_hessian": ([P, I32, C.POINTER(I32), C.POINTER(I64), P, P, P], C.c_int),
+        "symxg_element_outputs": ([P, I32, I32, P, P, P], C.c_int),
+        "symxg_op_counts": ([P, I32, P], C.c_int),
+        "symxg_project_pd_f32": ([P, I32, I64, C.c_float, I32, P, P], C.c_int),
+        "symxg_project_pd_f64": ([P, I32, I64, D, I32, P, P], C.c_int),
+        "symxg_bcsr_spmv_f32": ([I32, P, P, P, P, P, P], C.c_int),
+        "symxg_bcsr_spmv_f64": ([I32, P, P, P, P, P, P], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != 0:
+        msg = load().symxg_last_error().decode(errors="replace")
+        raise SymxgError(f"symx_gb300 call failed (status {rc}): {msg}")

@@ -1,0 +1,403 @@
+// C ABI of symx_gb300 (declared in include/symx_gb300.h).
+//
+// The elastic-step problem is defined here with the same C++ user API a SymX user writes
+// (GlobalPotential::add_potential with MappedWorkspace lambdas, fem_integrator,
+// NewtonsMethod), so the C entry points exercise exactly the drop-in path.
+#include "../../include/symx_gb300.h"
+
+#include <array>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fem.h"
+#include "global_potential.h"
+#include "kernels.cuh"
+#include "newton.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F&& f)
+{
+    try {
+        g_last_error.clear();
+        return f();
+    } catch (const std::invalid_argument& e) {
+        g_last_error = e.what();
+        return SYMXG_ERR_INVALID_ARGUMENT;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return SYMXG_ERR_RUNTIME;
+    } catch (...) {
+        g_last_error = "unknown error";
+        return SYMXG_ERR_RUNTIME;
+    }
+}
+
+using Vec3 = std::array<double, 3>;
+
+}  // namespace
+
+struct symxg_solver {
+    // host data the potentials are bound to (the maps keep pointers to these members)
+    std::vector<Vec3> x, x0, v0, X, bc_target;
+    std::vector<double> mu, lam, mass;
+    std::vector<int32_t> conn_numbered;  // element index + nodes
+    std::vector<std::array<int32_t, 1>> vertices;
+    symx::LabelledConnectivity<2> bc_conn{{"constraint_idx", "vertex_idx"}};
+    double dt = 0.0, k_bc = 0.0;
+    Vec3 gravity{0, 0, 0};
+    int nodes = 0;
+    bool has_inertia = false;
+    symx::spGlobalPotential G;
+    std::unique_ptr<symx::NewtonsMethod> newton;
+};
+
+template <typename T>
+static int project_impl(T* m, int32_t n, int64_t count, T eps, int32_t mirroring, int32_t* nc, void* stream)
+{
+    return guarded([&] {
+        if (!m || !nc) throw std::invalid_argument("null device pointer");
+        if (n <= 0 || n % 3 != 0 || n > 24) throw std::invalid_argument("n must be a multiple of 3 up to 24");
+        if (count < 0) throw std::invalid_argument("negative count");
+        symxg::launch_project_pd<T>(m, n, count, eps, mirroring != 0, nc, (cudaStream_t)stream);
+        return SYMXG_OK;
+    });
+}
+
+template <typename T>
+static int spmv_impl(int32_t nb, const int32_t* rp, const int32_t* cols, const T* vals, const T* x, T* y, void* stream)
+{
+    return guarded([&] {
+        if (nb < 0) throw std::invalid_argument("negative size");
+        if (nb > 0 && (!rp || !cols || !vals || !x || !y)) throw std::invalid_argument("null device pointer");
+        if (nb > 0) symxg::launch_bcsr_spmv<T>(nb, rp, cols, vals, x, y, (cudaStream_t)stream);
+        return SYMXG_OK;
+    });
+}
+
+static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_solve_stats* o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->solver_return = (int32_t)r;
+    o->newton_iterations = st.newton_iterations;
+    o->cg_iterations = st.cg_iterations;
+    o->ls_bt_iterations = st.ls_bt_iterations;
+    o->final_residual = st.final_residual;
+    o->final_energy = st.final_energy;
+    o->projection_not_converged = st.projection_not_converged;
+    auto get = [&](const char* k) {
+        auto it = st.timers.find(k);
+        return it == st.timers.end() ? 0.0 : it->second;
+    };
+    o->t_evaluate_P_grad_hess = get("evaluate_P_grad_hess");
+    o->t_project_to_PD = get("project_to_PD");
+    o->t_assembly = get("assembly");
+    o->t_linear_system_solve = get("linear_system_solve");
+    o->t_evaluate_P = get("evaluate_P");
+    o->h2d_bytes = st.h2d_bytes;
+    o->d2h_bytes = st.d2h_bytes;
+}
+
+extern "C" {
+
+const char* symxg_last_error(void) { return g_last_error.c_str(); }
+int symxg_abi_version(void) { return SYMXG_ABI_VERSION; }
+int64_t symxg_launch_count(void) { return symxg::launch_count(); }
+
+void symxg_default_settings(symxg_newton_settings* s)
+{
+    const symx::NewtonSettings d;
+    s->max_iterations = d.max_iterations;
+    s->min_iterations = d.min_iterations;
+    s->residual_tolerance_abs = d.residual_tolerance_abs;
+    s->residual_tolerance_rel = d.residual_tolerance_rel;
+    s->step_tolerance = d.step_tolerance;
+    s->max_iterations_as_success = d.max_iterations_as_success ? 1 : 0;
+    s->step_cap = d.step_cap;
+    s->enable_armijo_backtracking = d.enable_armijo_backtracking ? 1 : 0;
+    s->line_search_armijo_beta = d.line_search_armijo_beta;
+    s->max_backtracking_armijo_iterations = d.max_backtracking_armijo_iterations;
+    s->project_to_pd = 1;
+    s->projection_eps = d.projection_eps;
+    s->project_to_pd_use_mirroring = d.project_to_pd_use_mirroring ? 1 : 0;
+    s->cg_max_iterations = d.cg_max_iterations;
+    s->cg_abs_tolerance = d.cg_abs_tolerance;
+    s->cg_rel_tolerance = d.cg_rel_tolerance;
+    s->bailout_residual = d.bailout_residual;
+    s->precision = SYMXG_PRECISION_FP64;
+}
+
+int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, symxg_solver** out)
+{
+    return guarded([&] {
+        if (!p || !out) throw std::invalid_argument("null argument");
+        if (p->nodes_per_element != 4 && p->nodes_per_element != 8)
+            throw std::invalid_argument("nodes_per_element must be 4 (Tet4) or 8 (Hex8)");
+        if (p->n_vertices <= 0 || p->n_elements < 0 || !p->connectivity || !p->rest_positions || !p->mu || !p->lambda)
+            throw std::invalid_argument("missing mesh or material arrays");
+        if (p->n_bc > 0 && (!p->bc_vertices || !p->bc_targets)) throw std::invalid_argument("missing boundary arrays");
+        const int nn = p->nodes_per_element;
+        for (int64_t i = 0; i < (int64_t)p->n_elements * nn; ++i)
+            if (p->connectivity[i] < 0 || p->connectivity[i] >= p->n_vertices)
+                throw std::invalid_argument("connectivity references a vertex out of range");
+        for (int i = 0; i < p->n_bc; ++i)
+            if (p->bc_vertices[i] < 0 || p->bc_vertices[i] >= p->n_vertices)
+                throw std::invalid_argument("boundary vertex out of range");
+        auto S = std::make_unique<symxg_solver>();
+        const int nv = p->n_vertices;
+        S->nodes = nn;
+        S->X.resize(nv);
+        std::memcpy(S->X.data(), p->rest_positions, sizeof(double) * 3 * nv);
+        S->x = S->X;
+        S->x0 = S->X;
+        S->v0.assign(nv, Vec3{0, 0, 0});
+        S->mu.assign(p->mu, p->mu + p->n_elements);
+        S->lam.assign(p->lambda, p->lambda + p->n_elements);
+        S->has_inertia = p->mass != nullptr;
+        if (S->has_inertia) S->mass.assign(p->mass, p->mass + nv);
+        S->dt = p->dt;
+        S->gravity = {p->gravity[0], p->gravity[1], p->gravity[2]};
+        S->k_bc = p->bc_stiffness;
+        S->conn_numbered.reserve((size_t)p->n_elements * (nn + 1));
+        for (int e = 0; e < p->n_elements; ++e) {
+            S->conn_numbered.push_back(e);
+            for (int a = 0; a < nn; ++a) S->conn_numbered.push_back(p->connectivity[(int64_t)e * nn + a]);
+        }
+        S->vertices.resize(nv);
+        for (int i = 0; i < nv; ++i) S->vertices[i] = {i};
+        for (int i = 0; i < p->n_bc; ++i) {
+            S->bc_conn.numbered_push_back({p->bc_vertices[i]});
+            S->bc_target.push_back({p->bc_targets[3 * i], p->bc_targets[3 * i + 1], p->bc_targets[3 * i + 2]});
+        }
+
+        using namespace symx;
+        symxg_solver* s = S.get();
+        const FEM_Element type = nn == 4 ? FEM_Element::Tet4 : FEM_Element::Hex8;
+        S->G = GlobalPotential::create();
+        S->G->add_potential("neo_hookean_" + get_name(type), S->conn_numbered, nn + 1,
+            [s, type, nn](MappedWorkspace<double>& mws, Element& elem) {
+                std::vector<Vector> x = mws.make_vectors(s->x, elem.slice(1, nn + 1));
+                std::vector<Vector> X = mws.make_vectors(s->X, elem.slice(1, nn + 1));
+                Scalar mu = mws.make_scalar(s->mu, elem[0]);
+                Scalar lam = mws.make_scalar(s->lam, elem[0]);
+                return fem_integrator(mws, type, [&](Scalar& w, Vector& xi) {
+                    Matrix Jx = fem_jacobian(type, x, xi);
+                    Matrix JX = fem_jacobian(type, X, xi);
+                    Matrix F = Jx * JX.inv();
+                    Matrix C = F.transpose() * F;
+                    Scalar logdetF = log(F.det());
+                    Scalar psi = 0.5 * mu * (C.trace() - 3.0) - mu * logdetF + 0.5 * lam * logdetF.powN(2);
+                    return psi * JX.det() * w;
+                });
+            });
+        if (S->has_inertia) {
+            S->G->add_potential("backward_euler_inertia", S->vertices, [s](MappedWorkspace<double>& mws, Element& elem) {
+                Vector x1 = mws.make_vector(s->x, elem[0]);
+                Vector x0 = mws.make_vector(s->x0, elem[0]);
+                Vector v0 = mws.make_vector(s->v0, elem[0]);
+                Scalar m = mws.make_scalar(s->mass, elem[0]);
+                Vector g = mws.make_vector(s->gravity);
+                Scalar dt = mws.make_scalar(s->dt);
+                Vector dev = x1 - (x0 + dt * v0 + dt * dt * g);
+                return 0.5 * m * dev.squared_norm() / dt.powN(2);
+            });
+        }
+        if (p->n_bc > 0) {
+            S->G->add_potential("boundary_conditions", S->bc_conn, [s](MappedWorkspace<double>& mws, Element& conn) {
+                Vector x = mws.make_vector(s->x, conn["vertex_idx"]);
+                Vector target = mws.make_vector(s->bc_target, conn["constraint_idx"]);
+                Scalar k = mws.make_scalar(s->k_bc);
+                return 0.5 * k * (x - target).squared_norm();
+            });
+        }
+        S->G->add_dof(S->x);
+        auto ctx = Context::create();
+        if (cache_dir) ctx->compilation_directory = cache_dir;
+        S->newton = std::make_unique<NewtonsMethod>(S->G, ctx);
+        *out = S.release();
+        return SYMXG_OK;
+    });
+}
+
+int symxg_destroy(symxg_solver* s)
+{
+    return guarded([&] {
+        delete s;
+        return SYMXG_OK;
+    });
+}
+
+int symxg_set_settings(symxg_solver* s, const symxg_newton_settings* c)
+{
+    return guarded([&] {
+        if (!s || !c) throw std::invalid_argument("null argument");
+        if (c->precision != SYMXG_PRECISION_FP64 && c->precision != SYMXG_PRECISION_MIXED)
+            throw std::invalid_argument("unknown precision");
+        symx::NewtonSettings& t = s->newton->settings;
+        t.max_iterations = c->max_iterations;
+        t.min_iterations = c->min_iterations;
+        t.residual_tolerance_abs = c->residual_tolerance_abs;
+        t.residual_tolerance_rel = c->residual_tolerance_rel;
+        t.step_tolerance = c->step_tolerance;
+        t.max_iterations_as_success = c->max_iterations_as_success != 0;
+        t.step_cap = c->step_cap;
+        t.enable_armijo_backtracking = c->enable_armijo_backtracking != 0;
+        t.line_search_armijo_beta = c->line_search_armijo_beta;
+        t.max_backtracking_armijo_iterations = c->max_backtracking_armijo_iterations;
+        t.projection_mode = c->project_to_pd ? symx::ProjectionToPD::ProjectedNewton : symx::ProjectionToPD::Newton;
+        t.projection_eps = c->projection_eps;
+        t.project_to_pd_use_mirroring = c->project_to_pd_use_mirroring != 0;
+        t.cg_max_iterations = c->cg_max_iterations;
+        t.cg_abs_tolerance = c->cg_abs_tolerance;
+        t.cg_rel_tolerance = c->cg_rel_tolerance;
+        t.bailout_residual = c->bailout_residual;
+        t.precision = c->precision == SYMXG_PRECISION_MIXED ? symx::Precision::Mixed : symx::Precision::FP64;
+        return SYMXG_OK;
+    });
+}
+
+int symxg_set_state(symxg_solver* s, const double* x, const double* x0, const double* v0)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null solver");
+        const size_t n = s->x.size() * 3;
+        if (x) std::memcpy(s->x.data(), x, sizeof(double) * n);
+        if (x0) std::memcpy(s->x0.data(), x0, sizeof(double) * n);
+        if (v0) std::memcpy(s->v0.data(), v0, sizeof(double) * n);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_get_positions(symxg_solver* s, double* x)
+{
+    return guarded([&] {
+        if (!s || !x) throw std::invalid_argument("null argument");
+        std::memcpy(x, s->x.data(), sizeof(double) * 3 * s->x.size());
+        return SYMXG_OK;
+    });
+}
+
+int symxg_solve(symxg_solver* s, int32_t* ret, symxg_solve_stats* stats)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null solver");
+        const symx::SolverReturn r = s->newton->solve();
+        if (ret) *ret = (int32_t)r;
+        fill_stats(s->newton->get_last_solve_stats(), r, stats);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_upload(symxg_solver* s)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null solver");
+        s->newton->upload();
+        return SYMXG_OK;
+    });
+}
+
+int symxg_solve_device(symxg_solver* s, int32_t* ret, symxg_solve_stats* stats)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null solver");
+        const symx::SolverReturn r = s->newton->solve_device();
+        if (ret) *ret = (int32_t)r;
+        fill_stats(s->newton->get_last_solve_stats(), r, stats);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_download(symxg_solver* s)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null solver");
+        s->newton->download();
+        return SYMXG_OK;
+    });
+}
+
+int symxg_evaluate(symxg_solver* s, double* energy, double* grad)
+{
+    return guarded([&] {
+        if (!s || !energy) throw std::invalid_argument("null argument");
+        s->newton->upload();
+        *energy = s->newton->evaluate(grad);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_evaluate_energy(symxg_solver* s, double* energy)
+{
+    return guarded([&] {
+        if (!s || !energy) throw std::invalid_argument("null argument");
+        s->newton->upload();
+        *energy = s->newton->evaluate_energy();
+        return SYMXG_OK;
+    });
+}
+
+int symxg_assembled_hessian(symxg_solver* s, int32_t project, int32_t* n_blocks, int64_t* nnzb, int32_t* row_ptr,
+                            int32_t* cols, double* vals)
+{
+    return guarded([&] {
+        if (!s || !n_blocks || !nnzb) throw std::invalid_argument("null argument");
+        if (vals && (!row_ptr || !cols)) throw std::invalid_argument("row_ptr and cols are required with vals");
+        if (vals) s->newton->upload();
+        s->newton->assembled_hessian(project != 0, n_blocks, nnzb, row_ptr, cols, vals);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_element_outputs(symxg_solver* s, int32_t potential, int32_t project, double* E, double* g, double* H)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null solver");
+        if (potential < 0 || potential >= s->G->get_n_potentials()) throw std::invalid_argument("no such potential");
+        s->newton->upload();
+        s->newton->element_outputs(potential, project != 0, E, g, H);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_op_counts(symxg_solver* s, int32_t potential, int64_t counts[3])
+{
+    return guarded([&] {
+        if (!s || !counts) throw std::invalid_argument("null argument");
+        if (potential < 0 || potential >= s->G->get_n_potentials()) throw std::invalid_argument("no such potential");
+        const auto c = s->newton->op_counts(potential);
+        for (int i = 0; i < 3; ++i) counts[i] = c[i];
+        return SYMXG_OK;
+    });
+}
+
+int symxg_project_pd_f32(float* m, int32_t n, int64_t count, float eps, int32_t mirroring, int32_t* nc, void* stream)
+{
+    return project_impl<float>(m, n, count, eps, mirroring, nc, stream);
+}
+int symxg_project_pd_f64(double* m, int32_t n, int64_t count, double eps, int32_t mirroring, int32_t* nc, void* stream)
+{
+    return project_impl<double>(m, n, count, eps, mirroring, nc, stream);
+}
+
+int symxg_bcsr_spmv_f32(int32_t nb, const int32_t* rp, const int32_t* cols, const float* vals, const float* x, float* y,
+                        void* stream)
+{
+    return spmv_impl<float>(nb, rp, cols, vals, x, y, stream);
+}
+int symxg_bcsr_spmv_f64(int32_t nb, const int32_t* rp, const int32_t* cols, const double* vals, const double* x,
+                        double* y, void* stream)
+{
+    return spmv_impl<double>(nb, rp, cols, vals, x, y, stream);
+}
+
+}  // extern "C"

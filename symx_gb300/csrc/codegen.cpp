@@ -1,0 +1,135 @@
+#include "codegen.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+
+namespace symx {
+
+std::string double_literal(double v)
+{
+    if (std::isnan(v)) return "symxg_nan()";
+    if (std::isinf(v)) return v > 0 ? "symxg_inf()" : "(-symxg_inf())";
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%.17g", v);
+    std::string s(buf);
+    if (s.find_first_of(".eE") == std::string::npos) s += ".0";
+    return s;
+}
+
+std::string codegen_prelude()
+{
+    return R"(
+// ---- generated-code prelude ----
+__device__ __forceinline__ double symxg_inf() { return __longlong_as_double(0x7ff0000000000000LL); }
+__device__ __forceinline__ double symxg_nan() { return __longlong_as_double(0x7ff8000000000000LL); }
+// Natural/base-10 logarithm with the reference's guard: x <= 0 gives -inf
+// (symx/src/compile/Compilation.cpp:426-428).
+__device__ __forceinline__ double symxg_ln(double x) { return x > 0.0 ? log(x) : -symxg_inf(); }
+__device__ __forceinline__ float symxg_ln(float x) { return x > 0.0f ? logf(x) : -__int_as_float(0x7f800000); }
+__device__ __forceinline__ double symxg_log10(double x) { return x > 0.0 ? log10(x) : -symxg_inf(); }
+__device__ __forceinline__ float symxg_log10(float x) { return x > 0.0f ? log10f(x) : -__int_as_float(0x7f800000); }
+__device__ __forceinline__ double symxg_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float symxg_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double symxg_exp(double x) { return exp(x); }
+__device__ __forceinline__ float symxg_exp(float x) { return expf(x); }
+__device__ __forceinline__ double symxg_powf(double x, double p) { return pow(x, p); }
+__device__ __forceinline__ float symxg_powf(float x, float p) { return powf(x, p); }
+__device__ __forceinline__ double symxg_sin(double x) { return sin(x); }
+__device__ __forceinline__ float symxg_sin(float x) { return sinf(x); }
+__device__ __forceinline__ double symxg_cos(double x) { return cos(x); }
+__device__ __forceinline__ float symxg_cos(float x) { return cosf(x); }
+__device__ __forceinline__ double symxg_tan(double x) { return tan(x); }
+__device__ __forceinline__ float symxg_tan(float x) { return tanf(x); }
+__device__ __forceinline__ double symxg_asin(double x) { return asin(x); }
+__device__ __forceinline__ float symxg_asin(float x) { return asinf(x); }
+__device__ __forceinline__ double symxg_acos(double x) { return acos(x); }
+__device__ __forceinline__ float symxg_acos(float x) { return acosf(x); }
+__device__ __forceinline__ double symxg_atan(double x) { return atan(x); }
+__device__ __forceinline__ float symxg_atan(float x) { return atanf(x); }
+// x^n for n >= 2 by binary powering.
+template <typename T>
+__device__ __forceinline__ T symxg_powi(T x, int n)
+{
+    T r = T(1), b = x;
+    while (n > 0) { if (n & 1) r *= b; b *= b; n >>= 1; }
+    return r;
+}
+)";
+}
+
+std::string emit_device_function(const Expressions& g, const std::vector<int32_t>& outputs, const std::string& name,
+                                 const std::string& T, bool accumulate, OpCount* count)
+{
+    int32_t top = 0;
+    for (int32_t o : outputs) top = std::max(top, o);
+    std::vector<uint8_t> need(top + 1, 0);
+    for (int32_t o : outputs) need[o] = 1;
+    for (int32_t i = top; i >= 0; --i) {
+        if (!need[i]) continue;
+        const Node& n = g[i];
+        switch (n.op) {
+            case Op::Zero: case Op::One: case Op::Const: case Op::Symbol: break;
+            default:
+                if (n.a >= 0) need[n.a] = 1;
+                if (n.b >= 0 && n.op != Op::PowN) need[n.b] = 1;
+                if (n.c >= 0) need[n.c] = 1;
+        }
+    }
+    auto ref = [&](int32_t i) -> std::string {
+        const Node& n = g[i];
+        switch (n.op) {
+            case Op::Zero: return "(" + T + ")0";
+            case Op::One: return "(" + T + ")1";
+            case Op::Const: return "((" + T + ")" + double_literal(n.v) + ")";
+            case Op::Symbol: return "in[" + std::to_string((int32_t)n.v) + "]";
+            default: return "t" + std::to_string(i);
+        }
+    };
+    OpCount oc;
+    std::ostringstream s;
+    s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, " << T
+      << "* __restrict__ out)\n{\n";
+    for (int32_t i = 0; i <= top; ++i) {
+        if (!need[i]) continue;
+        const Node& n = g[i];
+        std::string e;
+        switch (n.op) {
+            case Op::Zero: case Op::One: case Op::Const: case Op::Symbol: continue;
+            case Op::Add: e = ref(n.a) + " + " + ref(n.b); ++oc.add; break;
+            case Op::Sub: e = ref(n.a) + " - " + ref(n.b); ++oc.sub; break;
+            case Op::Mul: e = ref(n.a) + " * " + ref(n.b); ++oc.mul; break;
+            case Op::Div: e = ref(n.a) + " / " + ref(n.b); ++oc.div; break;
+            case Op::Neg: e = "-" + ref(n.a); ++oc.neg; break;
+            case Op::PowN:
+                if (n.b == 2) { e = ref(n.a) + " * " + ref(n.a); ++oc.mul; }
+                else if (n.b == 3) { e = ref(n.a) + " * " + ref(n.a) + " * " + ref(n.a); oc.mul += 2; }
+                else { e = "symxg_powi<" + T + ">(" + ref(n.a) + ", " + std::to_string(n.b) + ")"; ++oc.pow; }
+                break;
+            case Op::PowF: e = "symxg_powf(" + ref(n.a) + ", (" + T + ")" + double_literal(n.v) + ")"; ++oc.pow; break;
+            case Op::Sqrt: e = "symxg_sqrt(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Ln: e = "symxg_ln(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Log10: e = "symxg_log10(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Exp: e = "symxg_exp(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Sin: e = "symxg_sin(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Cos: e = "symxg_cos(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Tan: e = "symxg_tan(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Asin: e = "symxg_asin(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Acos: e = "symxg_acos(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Atan: e = "symxg_atan(" + ref(n.a) + ")"; ++oc.transcendental; break;
+            case Op::Branch:
+                e = "(" + ref(n.c) + " > (" + T + ")0) ? " + ref(n.a) + " : " + ref(n.b);
+                ++oc.branch;
+                break;
+        }
+        s << "    const " << T << " t" << i << " = " << e << ";\n";
+    }
+    for (size_t k = 0; k < outputs.size(); ++k)
+        s << "    out[" << k << "] " << (accumulate ? "+=" : "=") << " " << ref(outputs[k]) << ";\n";
+    s << "}\n";
+    if (count) *count = oc;
+    return s.str();
+}
+
+}  // namespace symx

@@ -1,0 +1,35 @@
+// CUDA code generation from the expression DAG.
+//
+// The reference emits straight-line C++ for `void f(T* in, T* out)` and compiles it
+// with the system compiler (symx/src/compile/Compilation.cpp:243-469).  Here the
+// same DAG becomes a `__device__` function with the same slot contract
+// (in[i] = symbol i, out[k] = k-th requested expression), written for CUDA and
+// compiled at run time by NVRTC (cuda_module.h).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "symbolic.h"
+
+namespace symx {
+
+struct OpCount {
+    int64_t add = 0, sub = 0, mul = 0, div = 0, neg = 0, transcendental = 0, branch = 0, pow = 0;
+    int64_t total() const { return add + sub + mul + div + neg + transcendental + branch + pow; }
+};
+
+// Emit `__device__ __forceinline__ void <name>(const T* __restrict__ in, T* __restrict__ out)`
+// computing every expression of `outputs` (node ids) in type `T` ("double" or "float").
+// If `accumulate` is set, outputs are added to `out` instead of assigned (summations).
+std::string emit_device_function(const Expressions& g, const std::vector<int32_t>& outputs, const std::string& name,
+                                 const std::string& T, bool accumulate, OpCount* count = nullptr);
+
+// Prelude shared by all generated sources: guarded log, integer powers, infinities.
+std::string codegen_prelude();
+
+// Literal for a double constant in generated code, exact to the last bit.
+std::string double_literal(double v);
+
+}  // namespace symx

@@ -1,0 +1,80 @@
+#include "fem.h"
+
+#include <cmath>
+#include <stdexcept>
+
+namespace symx {
+
+std::string get_name(const FEM_Element& e)
+{
+    switch (e) {
+        case FEM_Element::Tet4: return "Tet4";
+        case FEM_Element::Tet10: return "Tet10";
+        case FEM_Element::Hex8: return "Hex8";
+        default: return "Hex27";
+    }
+}
+
+int get_stride(const FEM_Element& e)
+{
+    switch (e) {
+        case FEM_Element::Tet4: return 4;
+        case FEM_Element::Tet10: return 10;
+        case FEM_Element::Hex8: return 8;
+        default: return 27;
+    }
+}
+
+std::vector<std::array<double, 4>> get_integration_rule(const FEM_Element& e)
+{
+    if (e == FEM_Element::Tet4) return {{1.0 / 6.0, 0.25, 0.25, 0.25}};
+    if (e == FEM_Element::Hex8) {
+        const double p = 1.0 / std::sqrt(3.0);
+        return {{1.0, -p, -p, -p}, {1.0, p, -p, -p}, {1.0, p, p, -p}, {1.0, -p, p, -p},
+                {1.0, -p, -p, p},  {1.0, p, -p, p},  {1.0, p, p, p},  {1.0, -p, p, p}};
+    }
+    throw std::runtime_error("symx_gb300: integration rule available for Tet4 and Hex8");
+}
+
+Vector fem_interpolation(const FEM_Element& e, const std::vector<Vector>& vh, const Vector& xi)
+{
+    std::vector<Scalar> N;
+    if (e == FEM_Element::Tet4) {
+        if (vh.size() != 4) throw std::runtime_error("symx: Tet4 interpolation needs 4 nodes");
+        N = {1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+    } else if (e == FEM_Element::Hex8) {
+        if (vh.size() != 8) throw std::runtime_error("symx: Hex8 interpolation needs 8 nodes");
+        const Scalar xm = 0.5 * (1.0 - xi[0]), xp = 0.5 * (1.0 + xi[0]);
+        const Scalar ym = 0.5 * (1.0 - xi[1]), yp = 0.5 * (1.0 + xi[1]);
+        const Scalar zm = 0.5 * (1.0 - xi[2]), zp = 0.5 * (1.0 + xi[2]);
+        N = {xm * ym * zm, xp * ym * zm, xp * yp * zm, xm * yp * zm,
+             xm * ym * zp, xp * ym * zp, xp * yp * zp, xm * yp * zp};
+    } else {
+        throw std::runtime_error("symx_gb300: interpolation available for Tet4 and Hex8");
+    }
+    Vector x = vh[0] * N[0];
+    for (size_t a = 1; a < vh.size(); ++a) x = x + vh[a] * N[a];
+    return x;
+}
+
+Matrix fem_jacobian(const FEM_Element& e, const std::vector<Vector>& xh, const Vector& xi)
+{
+    const Vector x = fem_interpolation(e, xh, xi);
+    std::vector<Scalar> v;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) v.push_back(diff(x[i], xi[j]));
+    return Matrix(v, {3, 3});
+}
+
+Scalar fem_integrator(MappedWorkspace<double>& mws, const FEM_Element& e,
+                      std::function<Scalar(Scalar& w, Vector& xi)> summand)
+{
+    const std::vector<std::array<double, 4>> rule = get_integration_rule(e);
+    return mws.add_for_each(rule, [&](Vector& ip) {
+        Scalar w = ip[0];
+        Vector xi({ip[1], ip[2], ip[3]});
+        return summand(w, xi);
+    });
+}
+
+}  // namespace symx

@@ -1,0 +1,601 @@
+// Hand-written device kernels of the second-order solve path (sm_103a).
+//
+// Reference loops they replace:
+//   projection   symx/src/solver/second_order/ElementHessians.cpp:48-67 + project_to_PD.cpp:12-81
+//   assembly     ElementHessians.cpp:224-256 + BlockedSparseMatrix.h:780-895 (mutex-per-row insertion)
+//   gradient     SecondOrderCompiledPotential.cpp:158-169 + ParallelVector.h:185-197
+//   reductions   ParallelNumber.h:129-137, bsm_vector_ops.h:52-225
+//   SpMV         BlockedSparseMatrix.h:986-1138
+//   block Jacobi BlockedSparseMatrix.h:1146-1361
+//   PCG          solve_pcg.h:82-232
+// Every sum here is taken in a fixed order (no floating-point atomics), so results are
+// bitwise reproducible run to run.
+#include "kernels.cuh"
+#include "project_pd.cuh"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <stdexcept>
+#include <string>
+
+namespace symxg {
+
+namespace {
+
+constexpr int kWarp = 32;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide reduction of one value per thread (fixed tree order); result valid in thread 0.
+template <bool IsMax>
+__device__ double block_reduce(double v, double* sh)
+{
+    const int lane = threadIdx.x & (kWarp - 1), warp = threadIdx.x / kWarp;
+    const int nwarps = (blockDim.x + kWarp - 1) / kWarp;
+    v = IsMax ? warp_max(v) : warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = (lane < nwarps) ? sh[lane] : (IsMax ? 0.0 : 0.0);
+        v = IsMax ? warp_max(v) : warp_sum(v);
+    }
+    return v;
+}
+
+// Store this block's partial; the last block to arrive combines all partials in index
+// order and returns true in every one of its threads (result in *result of thread 0).
+// `nparts` partial arrays of gridDim.x doubles each are handled together.
+template <bool IsMax, int NPARTS>
+__device__ bool last_block_combine(const double (&mine)[NPARTS], double* partials, unsigned* ticket,
+                                   double (&result)[NPARTS])
+{
+    __shared__ double sh[32];
+    __shared__ bool is_last;
+    double blockv[NPARTS];
+#pragma unroll
+    for (int k = 0; k < NPARTS; ++k) blockv[k] = block_reduce<IsMax>(mine[k], sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NPARTS; ++k) partials[k * gridDim.x + blockIdx.x] = blockv[k];
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NPARTS; ++k) {
+        double acc = 0.0;
+        for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+            const double p = __ldcg(&partials[k * gridDim.x + i]);
+            acc = IsMax ? fmax(acc, p) : acc + p;
+        }
+        result[k] = block_reduce<IsMax>(acc, sh);
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+__device__ __forceinline__ void chunk_range(int64_t n, int64_t& begin, int64_t& end)
+{
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    begin = chunk * blockIdx.x;
+    end = begin + chunk < n ? begin + chunk : n;
+}
+
+__global__ void k_sum(const double* __restrict__ x, int64_t n, double* partials, unsigned* ticket, double* out)
+{
+    int64_t b, e;
+    chunk_range(n, b, e);
+    double acc = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) acc += x[i];
+    double mine[1] = {acc}, res[1];
+    if (last_block_combine<false, 1>(mine, partials, ticket, res) && threadIdx.x == 0) out[0] = res[0];
+}
+
+template <typename T>
+__global__ void k_max_abs(const T* __restrict__ x, int64_t n, double* partials, unsigned* ticket, double* out)
+{
+    int64_t b, e;
+    chunk_range(n, b, e);
+    double acc = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const double v = (double)x[i];
+        acc = fmax(acc, isnan(v) ? __longlong_as_double(0x7ff0000000000000LL) : fabs(v));
+    }
+    double mine[1] = {acc}, res[1];
+    if (last_block_combine<true, 1>(mine, partials, ticket, res) && threadIdx.x == 0) out[0] = res[0];
+}
+
+template <typename T>
+__global__ void k_dot_mixed(const T* __restrict__ a, const double* __restrict__ bv, int64_t n, double* partials,
+                            unsigned* ticket, double* out)
+{
+    int64_t b, e;
+    chunk_range(n, b, e);
+    double acc = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) acc += (double)a[i] * bv[i];
+    double mine[1] = {acc}, res[1];
+    if (last_block_combine<false, 1>(mine, partials, ticket, res) && threadIdx.x == 0) out[0] = res[0];
+}
+
+// ---------------------------------------------------------------- projection
+template <typename T, int N>
+__global__ void __launch_bounds__(128) k_project_pd_unrolled(T* __restrict__ H, int64_t count, T eps, int mirroring,
+                                                             int* not_converged)
+{
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= count) return;
+    int nc = 0;
+    symxg_dev::project_pd_inplace<T, N>(H + m * (N * N), eps, mirroring != 0, &nc);
+    if (nc) *not_converged = 1;
+}
+
+// Generic N (up to 24) with thread-private arrays; used for large element matrices.
+template <typename T>
+__global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, int N, int64_t count, T eps,
+                                                           int mirroring, int* not_converged)
+{
+    constexpr int NMAX = 24;
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= count) return;
+    T* h = H + m * (int64_t)N * N;
+    const int nb = N / 3;
+    auto bm = [nb](int i, int j) { return (((i / 3) * nb + (j / 3)) * 3 + (i % 3)) * 3 + (j % 3); };
+    T A[NMAX * NMAX], V[NMAX * NMAX];
+    T fro2 = T(0);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+            const T v = h[bm(i, j)];
+            A[i * NMAX + j] = v;
+            V[i * NMAX + j] = (i == j) ? T(1) : T(0);
+            fro2 += v * v;
+        }
+    int sweep = 0;
+    for (; sweep < symxg_dev::JacobiTol<T>::max_sweeps; ++sweep) {
+        T off = T(0);
+        for (int p = 0; p < N; ++p)
+            for (int q = p + 1; q < N; ++q) off += T(2) * A[p * NMAX + q] * A[p * NMAX + q];
+        if (!(off > symxg_dev::JacobiTol<T>::rel2() * fro2)) break;
+        for (int p = 0; p < N - 1; ++p)
+            for (int q = p + 1; q < N; ++q) {
+                const T apq = A[p * NMAX + q];
+                if (apq == T(0)) continue;
+                const T app = A[p * NMAX + p], aqq = A[q * NMAX + q];
+                const T tau = (aqq - app) / (T(2) * apq);
+                const T t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
+                const T c = T(1) / sqrt(T(1) + t * t), s = t * c;
+                for (int k = 0; k < N; ++k) {
+                    const T akp = A[k * NMAX + p], akq = A[k * NMAX + q];
+                    A[k * NMAX + p] = c * akp - s * akq;
+                    A[k * NMAX + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < N; ++k) {
+                    const T apk = A[p * NMAX + k], aqk = A[q * NMAX + k];
+                    A[p * NMAX + k] = c * apk - s * aqk;
+                    A[q * NMAX + k] = s * apk + c * aqk;
+                }
+                A[p * NMAX + q] = A[q * NMAX + p] = T(0);
+                for (int k = 0; k < N; ++k) {
+                    const T vkp = V[k * NMAX + p], vkq = V[k * NMAX + q];
+                    V[k * NMAX + p] = c * vkp - s * vkq;
+                    V[k * NMAX + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    if (sweep == symxg_dev::JacobiTol<T>::max_sweeps) *not_converged = 1;
+    bool changed = false;
+    for (int i = 0; i < N; ++i) {
+        T l = A[i * NMAX + i];
+        if (l < eps) { changed = true; l = mirroring ? -l : eps; }
+        A[i * NMAX + i] = l;
+    }
+    if (!changed) return;
+    for (int i = 0; i < N; ++i)
+        for (int j = i; j < N; ++j) {
+            T s = T(0);
+            for (int k = 0; k < N; ++k) s += V[i * NMAX + k] * A[k * NMAX + k] * V[j * NMAX + k];
+            h[bm(i, j)] = s;
+            h[bm(j, i)] = s;
+        }
+}
+
+// ---------------------------------------------------------------- assembly
+template <typename T>
+__global__ void k_assemble_blocks(int64_t nnzb, const int64_t* __restrict__ slot_ptr, const int32_t* __restrict__ contrib,
+                                  const T* __restrict__ blocks, T* __restrict__ vals)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nnzb) return;
+    T acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = T(0);
+    for (int64_t c = slot_ptr[s]; c < slot_ptr[s + 1]; ++c) {
+        const T* b = blocks + (int64_t)contrib[c] * 9;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] += b[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) vals[s * 9 + k] = acc[k];
+}
+
+__global__ void k_gather_gradient(int n_blocks, const int64_t* __restrict__ ptr, const int32_t* __restrict__ contrib,
+                                  const double* __restrict__ gel, double* __restrict__ g)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_blocks) return;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int64_t c = ptr[v]; c < ptr[v + 1]; ++c) {
+        const double* b = gel + (int64_t)contrib[c] * 3;
+        a0 += b[0];
+        a1 += b[1];
+        a2 += b[2];
+    }
+    g[3 * v] = a0;
+    g[3 * v + 1] = a1;
+    g[3 * v + 2] = a2;
+}
+
+// ---------------------------------------------------------------- block Jacobi
+template <typename T>
+__global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ diag_slot, const T* __restrict__ vals,
+                                     T* __restrict__ Dinv)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_blocks) return;
+    const T* m = vals + (int64_t)diag_slot[r] * 9;
+    // symmetric 3x3 inverse from the upper triangle (cofactors / determinant)
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[8];
+    const double c00 = d * f - e * e, c01 = c * e - b * f, c02 = b * e - c * d;
+    const double det = a * c00 + b * c01 + c * c02;
+    const double id = 1.0 / det;
+    T* o = Dinv + (int64_t)r * 9;
+    o[0] = (T)(c00 * id);
+    o[1] = (T)(c01 * id);
+    o[2] = (T)(c02 * id);
+    o[3] = o[1];
+    o[4] = (T)((a * f - c * c) * id);
+    o[5] = (T)((b * c - a * e) * id);
+    o[6] = o[2];
+    o[7] = o[5];
+    o[8] = (T)((a * d - b * b) * id);
+}
+
+// ---------------------------------------------------------------- SpMV / PCG
+constexpr int kSpmvThreads = 256;  // 16 rows per block, 16 lanes per row
+
+// Partial product of one block row over the lanes of a 16-lane group, reduced across the
+// group in a fixed butterfly order.  Valid in every lane of the group.
+template <typename T>
+__device__ __forceinline__ void row_product(int row, int lane16, const int32_t* __restrict__ row_ptr,
+                                            const int32_t* __restrict__ cols, const T* __restrict__ vals,
+                                            const T* __restrict__ x, T& s0, T& s1, T& s2)
+{
+    s0 = s1 = s2 = T(0);
+    const int kb = row_ptr[row], ke = row_ptr[row + 1];
+    for (int k = kb + lane16; k < ke; k += 16) {
+        const T* b = vals + (int64_t)k * 9;
+        const int c = cols[k];
+        const T x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
+        s0 += b[0] * x0 + b[1] * x1 + b[2] * x2;
+        s1 += b[3] * x0 + b[4] * x1 + b[5] * x2;
+        s2 += b[6] * x0 + b[7] * x1 + b[8] * x2;
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o, 16);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o, 16);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o, 16);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const int32_t* __restrict__ row_ptr,
+                                                            const int32_t* __restrict__ cols, const T* __restrict__ vals,
+                                                            const T* __restrict__ x, T* __restrict__ y)
+{
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    const int lane16 = threadIdx.x & 15;
+    if (row >= n_blocks) return;  // whole 16-lane groups exit together
+    T s0, s1, s2;
+    row_product<T>(row, lane16, row_ptr, cols, vals, x, s0, s1, s2);
+    if (lane16 == 0) {
+        y[3 * row] = s0;
+        y[3 * row + 1] = s1;
+        y[3 * row + 2] = s2;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B)
+{
+    if (B.state->done) return;
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    const int lane16 = threadIdx.x & 15;
+    double pq = 0.0;
+    if (row < B.n_blocks) {
+        T s0, s1, s2;
+        row_product<T>(row, lane16, B.row_ptr, B.cols, B.vals, B.p, s0, s1, s2);
+        if (lane16 == 0) {
+            B.q[3 * row] = s0;
+            B.q[3 * row + 1] = s1;
+            B.q[3 * row + 2] = s2;
+            pq = (double)B.p[3 * row] * (double)s0 + (double)B.p[3 * row + 1] * (double)s1 +
+                 (double)B.p[3 * row + 2] * (double)s2;
+        }
+    }
+    double mine[1] = {pq}, res[1];
+    if (last_block_combine<false, 1>(mine, B.partials, B.tickets, res) && threadIdx.x == 0) {
+        PcgState* st = B.state;
+        st->pAp = res[0];
+        if (!(res[0] > 0.0)) {  // indefinite (or NaN): stop as the reference does
+            st->indefinite = 1;
+            st->converged = 0;
+            st->done = 1;
+            st->iteration += 1;
+        } else {
+            st->alpha = st->rz / res[0];
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_pcg_update(PcgBuffers<T> B)
+{
+    if (B.state->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, rz = 0.0;
+    if (i < B.n_blocks) {
+        const double alpha = B.state->alpha;
+        T r[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int k = 3 * i + d;
+            B.x[k] = (T)((double)B.x[k] + alpha * (double)B.p[k]);
+            r[d] = (T)((double)B.r[k] - alpha * (double)B.q[k]);
+            B.r[k] = r[d];
+        }
+        const T* m = B.Dinv + (int64_t)i * 9;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T z = m[3 * d] * r[0] + m[3 * d + 1] * r[1] + m[3 * d + 2] * r[2];
+            B.z[3 * i + d] = z;
+            rr += (double)r[d] * (double)r[d];
+            rz += (double)r[d] * (double)z;
+        }
+    }
+    double mine[2] = {rr, rz}, res[2];
+    if (last_block_combine<false, 2>(mine, B.partials, B.tickets + 1, res) && threadIdx.x == 0) {
+        PcgState* st = B.state;
+        st->iteration += 1;
+        st->rr = res[0];
+        st->error = sqrt(res[0] / st->bb);
+        if (st->error < st->abs_tol || st->error / st->error0 < st->rel_tol) {
+            st->converged = 1;
+            st->done = 1;
+        } else if (st->iteration >= st->max_iterations) {
+            st->converged = 0;
+            st->done = 1;
+        } else {
+            st->beta = res[1] / st->rz;
+            st->rz = res[1];
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_pcg_direction(PcgBuffers<T> B)
+{
+    if (B.state->done) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 3 * (int64_t)B.n_blocks) return;
+    const double beta = B.state->beta;
+    B.p[k] = (T)((double)B.z[k] + beta * (double)B.p[k]);
+}
+
+template <typename T>
+__global__ void k_pcg_init(PcgBuffers<T> B, const double* __restrict__ grad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double bb = 0.0, rz = 0.0;
+    if (i < B.n_blocks) {
+        T r[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double b = -grad[3 * i + d];
+            r[d] = (T)b;
+            B.r[3 * i + d] = r[d];
+            B.x[3 * i + d] = T(0);
+            bb += b * b;
+        }
+        const T* m = B.Dinv + (int64_t)i * 9;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T z = m[3 * d] * r[0] + m[3 * d + 1] * r[1] + m[3 * d + 2] * r[2];
+            B.z[3 * i + d] = z;
+            B.p[3 * i + d] = z;
+            rz += (double)r[d] * (double)z;
+        }
+    }
+    double mine[2] = {bb, rz}, res[2];
+    if (last_block_combine<false, 2>(mine, B.partials, B.tickets + 2, res) && threadIdx.x == 0) {
+        PcgState* st = B.state;
+        st->bb = res[0];
+        st->rz = res[1];
+        st->iteration = 0;
+        st->indefinite = 0;
+        st->converged = 0;
+        st->done = 0;
+        if (res[0] < st->abs_tol * st->abs_tol) {  // zero right-hand side: x = 0
+            st->error = 0.0;
+            st->converged = 1;
+            st->done = 1;
+        } else {
+            st->error0 = 1.0;  // x0 = 0, so r = b exactly: sqrt(r.r / b.b) = 1
+            st->error = 1.0;
+            if (st->error < st->abs_tol) { st->converged = 1; st->done = 1; }
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_axpy_to(int64_t n, const double* __restrict__ x0, double step, const T* __restrict__ du,
+                          double* __restrict__ x)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = x0[i] + step * (double)du[i];
+}
+
+template <typename T>
+__global__ void k_convert(int64_t n, const T* __restrict__ x, double* __restrict__ y)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (double)x[i];
+}
+
+std::atomic<int64_t> g_launches{0};
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+void check_launch(const char* what)
+{
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: launch of ") + what + " failed: " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+int64_t launch_count() { return g_launches.load(); }
+void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+void launch_sum(const double* x, int64_t n, double* partials, unsigned* ticket, double* out, cudaStream_t s)
+{
+    k_sum<<<kReduceBlocks, kReduceThreads, 0, s>>>(x, n, partials, ticket, out);
+    check_launch("sum");
+}
+
+void launch_max_abs(const double* x, int64_t n, double* partials, unsigned* ticket, double* out, cudaStream_t s)
+{
+    k_max_abs<double><<<kReduceBlocks, kReduceThreads, 0, s>>>(x, n, partials, ticket, out);
+    check_launch("max_abs");
+}
+
+template <typename T>
+void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, unsigned* ticket, double* out,
+                      cudaStream_t s)
+{
+    k_dot_mixed<T><<<kReduceBlocks, kReduceThreads, 0, s>>>(a, b, n, partials, ticket, out);
+    check_launch("dot");
+}
+
+template <typename T>
+void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s)
+{
+    if (count <= 0) return;
+    switch (N) {
+        case 3: k_project_pd_unrolled<T, 3><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
+        case 6: k_project_pd_unrolled<T, 6><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
+        case 9: k_project_pd_unrolled<T, 9><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
+        case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
+        default:
+            if (N > 24 || N % 3 != 0) throw std::runtime_error("symx_gb300: projection supports N = 3k <= 24");
+            k_project_pd_generic<T><<<blocks_for(count, 64), 64, 0, s>>>(H, N, count, eps, mirroring, not_converged);
+    }
+    check_launch("project_pd");
+}
+
+template <typename T>
+void launch_assemble_blocks(int64_t nnzb, const int64_t* slot_ptr, const int32_t* contrib, const T* blocks, T* vals,
+                            cudaStream_t s)
+{
+    if (nnzb <= 0) return;
+    k_assemble_blocks<T><<<blocks_for(nnzb, 256), 256, 0, s>>>(nnzb, slot_ptr, contrib, blocks, vals);
+    check_launch("assemble");
+}
+
+void launch_gather_gradient(int n_blocks, const int64_t* ptr, const int32_t* contrib, const double* gel, double* g,
+                            cudaStream_t s)
+{
+    k_gather_gradient<<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, ptr, contrib, gel, g);
+    check_launch("gather_gradient");
+}
+
+template <typename T>
+void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, T* Dinv, cudaStream_t s)
+{
+    k_block_jacobi_setup<T><<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, diag_slot, vals, Dinv);
+    check_launch("block_jacobi_setup");
+}
+
+template <typename T>
+void launch_pcg_init(const PcgBuffers<T>& B, const double* grad, cudaStream_t s)
+{
+    const unsigned g = blocks_for(B.n_blocks, 256);
+    if (g > (unsigned)kPcgMaxPartials) throw std::runtime_error("symx_gb300: system too large for the PCG partials");
+    k_pcg_init<T><<<g, 256, 0, s>>>(B, grad);
+    check_launch("pcg_init");
+}
+
+template <typename T>
+void launch_pcg_iteration(const PcgBuffers<T>& B, cudaStream_t s)
+{
+    const unsigned gs = blocks_for((int64_t)B.n_blocks * 16, kSpmvThreads);
+    k_pcg_spmv<T><<<gs, kSpmvThreads, 0, s>>>(B);
+    k_pcg_update<T><<<blocks_for(B.n_blocks, 256), 256, 0, s>>>(B);
+    k_pcg_direction<T><<<blocks_for(3 * (int64_t)B.n_blocks, 256), 256, 0, s>>>(B);
+    count_launch(2);
+    check_launch("pcg_iteration");
+}
+
+template <typename T>
+void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, const T* x, T* y,
+                      cudaStream_t s)
+{
+    k_bcsr_spmv<T><<<blocks_for((int64_t)n_blocks * 16, kSpmvThreads), kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols,
+                                                                                           vals, x, y);
+    check_launch("bcsr_spmv");
+}
+
+template <typename T>
+void launch_axpy_to(int64_t n, const double* x0, double step, const T* du, double* x_out, cudaStream_t s)
+{
+    k_axpy_to<T><<<blocks_for(n, 256), 256, 0, s>>>(n, x0, step, du, x_out);
+    check_launch("axpy");
+}
+
+template <typename T>
+void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
+{
+    k_convert<T><<<blocks_for(n, 256), 256, 0, s>>>(n, x, y);
+    check_launch("convert");
+}
+
+#define SYMXG_INSTANTIATE(T)                                                                                          \
+    template void launch_dot_mixed<T>(const T*, const double*, int64_t, double*, unsigned*, double*, cudaStream_t);  \
+    template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t);                                 \
+    template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, cudaStream_t);      \
+    template void launch_block_jacobi_setup<T>(int, const int32_t*, const T*, T*, cudaStream_t);                       \
+    template void launch_pcg_init<T>(const PcgBuffers<T>&, const double*, cudaStream_t);                               \
+    template void launch_pcg_iteration<T>(const PcgBuffers<T>&, cudaStream_t);                                        \
+    template void launch_bcsr_spmv<T>(int, const int32_t*, const int32_t*, const T*, const T*, T*, cudaStream_t);      \
+    template void launch_axpy_to<T>(int64_t, const double*, double, const T*, double*, cudaStream_t);                  \
+    template void launch_convert_to_double<T>(int64_t, const T*, double*, cudaStream_t);
+SYMXG_INSTANTIATE(float)
+SYMXG_INSTANTIATE(double)
+
+}  // namespace symxg

@@ -1,0 +1,105 @@
+// Host-side launchers of the hand-written device kernels of the solve path.
+// All launches are asynchronous on the given stream; no launcher allocates.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace symxg {
+
+// Number of kernels launched by this library since load (all handles, all streams).
+int64_t launch_count();
+void count_launch(int64_t n = 1);
+
+// Device-resident state of one PCG solve (read by the host between chunks of iterations).
+struct PcgState {
+    double bb;        // b.b
+    double rz;        // r.z of the current iterate
+    double pAp;
+    double rr;
+    double alpha, beta;
+    double error, error0;
+    double abs_tol, rel_tol;
+    int iteration;
+    int max_iterations;
+    int done;         // 1 once converged, failed or out of iterations
+    int converged;
+    int indefinite;
+    int pad;
+};
+
+// Deterministic reductions: each launch uses a fixed grid, every block sums a fixed
+// contiguous range, and the last block to finish combines the block partials in index
+// order.  `partials` holds kReduceBlocks doubles, `ticket` one unsigned int (zeroed).
+constexpr int kReduceBlocks = 304;  // 2 x 152 SMs
+constexpr int kReduceThreads = 256;
+
+// out[0] = sum(x[0..n))
+void launch_sum(const double* x, int64_t n, double* partials, unsigned* ticket, double* out, cudaStream_t s);
+// out[0] = max |x[i]|
+void launch_max_abs(const double* x, int64_t n, double* partials, unsigned* ticket, double* out, cudaStream_t s);
+// out[0] = sum a[i]*b[i] with a in T, b in double
+template <typename T>
+void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, unsigned* ticket, double* out,
+                      cudaStream_t s);
+
+// Element-Hessian projection, in place, block-major storage, `count` matrices of N x N.
+// not_converged: one int, set to 1 if any matrix hit the sweep cap.
+template <typename T>
+void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s);
+
+// Assembly: vals[s] = sum over c in [slot_ptr[s], slot_ptr[s+1]) of blocks[contrib[c]],
+// in that fixed order (3x3 blocks, 9 values each).
+template <typename T>
+void launch_assemble_blocks(int64_t nnzb, const int64_t* slot_ptr, const int32_t* contrib, const T* blocks, T* vals,
+                            cudaStream_t s);
+// Gradient: g[3v+d] = sum over c in [ptr[v], ptr[v+1]) of gel[3*contrib[c]+d].
+void launch_gather_gradient(int n_blocks, const int64_t* ptr, const int32_t* contrib, const double* gel, double* g,
+                            cudaStream_t s);
+
+// Block-Jacobi: Dinv[r] = inverse of the diagonal block vals[diag_slot[r]] (computed in
+// double, stored as T).
+template <typename T>
+void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, T* Dinv, cudaStream_t s);
+
+// PCG over a 3x3-block CSR matrix (row_ptr/cols/vals), block-Jacobi preconditioner.
+// Vectors in T, dot products accumulated in double, scalars in `state`.
+template <typename T>
+struct PcgBuffers {
+    int n_blocks;
+    const int32_t* row_ptr;
+    const int32_t* cols;
+    const T* vals;
+    const T* Dinv;
+    T* x;
+    T* r;
+    T* z;
+    T* p;
+    T* q;
+    double* partials;   // kPcgPartials doubles x 2
+    unsigned* tickets;  // 4 counters
+    PcgState* state;
+};
+constexpr int kPcgMaxPartials = 1 << 16;
+
+// Set x = 0, r = b (b = -grad converted to T), z = M^-1 r, p = z, bb, rz, error0.
+template <typename T>
+void launch_pcg_init(const PcgBuffers<T>& B, const double* neg_rhs_source, cudaStream_t s);
+// One PCG iteration (SpMV + p.Ap, update + dots, direction update), each a no-op once
+// state->done is set.
+template <typename T>
+void launch_pcg_iteration(const PcgBuffers<T>& B, cudaStream_t s);
+
+// y = A x over a 3x3-block CSR matrix (standalone SpMV, used by tests and benchmarks).
+template <typename T>
+void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, const T* x, T* y,
+                      cudaStream_t s);
+
+// x_out = x0 + step * du (du in T, x in double)
+template <typename T>
+void launch_axpy_to(int64_t n, const double* x0, double step, const T* du, double* x_out, cudaStream_t s);
+// y = (double) x
+template <typename T>
+void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s);
+
+}  // namespace symxg

@@ -1,0 +1,891 @@
+// Projected Newton's method on one GPU.  See newton.h.
+//
+// Reference control flow followed here: symx/src/solver/NewtonsMethod.cpp
+//   solve loop :28-252, projection + assembly :254-352, BDPCG with forcing term :388-452,
+//   line search (cap, max step, Armijo) :459-641.
+#include "newton.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+#include <stdexcept>
+#include <unordered_map>
+
+#include <cuda_runtime.h>
+
+#include "codegen.h"
+#include "cuda_module.h"
+#include "kernels.cuh"
+
+namespace symx {
+
+using symxg::CudaModule;
+using symxg::PcgBuffers;
+using symxg::PcgState;
+
+namespace {
+
+void ck(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: ") + what + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    ~DevBuf() { release(); }
+    void alloc(size_t count)
+    {
+        if (count == n && p) return;
+        release();
+        if (count) ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct StageTimer {
+    struct Rec { std::string label; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    cudaStream_t s = nullptr;
+    std::string open_label;
+    cudaEvent_t open_a = nullptr;
+    void start(const std::string& label)
+    {
+        cudaEvent_t a;
+        cudaEventCreate(&a);
+        cudaEventRecord(a, s);
+        open_label = label;
+        open_a = a;
+    }
+    void stop()
+    {
+        cudaEvent_t b;
+        cudaEventCreate(&b);
+        cudaEventRecord(b, s);
+        recs.push_back({open_label, open_a, b});
+        open_a = nullptr;
+    }
+    void flush(std::map<std::string, double>& out)
+    {
+        for (auto& r : recs) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, r.a, r.b);
+            out[r.label] += ms * 1e-3;
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        recs.clear();
+    }
+};
+
+struct UploadedArray {
+    std::uintptr_t id = 0;
+    const double* host = nullptr;
+    int64_t n = 0;
+    DevBuf<double> dev;
+};
+
+struct CompiledPotential {
+    std::string name;
+    const Potential* pot = nullptr;
+    int nb = 0;                    // DoF blocks per element
+    std::vector<int> dof_set;      // per block: DoF set index
+    std::vector<int> dof_col;      // per block: connectivity column
+    std::vector<int> map_upload;   // per map: index into uploaded arrays, or -1-dofset for DoF maps
+    int64_t n_elements = 0;
+    int conn_stride = 0;
+    std::shared_ptr<CudaModule> module;
+    std::string source;
+    OpCount ops_eg, ops_h, ops_e;
+    DevBuf<int32_t> conn;
+    DevBuf<const double*> map_ptrs;
+    int64_t e_off = 0, g_off = 0, h_off = 0;  // offsets: elements, gradient blocks, Hessian blocks
+};
+
+std::string build_source(const CompiledPotential& cp, const Expressions& g, const std::vector<int32_t>& eg,
+                         const std::vector<int32_t>& h_bm, const std::vector<int32_t>& e_only, int32_t cond,
+                         const Summation& sum, OpCount* oeg, OpCount* oh, OpCount* oe)
+{
+    const MappedWorkspace<double>& mws = *cp.pot->mws;
+    const int NS = g.n_symbols();
+    const int NG = (int)eg.size() - 1;
+    const int NH = (int)h_bm.size();
+    const int NQ = std::max(1, sum.n_iterations);
+    const bool acc = sum.n_iterations > 1;
+    std::ostringstream s;
+    s << "// generated element kernels for potential '" << cp.name << "'\n";
+    s << codegen_prelude();
+    s << emit_device_function(g, eg, "symxg_eval_eg", "double", acc, oeg);
+    s << emit_device_function(g, h_bm, "symxg_eval_h_f64", "double", acc, oh);
+    s << emit_device_function(g, h_bm, "symxg_eval_h_f32", "float", acc, nullptr);
+    s << emit_device_function(g, e_only, "symxg_eval_e", "double", acc, oe);
+    if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond", "double", false, nullptr);
+    if (sum.n_iterations > 0) {
+        s << "static __device__ const double symxg_sum_data[" << sum.data.size() << "] = {";
+        for (size_t i = 0; i < sum.data.size(); ++i) s << (i ? ", " : "") << double_literal(sum.data[i]);
+        s << "};\n";
+    }
+    // gather of all bound data for element e
+    s << "__device__ __forceinline__ void symxg_gather(long long e, const int* __restrict__ conn, "
+         "const double* const* __restrict__ maps, double* in)\n{\n";
+    s << "    const int* __restrict__ ce = conn + e * " << cp.conn_stride << "LL;\n";
+    for (size_t k = 0; k < mws.maps.size(); ++k) {
+        const DataMap& m = mws.maps[k];
+        s << "    { const double* __restrict__ m = maps[" << k << "]";
+        if (m.conn_column >= 0) s << " + (long long)ce[" << m.conn_column << "] * " << m.stride << "LL";
+        s << ";";
+        for (int j = 0; j < m.stride; ++j) s << " in[" << (m.first_symbol + j) << "] = m[" << j << "];";
+        s << " }\n";
+    }
+    s << "}\n";
+    auto set_sum = [&](const std::string& q) {
+        std::ostringstream t;
+        for (int j = 0; j < sum.stride; ++j)
+            t << "        in[" << (sum.first_symbol + j) << "] = symxg_sum_data[" << q << " * " << sum.stride << " + " << j
+              << "];\n";
+        return t.str();
+    };
+    auto cond_check = [&](const std::string& zero_writes) {
+        if (cond < 0) return std::string();
+        std::ostringstream t;
+        t << "    { double c[1]; symxg_eval_cond(in, c); if (!(c[0] > 0.0)) {\n" << zero_writes << "        return; } }\n";
+        return t.str();
+    };
+    // E + g + H kernels, H in double or float
+    for (int prec = 0; prec < 2; ++prec) {
+        const std::string TH = prec == 0 ? "double" : "float";
+        const std::string kname = prec == 0 ? "symxg_egh_f64" : "symxg_egh_f32";
+        s << "extern \"C\" __global__ void __launch_bounds__(128) " << kname
+          << "(long long n, const int* __restrict__ conn, const double* const* __restrict__ maps, "
+             "double* __restrict__ E, double* __restrict__ G, "
+          << TH << "* __restrict__ H)\n{\n";
+        s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
+        s << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
+        std::ostringstream zw;
+        zw << "        E[e] = 0.0;\n        for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = 0.0;\n"
+           << "        for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = (" << TH << ")0;\n";
+        if (sum.n_iterations > 0) s << set_sum("0");
+        s << cond_check(zw.str());
+        s << "    double eg[" << (NG + 1) << "];\n    " << TH << " h[" << NH << "];\n";
+        if (acc) {
+            s << "    for (int i = 0; i < " << NG + 1 << "; ++i) eg[i] = 0.0;\n";
+            s << "    for (int i = 0; i < " << NH << "; ++i) h[i] = (" << TH << ")0;\n";
+            s << "    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q");
+        } else {
+            s << "    {\n";
+        }
+        s << "        symxg_eval_eg(in, eg);\n";
+        if (prec == 0) {
+            s << "        symxg_eval_h_f64(in, h);\n";
+        } else {
+            s << "        float inf32[" << NS << "];\n        for (int i = 0; i < " << NS << "; ++i) inf32[i] = (float)in[i];\n";
+            s << "        symxg_eval_h_f32(inf32, h);\n";
+        }
+        s << "    }\n";
+        s << "    E[e] = eg[0];\n    for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = eg[1 + i];\n";
+        s << "    for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = h[i];\n}\n";
+    }
+    // energy-only kernel (line search)
+    s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_e(long long n, const int* __restrict__ conn, "
+         "const double* const* __restrict__ maps, double* __restrict__ E)\n{\n";
+    s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
+    s << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
+    if (sum.n_iterations > 0) s << set_sum("0");
+    s << cond_check("        E[e] = 0.0;\n");
+    s << "    double ev[1];\n";
+    if (acc) s << "    ev[0] = 0.0;\n    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q");
+    else s << "    {\n";
+    s << "        symxg_eval_e(in, ev);\n    }\n    E[e] = ev[0];\n}\n";
+    return s.str();
+}
+
+// DoF symbols of a potential, its derivatives and the generated CUDA source.
+CompiledPotential prepare_potential(const Potential& pot, const GlobalPotential& GP)
+{
+    CompiledPotential cp;
+    cp.name = pot.name;
+    cp.pot = &pot;
+    MappedWorkspace<double>& mws = *pot.mws;
+    Expressions& g = mws.ws.get_expression_graph();
+    std::vector<Scalar> wrt;
+    for (size_t k = 0; k < mws.maps.size(); ++k) {
+        const DataMap& m = mws.maps[k];
+        int set = -1;
+        for (size_t s = 0; s < GP.dofs.size(); ++s)
+            if (GP.dofs[s].id == m.id) set = (int)s;
+        if (set < 0) continue;
+        if (m.stride != 3 || m.conn_column < 0)
+            throw std::runtime_error("symx: DoF data of potential '" + pot.name +
+                                     "' must be bound per item with 3 values (make_vector(s) with an index)");
+        cp.dof_set.push_back(set);
+        cp.dof_col.push_back(m.conn_column);
+        for (int j = 0; j < 3; ++j) wrt.push_back(Scalar(g.symbol_node(m.first_symbol + j), &g));
+    }
+    cp.nb = (int)cp.dof_set.size();
+    if (cp.nb == 0) throw std::runtime_error("symx: potential '" + pot.name + "' depends on no DoF");
+    if (cp.nb > 8) throw std::runtime_error("symx_gb300: at most 8 DoF blocks per element (24x24 Hessians)");
+    cp.conn_stride = mws.conn.stride;
+    DiffCache cache;
+    Vector grad = gradient(pot.expression, wrt, cache);
+    Matrix hess = gradient(grad, wrt, true, cache);
+    std::vector<int32_t> eg{pot.expression.expr_id};
+    for (const Scalar& s : grad.values()) eg.push_back(s.expr_id);
+    const int n = 3 * cp.nb;
+    std::vector<int32_t> h_bm(n * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            h_bm[(((i / 3) * cp.nb + (j / 3)) * 3 + (i % 3)) * 3 + (j % 3)] = hess(i, j).expr_id;
+    const int32_t cond = pot.has_condition ? pot.condition.expr_id : -1;
+    cp.source = build_source(cp, g, eg, h_bm, {pot.expression.expr_id}, cond, mws.summation, &cp.ops_eg, &cp.ops_h,
+                             &cp.ops_e);
+    return cp;
+}
+
+}  // namespace
+
+struct SolverImpl {
+    cudaStream_t stream = nullptr;
+    std::vector<CompiledPotential> pots;
+    std::vector<UploadedArray> arrays;
+    int n_dofs = 0, n_blocks = 0;
+    std::vector<int> dof_offsets;  // doubles, per DoF set (+ total)
+
+    DevBuf<double> x, x_before, grad;
+    DevBuf<double> E_el, g_el;
+    DevBuf<float> H32;
+    DevBuf<double> H64;
+    int64_t n_elements_total = 0, n_gblocks = 0, n_hblocks = 0;
+
+    DevBuf<int32_t> row_ptr, cols, diag_slot, contrib, gcontrib;
+    DevBuf<int64_t> slot_ptr, gptr;
+    int64_t nnzb = 0;
+    DevBuf<float> vals32, Dinv32;
+    DevBuf<double> vals64, Dinv64;
+    DevBuf<float> v32[5];
+    DevBuf<double> v64[5];
+    DevBuf<double> partials, scalars;
+    DevBuf<unsigned> tickets;
+    DevBuf<PcgState> pcg_state;
+    DevBuf<int> flags;
+    double* h_scalars = nullptr;
+    PcgState* h_state = nullptr;
+    Precision allocated_precision = Precision::FP64;
+    bool precision_allocated[2] = {false, false};
+
+    ~SolverImpl()
+    {
+        if (h_scalars) cudaFreeHost(h_scalars);
+        if (h_state) cudaFreeHost(h_state);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void ensure_precision(Precision p)
+    {
+        const int k = (int)p;
+        if (precision_allocated[k]) return;
+        const size_t n = 3 * (size_t)n_blocks;
+        if (p == Precision::Mixed) {
+            H32.alloc((size_t)n_hblocks * 9);
+            vals32.alloc((size_t)nnzb * 9);
+            Dinv32.alloc((size_t)n_blocks * 9);
+            for (auto& v : v32) v.alloc(n);
+        } else {
+            H64.alloc((size_t)n_hblocks * 9);
+            vals64.alloc((size_t)nnzb * 9);
+            Dinv64.alloc((size_t)n_blocks * 9);
+            for (auto& v : v64) v.alloc(n);
+        }
+        precision_allocated[k] = true;
+    }
+
+    template <typename T> T* Hbuf();
+    template <typename T> T* vals();
+    template <typename T> T* Dinv();
+    template <typename T> DevBuf<T>* vecs();
+
+    void read_scalars(int count)
+    {
+        ck(cudaMemcpyAsync(h_scalars, scalars.p, sizeof(double) * count, cudaMemcpyDeviceToHost, stream), "copy scalars");
+        ck(cudaStreamSynchronize(stream), "synchronize");
+    }
+
+    void launch_eval(int mode /*0 f64 H, 1 f32 H, 2 energy only*/)
+    {
+        for (auto& cp : pots) {
+            if (cp.n_elements == 0) continue;
+            long long n = cp.n_elements;
+            const int32_t* conn = cp.conn.p;
+            const double* const* maps = cp.map_ptrs.p;
+            double* E = E_el.p + cp.e_off;
+            const unsigned grid = (unsigned)((n + 127) / 128);
+            if (mode == 2) {
+                void* args[] = {&n, &conn, &maps, &E};
+                cp.module->launch("symxg_e", dim3(grid), dim3(128), 0, stream, args);
+            } else {
+                double* G = g_el.p + cp.g_off * 3;
+                void* H = mode == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
+                void* args[] = {&n, &conn, &maps, &E, &G, &H};
+                cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_f32", dim3(grid), dim3(128), 0, stream, args);
+            }
+        }
+    }
+};
+
+template <> float* SolverImpl::Hbuf<float>() { return H32.p; }
+template <> double* SolverImpl::Hbuf<double>() { return H64.p; }
+template <> float* SolverImpl::vals<float>() { return vals32.p; }
+template <> double* SolverImpl::vals<double>() { return vals64.p; }
+template <> float* SolverImpl::Dinv<float>() { return Dinv32.p; }
+template <> double* SolverImpl::Dinv<double>() { return Dinv64.p; }
+template <> DevBuf<float>* SolverImpl::vecs<float>() { return v32; }
+template <> DevBuf<double>* SolverImpl::vecs<double>() { return v64; }
+
+std::vector<std::string> generate_element_kernel_sources(const GlobalPotential& GP)
+{
+    std::vector<std::string> out;
+    for (const Potential& pot : GP.potentials) out.push_back(prepare_potential(pot, GP).source);
+    return out;
+}
+
+std::string to_string(SolverReturn r)
+{
+    switch (r) {
+        case SolverReturn::Successful: return "Successful";
+        case SolverReturn::Running: return "Running";
+        case SolverReturn::InvalidInitialState: return "InvalidInitialState";
+        case SolverReturn::TooManyIterations: return "TooManyIterations";
+        case SolverReturn::TooManyArmijoIterations: return "TooManyArmijoIterations";
+        case SolverReturn::LinearSystemSolveFailure: return "LinearSystemSolveFailure";
+        case SolverReturn::TooManyInvalidIntermediateIterations: return "TooManyInvalidIntermediateIterations";
+        case SolverReturn::StepDoesNotDescend: return "StepDoesNotDescend";
+        default: return "InvalidConvergedState";
+    }
+}
+
+NewtonsMethod::~NewtonsMethod() = default;
+
+NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
+    : global_potential(std::move(G)), context(ctx ? std::move(ctx) : Context::create()), impl(new SolverImpl())
+{
+    SolverImpl& I = *impl;
+    GlobalPotential& GP = *global_potential;
+    if (GP.dofs.empty()) throw std::runtime_error("symx: no degrees of freedom registered (add_dof)");
+    I.dof_offsets = GP.get_dofs_offsets();
+    I.n_dofs = I.dof_offsets.back();
+    if (I.n_dofs <= 0 || I.n_dofs % 3 != 0) throw std::runtime_error("symx: number of DoFs must be a positive multiple of 3");
+    I.n_blocks = I.n_dofs / 3;
+    const std::string cache_dir =
+        context->compilation_directory.empty() ? symxg::default_cache_dir() : context->compilation_directory;
+
+    // ---- per potential: DoF symbols, differentiation, code generation, compilation
+    for (const Potential& pot : GP.potentials) {
+        CompiledPotential cp = prepare_potential(pot, GP);
+        symxg::CompileInfo info;
+        cp.module = CudaModule::build(cp.source, cache_dir, {}, &info);
+        if (context->verbosity > 0)
+            std::printf("symx_gb300: potential '%s' %s in %.2f s (E+g %lld ops, H %lld ops)\n", cp.name.c_str(),
+                        info.cached ? "loaded" : "compiled", info.seconds, (long long)cp.ops_eg.total(),
+                        (long long)cp.ops_h.total());
+        I.pots.push_back(std::move(cp));
+    }
+    ck(cudaStreamCreateWithFlags(&I.stream, cudaStreamNonBlocking), "stream");
+
+    // ---- topology: element blocks -> BCSR slots (fixed order), gradient gather map
+    std::vector<int64_t> set_block_off;
+    for (size_t s = 0; s < GP.dofs.size(); ++s) set_block_off.push_back(I.dof_offsets[s] / 3);
+    int64_t e_off = 0, g_off = 0, h_off = 0;
+    for (auto& cp : I.pots) {
+        cp.n_elements = cp.pot->mws->conn.n_elements();
+        cp.e_off = e_off;
+        cp.g_off = g_off;
+        cp.h_off = h_off;
+        e_off += cp.n_elements;
+        g_off += cp.n_elements * cp.nb;
+        h_off += cp.n_elements * cp.nb * cp.nb;
+    }
+    I.n_elements_total = e_off;
+    I.n_gblocks = g_off;
+    I.n_hblocks = h_off;
+    if (h_off > (int64_t)INT32_MAX) throw std::runtime_error("symx_gb300: more than 2^31 element Hessian blocks");
+
+    auto row_of = [&](const CompiledPotential& cp, const int32_t* conn, int64_t e, int a) -> int64_t {
+        const int32_t v = conn[e * cp.conn_stride + cp.dof_col[a]];
+        const int set = cp.dof_set[a];
+        const int64_t n_items = GP.dofs[set].n_dofs() / 3;
+        if (v < 0 || v >= n_items)
+            throw std::runtime_error("symx: potential '" + cp.name + "' references DoF item " + std::to_string(v) +
+                                     " out of range");
+        return set_block_off[set] + v;
+    };
+    const int nbk = I.n_blocks;
+    std::vector<int64_t> cnt(nbk + 1, 0);
+    for (auto& cp : I.pots) {
+        const int32_t* conn = cp.pot->mws->conn.data();
+        for (int64_t e = 0; e < cp.n_elements; ++e)
+            for (int a = 0; a < cp.nb; ++a) cnt[row_of(cp, conn, e, a) + 1] += cp.nb;
+    }
+    for (int r = 0; r < nbk; ++r) cnt[r + 1] += cnt[r] + 1;  // +1: the diagonal block always exists
+    std::vector<int32_t> raw(cnt[nbk]);
+    {
+        std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+        for (int r = 0; r < nbk; ++r) raw[fill[r]++] = r;
+        for (auto& cp : I.pots) {
+            const int32_t* conn = cp.pot->mws->conn.data();
+            for (int64_t e = 0; e < cp.n_elements; ++e) {
+                int64_t rows[64];
+                for (int a = 0; a < cp.nb; ++a) rows[a] = row_of(cp, conn, e, a);
+                for (int a = 0; a < cp.nb; ++a)
+                    for (int b = 0; b < cp.nb; ++b) raw[fill[rows[a]]++] = (int32_t)rows[b];
+            }
+        }
+    }
+    std::vector<int32_t> row_ptr(nbk + 1, 0), cols;
+    cols.reserve(raw.size() / 4);
+    for (int r = 0; r < nbk; ++r) {
+        auto b = raw.begin() + cnt[r], e = raw.begin() + cnt[r + 1];
+        std::sort(b, e);
+        auto u = std::unique(b, e);
+        cols.insert(cols.end(), b, u);
+        row_ptr[r + 1] = (int32_t)cols.size();
+    }
+    std::vector<int32_t>().swap(raw);
+    I.nnzb = (int64_t)cols.size();
+    auto slot_of = [&](int64_t r, int64_t c) -> int64_t {
+        auto b = cols.begin() + row_ptr[r], e = cols.begin() + row_ptr[r + 1];
+        return std::lower_bound(b, e, (int32_t)c) - cols.begin();
+    };
+    std::vector<int32_t> diag(nbk);
+    for (int r = 0; r < nbk; ++r) diag[r] = (int32_t)slot_of(r, r);
+    // contributions per slot, in (potential, element, a, b) order
+    std::vector<int64_t> sptr(I.nnzb + 1, 0);
+    std::vector<int32_t> slot_of_contrib(I.n_hblocks);
+    std::vector<int64_t> gcnt(nbk + 1, 0);
+    for (auto& cp : I.pots) {
+        const int32_t* conn = cp.pot->mws->conn.data();
+        for (int64_t e = 0; e < cp.n_elements; ++e) {
+            int64_t rows[64];
+            for (int a = 0; a < cp.nb; ++a) rows[a] = row_of(cp, conn, e, a);
+            for (int a = 0; a < cp.nb; ++a) {
+                gcnt[rows[a] + 1]++;
+                for (int b = 0; b < cp.nb; ++b) {
+                    const int64_t s = slot_of(rows[a], rows[b]);
+                    slot_of_contrib[cp.h_off + (e * cp.nb + a) * cp.nb + b] = (int32_t)s;
+                    sptr[s + 1]++;
+                }
+            }
+        }
+    }
+    for (int64_t s = 0; s < I.nnzb; ++s) sptr[s + 1] += sptr[s];
+    for (int r = 0; r < nbk; ++r) gcnt[r + 1] += gcnt[r];
+    std::vector<int32_t> contrib(I.n_hblocks), gcontrib(I.n_gblocks);
+    {
+        std::vector<int64_t> fill(sptr.begin(), sptr.end() - 1);
+        for (int64_t k = 0; k < I.n_hblocks; ++k) contrib[fill[slot_of_contrib[k]]++] = (int32_t)k;
+        std::vector<int64_t> gfill(gcnt.begin(), gcnt.end() - 1);
+        for (auto& cp : I.pots) {
+            const int32_t* conn = cp.pot->mws->conn.data();
+            for (int64_t e = 0; e < cp.n_elements; ++e)
+                for (int a = 0; a < cp.nb; ++a)
+                    gcontrib[gfill[row_of(cp, conn, e, a)]++] = (int32_t)(cp.g_off + e * cp.nb + a);
+        }
+    }
+
+    // ---- device buffers
+    auto up = [&](auto& buf, const auto& host) {
+        using T = typename std::decay<decltype(host[0])>::type;
+        buf.alloc(host.size());
+        if (!host.empty()) ck(cudaMemcpy(buf.p, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice), "upload");
+    };
+    up(I.row_ptr, row_ptr);
+    up(I.cols, cols);
+    up(I.diag_slot, diag);
+    up(I.slot_ptr, sptr);
+    up(I.contrib, contrib);
+    up(I.gptr, gcnt);
+    up(I.gcontrib, gcontrib);
+    I.x.alloc(I.n_dofs);
+    I.x_before.alloc(I.n_dofs);
+    I.grad.alloc(I.n_dofs);
+    I.E_el.alloc(std::max<int64_t>(1, I.n_elements_total));
+    I.g_el.alloc(std::max<int64_t>(1, I.n_gblocks * 3));
+    I.partials.alloc(2 * symxg::kPcgMaxPartials);
+    I.scalars.alloc(16);
+    I.tickets.alloc(8);
+    ck(cudaMemset(I.tickets.p, 0, sizeof(unsigned) * 8), "memset");
+    I.pcg_state.alloc(1);
+    I.flags.alloc(4);
+    ck(cudaMallocHost(&I.h_scalars, sizeof(double) * 16), "pinned");
+    ck(cudaMallocHost(&I.h_state, sizeof(PcgState)), "pinned");
+    for (auto& cp : I.pots) {
+        const int32_t* conn = cp.pot->mws->conn.data();
+        cp.conn.alloc((size_t)cp.n_elements * cp.conn_stride);
+        if (cp.conn.n)
+            ck(cudaMemcpy(cp.conn.p, conn, sizeof(int32_t) * cp.conn.n, cudaMemcpyHostToDevice), "upload connectivity");
+        cp.map_ptrs.alloc(cp.pot->mws->maps.size());
+        cp.pot->mws->verify_no_out_of_bounds();
+    }
+}
+
+int NewtonsMethod::n_dof_blocks() const { return impl->n_blocks; }
+int64_t NewtonsMethod::n_hessian_blocks() const { return impl->nnzb; }
+double* NewtonsMethod::device_dofs() { return impl->x.p; }
+std::array<int64_t, 3> NewtonsMethod::op_counts(int p) const
+{
+    const auto& cp = impl->pots.at(p);
+    return {cp.ops_eg.total(), cp.ops_h.total(), cp.ops_e.total()};
+}
+std::string NewtonsMethod::generated_source(int p) const { return impl->pots.at(p).source; }
+
+void NewtonsMethod::upload()
+{
+    SolverImpl& I = *impl;
+    GlobalPotential& GP = *global_potential;
+    int64_t bytes = sizeof(double) * (int64_t)I.n_dofs;
+    // DoFs
+    for (size_t s = 0; s < GP.dofs.size(); ++s)
+        ck(cudaMemcpyAsync(I.x.p + I.dof_offsets[s], GP.dofs[s].data(), sizeof(double) * GP.dofs[s].n_dofs(),
+                           cudaMemcpyHostToDevice, I.stream),
+           "upload dofs");
+    // every other bound array, de-duplicated by container and pointer
+    for (auto& cp : I.pots) {
+        const auto& maps = cp.pot->mws->maps;
+        std::vector<const double*> ptrs(maps.size());
+        for (size_t k = 0; k < maps.size(); ++k) {
+            const DataMap& m = maps[k];
+            int set = -1;
+            for (size_t s = 0; s < GP.dofs.size(); ++s)
+                if (GP.dofs[s].id == m.id) set = (int)s;
+            if (set >= 0) {
+                ptrs[k] = I.x.p + I.dof_offsets[set];
+                continue;
+            }
+            const double* host = m.data();
+            const int64_t items = m.n_items();
+            const int64_t n = items < 0 ? m.stride : items * m.stride;
+            UploadedArray* ua = nullptr;
+            for (auto& a : I.arrays)
+                if (a.id == m.id && a.host == host && a.n == n) ua = &a;
+            if (!ua) {
+                I.arrays.emplace_back();
+                ua = &I.arrays.back();
+                ua->id = m.id;
+                ua->host = host;
+                ua->n = n;
+                ua->dev.alloc((size_t)n);
+            }
+            ptrs[k] = ua->dev.p;
+        }
+        // arrays are re-read on every upload: the user may change them between solves
+        ck(cudaMemcpyAsync(cp.map_ptrs.p, ptrs.data(), sizeof(double*) * ptrs.size(), cudaMemcpyHostToDevice, I.stream),
+           "upload map pointers");
+        bytes += (int64_t)(sizeof(double*) * ptrs.size());
+        ck(cudaStreamSynchronize(I.stream), "synchronize");
+    }
+    for (auto& a : I.arrays) {
+        ck(cudaMemcpyAsync(a.dev.p, a.host, sizeof(double) * a.n, cudaMemcpyHostToDevice, I.stream), "upload data");
+        bytes += (int64_t)sizeof(double) * a.n;
+    }
+    ck(cudaStreamSynchronize(I.stream), "synchronize");
+    h2d_bytes_ = bytes;
+}
+
+void NewtonsMethod::download()
+{
+    SolverImpl& I = *impl;
+    GlobalPotential& GP = *global_potential;
+    for (size_t s = 0; s < GP.dofs.size(); ++s)
+        ck(cudaMemcpyAsync(GP.dofs[s].data(), I.x.p + I.dof_offsets[s], sizeof(double) * GP.dofs[s].n_dofs(),
+                           cudaMemcpyDeviceToHost, I.stream),
+           "download dofs");
+    ck(cudaStreamSynchronize(I.stream), "synchronize");
+    d2h_bytes_ = sizeof(double) * (int64_t)I.n_dofs;
+}
+
+SolverReturn NewtonsMethod::solve()
+{
+    upload();
+    const SolverReturn r = solve_device();
+    download();
+    stats.d2h_bytes = d2h_bytes_;
+    return r;
+}
+
+double NewtonsMethod::evaluate_energy()
+{
+    SolverImpl& I = *impl;
+    I.launch_eval(2);
+    symxg::launch_sum(I.E_el.p, I.n_elements_total, I.partials.p, I.tickets.p + 4, I.scalars.p, I.stream);
+    I.read_scalars(1);
+    return I.h_scalars[0];
+}
+
+double NewtonsMethod::evaluate(double* grad_host)
+{
+    SolverImpl& I = *impl;
+    I.ensure_precision(Precision::FP64);
+    I.launch_eval(0);
+    symxg::launch_sum(I.E_el.p, I.n_elements_total, I.partials.p, I.tickets.p + 4, I.scalars.p, I.stream);
+    symxg::launch_gather_gradient(I.n_blocks, I.gptr.p, I.gcontrib.p, I.g_el.p, I.grad.p, I.stream);
+    I.read_scalars(1);
+    if (grad_host)
+        ck(cudaMemcpy(grad_host, I.grad.p, sizeof(double) * I.n_dofs, cudaMemcpyDeviceToHost), "download gradient");
+    return I.h_scalars[0];
+}
+
+namespace {
+template <typename T>
+void assemble_t(SolverImpl& I, bool project, const NewtonSettings& s, int mode)
+{
+    I.ensure_precision(std::is_same<T, float>::value ? Precision::Mixed : Precision::FP64);
+    I.launch_eval(mode);
+    if (project) {
+        ck(cudaMemsetAsync(I.flags.p, 0, sizeof(int), I.stream), "memset");
+        for (auto& cp : I.pots)
+            symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)s.projection_eps,
+                                        s.project_to_pd_use_mirroring, I.flags.p, I.stream);
+    }
+    symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.stream);
+}
+}  // namespace
+
+void NewtonsMethod::assembled_hessian(bool project, int32_t* n_blocks, int64_t* nnzb, int32_t* row_ptr, int32_t* cols,
+                                      double* vals)
+{
+    SolverImpl& I = *impl;
+    *n_blocks = I.n_blocks;
+    *nnzb = I.nnzb;
+    if (!vals) return;
+    if (settings.precision == Precision::Mixed) {
+        assemble_t<float>(I, project, settings, 1);
+        DevBuf<double> tmp;
+        tmp.alloc((size_t)I.nnzb * 9);
+        symxg::launch_convert_to_double<float>((int64_t)I.nnzb * 9, I.vals32.p, tmp.p, I.stream);
+        ck(cudaStreamSynchronize(I.stream), "synchronize");
+        ck(cudaMemcpy(vals, tmp.p, sizeof(double) * I.nnzb * 9, cudaMemcpyDeviceToHost), "download");
+    } else {
+        assemble_t<double>(I, project, settings, 0);
+        ck(cudaStreamSynchronize(I.stream), "synchronize");
+        ck(cudaMemcpy(vals, I.vals64.p, sizeof(double) * I.nnzb * 9, cudaMemcpyDeviceToHost), "download");
+    }
+    ck(cudaMemcpy(row_ptr, I.row_ptr.p, sizeof(int32_t) * (I.n_blocks + 1), cudaMemcpyDeviceToHost), "download");
+    ck(cudaMemcpy(cols, I.cols.p, sizeof(int32_t) * I.nnzb, cudaMemcpyDeviceToHost), "download");
+}
+
+void NewtonsMethod::element_outputs(int p, bool project, double* E, double* g, double* H)
+{
+    SolverImpl& I = *impl;
+    const auto& cp = I.pots.at(p);
+    const int n = 3 * cp.nb;
+    const bool mixed = settings.precision == Precision::Mixed;
+    if (mixed) assemble_t<float>(I, project, settings, 1);
+    else assemble_t<double>(I, project, settings, 0);
+    ck(cudaStreamSynchronize(I.stream), "synchronize");
+    if (E) ck(cudaMemcpy(E, I.E_el.p + cp.e_off, sizeof(double) * cp.n_elements, cudaMemcpyDeviceToHost), "download");
+    if (g) ck(cudaMemcpy(g, I.g_el.p + cp.g_off * 3, sizeof(double) * cp.n_elements * n, cudaMemcpyDeviceToHost), "download");
+    if (H) {
+        std::vector<double> bm((size_t)cp.n_elements * n * n);
+        if (mixed) {
+            std::vector<float> f(bm.size());
+            ck(cudaMemcpy(f.data(), I.H32.p + cp.h_off * 9, sizeof(float) * f.size(), cudaMemcpyDeviceToHost), "download");
+            std::copy(f.begin(), f.end(), bm.begin());
+        } else {
+            ck(cudaMemcpy(bm.data(), I.H64.p + cp.h_off * 9, sizeof(double) * bm.size(), cudaMemcpyDeviceToHost), "download");
+        }
+        for (int64_t e = 0; e < cp.n_elements; ++e)
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j)
+                    H[(e * n + i) * n + j] = bm[e * n * n + (((i / 3) * cp.nb + (j / 3)) * 3 + (i % 3)) * 3 + (j % 3)];
+    }
+}
+
+namespace {
+
+template <typename T>
+SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int verbosity)
+{
+    I.ensure_precision(std::is_same<T, float>::value ? Precision::Mixed : Precision::FP64);
+    const int mode = std::is_same<T, float>::value ? 1 : 0;
+    const int64_t n = I.n_dofs;
+    cudaStream_t s = I.stream;
+    StageTimer timer;
+    timer.s = s;
+    DevBuf<T>* V = I.vecs<T>();
+    PcgBuffers<T> B;
+    B.n_blocks = I.n_blocks;
+    B.row_ptr = I.row_ptr.p;
+    B.cols = I.cols.p;
+    B.vals = I.vals<T>();
+    B.Dinv = I.Dinv<T>();
+    B.x = V[0].p;
+    B.r = V[1].p;
+    B.z = V[2].p;
+    B.p = V[3].p;
+    B.q = V[4].p;
+    B.partials = I.partials.p;
+    B.tickets = I.tickets.p;
+    B.state = I.pcg_state.p;
+    T* du = V[0].p;
+
+    if (S.projection_mode != ProjectionToPD::ProjectedNewton && S.projection_mode != ProjectionToPD::Newton)
+        throw std::runtime_error("symx_gb300: projection modes ProjectOnDemand/Progressive are not implemented");
+    if (S.linear_solver != LinearSolver::BDPCG) throw std::runtime_error("symx_gb300: only the BDPCG linear solver is implemented");
+
+    double res0 = std::numeric_limits<double>::max();
+    double E0 = 0.0, residual = 0.0;
+    SolverReturn result = SolverReturn::Running;
+    int it = -1;
+    ck(cudaMemsetAsync(I.flags.p, 0, sizeof(int), s), "memset");
+    while (result == SolverReturn::Running) {
+        ++it;
+        if (it == S.max_iterations) {
+            result = S.max_iterations_as_success ? SolverReturn::Successful : SolverReturn::TooManyIterations;
+            break;
+        }
+        // energy, gradient and element Hessians
+        timer.start("evaluate_P_grad_hess");
+        I.launch_eval(mode);
+        symxg::launch_sum(I.E_el.p, I.n_elements_total, I.partials.p, I.tickets.p + 4, I.scalars.p, s);
+        symxg::launch_gather_gradient(I.n_blocks, I.gptr.p, I.gcontrib.p, I.g_el.p, I.grad.p, s);
+        symxg::launch_max_abs(I.grad.p, n, I.partials.p, I.tickets.p + 4, I.scalars.p + 1, s);
+        timer.stop();
+        I.read_scalars(2);
+        E0 = I.h_scalars[0];
+        residual = I.h_scalars[1];
+        if (verbosity > 0) std::printf("  %2d. r0: %.2e | E: %.6e | ", it, residual, E0);
+        if (it == 0) res0 = residual;
+        if (residual < S.bailout_residual) { result = SolverReturn::Successful; break; }
+        if (it >= S.min_iterations) {
+            if (residual < S.residual_tolerance_abs) { result = SolverReturn::Successful; break; }
+            if (it > 0 && residual / res0 < S.residual_tolerance_rel) { result = SolverReturn::Successful; break; }
+        }
+        // projection and assembly
+        if (S.projection_mode == ProjectionToPD::ProjectedNewton) {
+            timer.start("project_to_PD");
+            for (auto& cp : I.pots)
+                symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)S.projection_eps,
+                                            S.project_to_pd_use_mirroring, I.flags.p, s);
+            timer.stop();
+            st.n_projected_hessians += (uint64_t)I.n_elements_total;
+        }
+        st.n_hessians += (uint64_t)I.n_elements_total;
+        timer.start("assembly");
+        symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), s);
+        symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.Dinv<T>(), s);
+        timer.stop();
+        // linear solve: block-Jacobi PCG with the reference's forcing sequence
+        timer.start("linear_system_solve");
+        const double forcing = std::min(1e-2, residual * std::min(0.5, std::sqrt(residual)));
+        PcgState init{};
+        init.abs_tol = std::max(forcing, S.cg_abs_tolerance);
+        init.rel_tol = S.cg_rel_tolerance;
+        init.max_iterations = S.cg_max_iterations;
+        ck(cudaMemcpyAsync(I.pcg_state.p, &init, sizeof(PcgState), cudaMemcpyHostToDevice, s), "pcg state");
+        symxg::launch_pcg_init<T>(B, I.grad.p, s);
+        int launched = 0, chunk = 4;
+        while (true) {
+            for (int k = 0; k < chunk; ++k) symxg::launch_pcg_iteration<T>(B, s);
+            launched += chunk;
+            ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
+            ck(cudaStreamSynchronize(s), "synchronize");
+            if (I.h_state->done || launched > S.cg_max_iterations + 1) break;
+            chunk = std::min(chunk * 2, 64);
+        }
+        timer.stop();
+        const PcgState ps = *I.h_state;
+        st.cg_iterations += ps.iteration;
+        if (verbosity > 0) std::printf("#CG: %4d | ", ps.iteration);
+        if (!ps.converged) {
+            result = SolverReturn::LinearSystemSolveFailure;
+            break;
+        }
+        symxg::launch_dot_mixed<T>(du, I.grad.p, n, I.partials.p, I.tickets.p + 4, I.scalars.p + 2, s);
+        // max |du|
+        symxg::launch_convert_to_double<T>(n, du, I.x_before.p, s);
+        symxg::launch_max_abs(I.x_before.p, n, I.partials.p, I.tickets.p + 4, I.scalars.p + 3, s);
+        I.read_scalars(4);
+        const double du_dot_grad = I.h_scalars[2];
+        double du_max = I.h_scalars[3];
+        if (!(du_dot_grad < 0.0)) {
+            result = SolverReturn::StepDoesNotDescend;
+            break;
+        }
+        if (verbosity > 0) std::printf("du: %.1e | ", du_max);
+        if (it >= S.min_iterations && du_max < S.step_tolerance) {
+            result = SolverReturn::Successful;
+            break;
+        }
+        // line search: cap, then Armijo backtracking on the energy
+        double retraction = 1.0;
+        if (du_max > S.step_cap) {
+            retraction *= S.step_cap / du_max;
+            du_max = S.step_cap;
+            st.ls_cap_iterations++;
+        }
+        timer.start("evaluate_P");
+        ck(cudaMemcpyAsync(I.x_before.p, I.x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy");
+        double step = 1.0;
+        symxg::launch_axpy_to<T>(n, I.x_before.p, step * retraction, du, I.x.p, s);
+        if (S.enable_armijo_backtracking) {
+            const double expected = S.line_search_armijo_beta * du_dot_grad * retraction;
+            double E_thr = E0 + expected * step;
+            int a = 0;
+            for (; a < S.max_backtracking_armijo_iterations; ++a) {
+                I.launch_eval(2);
+                symxg::launch_sum(I.E_el.p, I.n_elements_total, I.partials.p, I.tickets.p + 4, I.scalars.p, s);
+                I.read_scalars(1);
+                const double E1 = I.h_scalars[0];
+                if (E1 < E_thr) break;
+                step *= 0.5;
+                symxg::launch_axpy_to<T>(n, I.x_before.p, step * retraction, du, I.x.p, s);
+                E_thr = E0 + expected * step;
+                st.ls_bt_iterations++;
+            }
+            if (verbosity > 0 && a > 0) std::printf("ls bt %2d | ", a);
+            if (a == S.max_backtracking_armijo_iterations) {
+                timer.stop();
+                result = SolverReturn::TooManyArmijoIterations;
+                break;
+            }
+        }
+        timer.stop();
+        if (verbosity > 0) std::printf("\n");
+    }
+    if (verbosity > 0) std::printf("\n");
+    ck(cudaStreamSynchronize(s), "synchronize");
+    int nc = 0;
+    ck(cudaMemcpy(&nc, I.flags.p, sizeof(int), cudaMemcpyDeviceToHost), "flags");
+    st.projection_not_converged = nc;
+    timer.flush(st.timers);
+    st.newton_iterations = it;
+    st.final_residual = residual;
+    st.final_energy = E0;
+    if (st.n_hessians > 0) st.projected_hessians_ratio = (double)st.n_projected_hessians / (double)st.n_hessians;
+    return result;
+}
+
+}  // namespace
+
+SolverReturn NewtonsMethod::solve_device()
+{
+    stats = SolveStats();
+    stats.h2d_bytes = h2d_bytes_;
+    stats.d2h_bytes = d2h_bytes_;
+    if (settings.precision == Precision::Mixed) return solve_t<float>(*impl, settings, stats, context->verbosity);
+    return solve_t<double>(*impl, settings, stats, context->verbosity);
+}
+
+}  // namespace symx

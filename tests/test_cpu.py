@@ -1,0 +1,182 @@
+"""CPU tests: the oracle against the reference's golden vectors, the C ABI library loading
+and exporting every declared symbol, argument validation, and the C++ API (symbolic front
+end, differentiation, NVRTC compilation of the generated kernels)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from symx_gb300 import problems
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CASES = ["tet4_3", "tet4_6p", "hex8_3", "tet4_10"]
+
+
+# ------------------------------------------------------------------ oracle pinning
+def test_oracle_element_matches_reference(golden):
+    d = golden("elem_nh_tet4")
+    rows, ref = d["inputs"], d["outputs"]
+    E, g, H = O.nh_element_batch(rows[:, :12].reshape(-1, 4, 3), rows[:, 12:24].reshape(-1, 4, 3), rows[:, 24], rows[:, 25])
+    assert np.max(np.abs(E - ref[:, 0]) / np.abs(ref[:, 0])) < 1e-11
+    assert np.max(np.abs(g - ref[:, 1:13])) < 1e-12 * np.max(np.abs(ref[:, 1:13]))
+    assert np.max(np.abs(H.reshape(-1, 144) - ref[:, 13:])) < 1e-12 * np.max(np.abs(ref[:, 13:]))
+
+
+def test_doc_hessian_kat_structure(golden):
+    """docs/source/compilation.md:269-281 prints a 12x12 Hessian for this element; the
+    reference's own current code (run through oracle/_ref) gives different values for these
+    inputs, so the printed values are not used as a pin.  Its zero pattern and symmetry are."""
+    k = golden("doc_hessian_kat")
+    _, _, H = O.nh_element_batch(k["x"][None], k["X"][None], np.array([float(k["mu"])]), np.array([float(k["lam"])]))
+    H = H[0]
+    assert np.array_equal(np.abs(H) < 1e-9 * np.abs(H).max(), k["H"] == 0)
+    assert np.allclose(H, H.T, atol=1e-9 * np.abs(H).max())
+
+
+@pytest.mark.parametrize("name", ["project12", "project24"])
+def test_oracle_projection_matches_reference(golden, name):
+    d = golden(name)
+    out, changed = O.project_pd_batch(d["inputs"])
+    for i in range(out.shape[0]):
+        assert np.max(np.abs(out[i] - d["outputs"][i])) <= 1e-12 * np.max(np.abs(d["inputs"][i]))
+    assert np.array_equal(changed, d["changed"].astype(bool))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_problem_matches_reference(golden, case):
+    p = problems.step_problem(case)
+    P = O.Problem(p, 1)
+    ev = golden(f"{case}_eval")
+    E, g = P.evaluate()
+    assert abs(E - ev["E"]) <= 1e-13 * abs(ev["E"])
+    assert np.max(np.abs(g - ev["grad"])) <= 1e-11 * np.max(np.abs(ev["grad"]))
+    rp, cols, vals, _ = P.assemble(True)
+    A = O.bcsr_to_scipy(rp, cols, vals)
+    assert A.nnz == int(ev["nnz"])
+    for v, ref in zip(ev["probe_vectors"], ev["probe_products"]):
+        assert np.max(np.abs(A @ v - ref)) <= 1e-12 * np.max(np.abs(ref))
+    sol = golden(f"{case}_solve")
+    P.set_x(p["x_init"])
+    st = P.solve(O.default_settings(cg_rel_tolerance=1e-3))
+    assert st["solver_return"] == 0
+    assert st["newton_iterations"] == int(sol["newton_iterations_full"])
+    assert st["cg_iterations"] == int(sol["cg_iterations_full"])
+    x = P.get_x()
+    assert np.linalg.norm(x - sol["x_full"]) / np.linalg.norm(sol["x_full"] - p["x0"]) < 1e-10
+
+
+def test_oracle_failure_codes():
+    p = problems.step_problem("tet4_3")
+    P = O.Problem(p, 1)
+    st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, max_iterations=1))
+    assert st["solver_return"] == 2  # too many iterations
+    P.set_x(p["x_init"])
+    st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, armijo_beta=1e6, max_armijo=3))
+    assert st["solver_return"] == 6  # Armijo failure
+
+
+def test_problem_sizes():
+    # mesh sizes of the named workloads (vertices, elements)
+    for name, nv, ne in (("tet4_10", 1331, 6000), ("tet4_32", 35937, 196608)):
+        c = problems.CONFIGS[name]
+        X, conn = problems.cuboid_tet4(*c["cells"], [n * c["h"] for n in c["cells"]])
+        assert X.shape == (nv, 3) and conn.shape == (ne, 4)
+    X, conn = problems.cuboid_hex8(4, 3, 2, (0.04, 0.03, 0.02))
+    assert X.shape == (60, 3) and conn.shape == (24, 8)
+    # every tet has positive rest volume (orientation of the 6-tet split)
+    X, conn = problems.cuboid_tet4(3, 3, 3, (0.03, 0.03, 0.03))
+    P = X[conn]
+    D = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=2)
+    assert np.all(np.linalg.det(D) > 0)
+    # seeded normals are reproducible and standard
+    z = problems.normal(3, 200000)
+    assert np.array_equal(z, problems.normal(3, 200000))
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+
+
+# ------------------------------------------------------------------ C ABI
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "symx_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(symxg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from symx_gb300 import capi
+
+    declared = _declared_symbols()
+    assert sorted(capi.EXPORTS) == declared
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert lib.symxg_abi_version() == 1
+
+
+def test_invalid_arguments_are_reported(lib):
+    import ctypes as C
+
+    from symx_gb300 import capi
+
+    p = capi.ElasticProblem()
+    p.n_vertices = 4
+    p.n_elements = 1
+    p.nodes_per_element = 5  # invalid element type
+    h = C.c_void_p()
+    rc = lib.symxg_elastic_create(C.byref(p), None, C.byref(h))
+    assert rc == 1
+    assert b"nodes_per_element" in lib.symxg_last_error()
+    conn = np.array([[0, 1, 2, 7]], dtype=np.int32)  # vertex 7 does not exist
+    X = np.zeros((4, 3))
+    mu = np.ones(1)
+    p.nodes_per_element = 4
+    p.connectivity = conn.ctypes.data_as(C.c_void_p)
+    p.rest_positions = X.ctypes.data_as(C.c_void_p)
+    p.mu = mu.ctypes.data_as(C.c_void_p)
+    p.lam = mu.ctypes.data_as(C.c_void_p)
+    rc = lib.symxg_elastic_create(C.byref(p), None, C.byref(h))
+    assert rc == 1 and b"out of range" in lib.symxg_last_error()
+    assert lib.symxg_project_pd_f32(None, 12, 1, C.c_float(1e-10), 0, None, None) == 1
+    assert lib.symxg_project_pd_f64(C.c_void_p(8), 13, 1, 1e-10, 0, C.c_void_p(8), None) == 1
+    s = capi.NewtonSettings()
+    lib.symxg_default_settings(C.byref(s))
+    assert s.residual_tolerance_abs == 1e-6 and s.cg_rel_tolerance == 1e-4 and s.max_backtracking_armijo_iterations == 20
+
+
+# ------------------------------------------------------------------ C++ API
+@pytest.fixture(scope="module")
+def cpp_test(lib):
+    exe = os.path.join(ROOT, "symx_gb300", "_build", "test_cpu_api")
+    src = os.path.join(ROOT, "tests", "cpp", "test_cpu_api.cpp")
+    libdir = os.path.join(ROOT, "symx_gb300", "_build")
+    from symx_gb300.build import cuda_home
+
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+                    "-I" + os.path.join(cuda_home(), "include"), src, "-o", exe, "-L" + libdir, "-lsymxg",
+                    "-Wl,-rpath," + libdir], check=True)
+    return exe
+
+
+def test_cpp_symbolic_selftest(cpp_test):
+    r = subprocess.run([cpp_test, "selftest"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "selftest PASS" in r.stdout
+
+
+def test_cpp_symbolic_nh_matches_reference(cpp_test, golden, tmp_path):
+    d = golden("elem_nh_tet4")
+    rows, ref = d["inputs"], d["outputs"]
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        np.array([rows.shape[0]], dtype=np.int64).tofile(f)
+        rows.tofile(f)
+    subprocess.run([cpp_test, "nh_elem", str(fin), str(fout)], check=True)
+    out = np.fromfile(fout).reshape(-1, 157)
+    for sl in (slice(0, 1), slice(1, 13), slice(13, 157)):
+        assert np.max(np.abs(out[:, sl] - ref[:, sl])) <= 1e-13 * np.max(np.abs(ref[:, sl]))
+
+
+def test_cpp_generated_kernels_compile_with_nvrtc(cpp_test, tmp_path):
+    r = subprocess.run([cpp_test, "nvrtc", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "nvrtc PASS" in r.stdout

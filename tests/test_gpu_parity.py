@@ -1,0 +1,225 @@
+"""GPU parity of the CUDA solve path against the oracle and the reference's golden outputs.
+
+Every call goes through the C ABI (libsymxg.so).  Tolerances:
+  FP64 path   energy 1e-12 rel, gradient 1e-9 of max |g|, element Hessians 1e-10 of max |H|,
+              projected Hessians 1e-9 of max |H|, final positions 1e-8 of |x - x0|.
+  Mixed path  element Hessians 1e-5 of max |H| (float storage), final positions 1e-6 rel.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["tet4_3", "tet4_6p", "hex8_3", "tet4_10"]
+
+
+@pytest.fixture(scope="module")
+def sg(lib):
+    import symx_gb300
+
+    return symx_gb300
+
+
+def make(sg, case, precision="fp64"):
+    from symx_gb300 import problems
+
+    p = problems.step_problem(case)
+    s = sg.ElasticSolver(p)
+    s.set_settings(cg_rel_tolerance=1e-3, precision=precision)
+    s.set_state(p["x_init"], p["x0"], p["v0"])
+    return p, s
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_energy_gradient_match_reference(sg, golden, case):
+    p, s = make(sg, case)
+    ev = golden(f"{case}_eval")
+    E, g = s.evaluate()
+    assert abs(E - ev["E"]) <= 1e-12 * abs(ev["E"])
+    assert np.max(np.abs(g - ev["grad"])) <= 1e-9 * np.max(np.abs(ev["grad"]))
+    assert abs(s.evaluate_energy() - ev["E_only"]) <= 1e-12 * abs(ev["E_only"])
+
+
+@pytest.mark.parametrize("case", ["tet4_3", "hex8_3", "tet4_6p"])
+def test_element_outputs_match_oracle(sg, golden, case):
+    from oracle import oracle as O
+
+    p, s = make(sg, case)
+    E, g, H = s.element_outputs(0, project=False)
+    nodes = p["conn"].shape[1]
+    xe = p["x_init"][p["conn"]]
+    Xe = p["X"][p["conn"]]
+    E_o, g_o, H_o = O.nh_element_batch(xe, Xe, p["mu"], p["lam"])
+    assert np.max(np.abs(E - E_o)) <= 1e-12 * np.max(np.abs(E_o)) + 1e-300
+    assert np.max(np.abs(g - g_o)) <= 1e-10 * np.max(np.abs(g_o)) + 1e-300
+    assert np.max(np.abs(H - H_o)) <= 1e-10 * np.max(np.abs(H_o))
+    # projected element Hessians against the reference's project_to_PD_inplace
+    ev = golden(f"{case}_eval")
+    _, _, Hp = s.element_outputs(0, project=True)
+    idx = ev["hess_sample_idx"]
+    ref = ev["hess_sample_projected"]
+    assert np.max(np.abs(Hp[idx] - ref)) <= 1e-9 * np.max(np.abs(ref))
+    assert nodes in (4, 8)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_assembled_hessian_matches_reference(sg, golden, case):
+    from oracle import oracle as O
+
+    p, s = make(sg, case)
+    ev = golden(f"{case}_eval")
+    rp, cols, vals = s.assembled_hessian(project=True)
+    A = O.bcsr_to_scipy(rp, cols, vals)
+    assert A.nnz == int(ev["nnz"])
+    for v, ref in zip(ev["probe_vectors"], ev["probe_products"]):
+        y = A @ v
+        # the penalty rows dominate the scale; compare the elastic part separately too
+        assert np.max(np.abs(y - ref)) <= 1e-10 * np.max(np.abs(ref))
+    free = np.setdiff1d(np.arange(p["X"].shape[0]), p["bc_idx"])
+    rows = (3 * free[:, None] + np.arange(3)).ravel()
+    for v, ref in zip(ev["probe_vectors"], ev["probe_products"]):
+        y = A @ v
+        assert np.max(np.abs(y[rows] - ref[rows])) <= 1e-9 * np.max(np.abs(ref[rows]))
+    if "triplet_idx" in ev.files:
+        import scipy.sparse as sp
+
+        ti, tv = ev["triplet_idx"], ev["triplet_val"]
+        R = sp.coo_matrix((tv, (ti[:, 0], ti[:, 1])), shape=A.shape).tocsr()
+        D = (A - R).tocoo()
+        scale = np.max(np.abs(R[rows][:, rows].data))
+        dd = (A - R)[rows][:, rows]
+        assert np.max(np.abs(dd.data), initial=0.0) <= 1e-9 * scale
+        assert np.max(np.abs(D.data), initial=0.0) <= 1e-9 * np.max(np.abs(R.data))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_newton_fp64_matches_reference(sg, golden, case):
+    p, s = make(sg, case)
+    st = s.solve()
+    sol = golden(f"{case}_solve")
+    assert st["solver_return"] == 0
+    assert st["final_residual"] < 1e-6
+    assert st["newton_iterations"] == int(sol["newton_iterations_full"])
+    assert abs(st["cg_iterations"] - int(sol["cg_iterations_full"])) <= 2 + 0.02 * int(sol["cg_iterations_full"])
+    x, xr = s.get_positions(), sol["x_full"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr - p["x0"]) < 1e-8
+    # a single Newton iteration reproduces the reference's first step too
+    s.set_settings(max_iterations=1, max_iterations_as_success=1)
+    s.set_state(p["x_init"], p["x0"], p["v0"])
+    st1 = s.solve()
+    x1, xr1 = s.get_positions(), sol["x_it1"]
+    assert st1["solver_return"] == 0
+    assert np.linalg.norm(x1 - xr1) / np.linalg.norm(xr1 - p["x0"]) < 1e-8
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_newton_mixed_converges_to_fp64_solution(sg, golden, case):
+    p, s = make(sg, case, precision="mixed")
+    st = s.solve()
+    sol = golden(f"{case}_solve")
+    assert st["solver_return"] == 0
+    assert st["final_residual"] < 1e-6
+    x, xr = s.get_positions(), sol["x_full"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr - p["x0"]) < 1e-4
+
+
+def test_mixed_element_hessians_within_float_tolerance(sg):
+    p, s = make(sg, "tet4_6p", precision="mixed")
+    _, _, H32 = s.element_outputs(0, project=False)
+    s.set_settings(precision="fp64")
+    _, _, H64 = s.element_outputs(0, project=False)
+    assert np.max(np.abs(H32 - H64)) <= 1e-5 * np.max(np.abs(H64))
+
+
+@pytest.mark.parametrize("dtype,tol", [("float64", 1e-9), ("float32", 1e-4)])
+def test_project_pd_kernel_matches_reference(sg, golden, dtype, tol):
+    import torch
+
+    for name in ("project12", "project24"):
+        d = golden(name)
+        H = torch.tensor(d["inputs"], dtype=getattr(torch, dtype), device="cuda")
+        nc = sg.project_pd(H)
+        out = H.double().cpu().numpy()
+        for i in range(out.shape[0]):
+            scale = np.max(np.abs(d["inputs"][i]))
+            assert np.max(np.abs(out[i] - d["outputs"][i])) <= tol * scale, (name, i)
+        assert not nc
+
+
+def test_project_pd_edge_cases(sg):
+    import torch
+
+    # already positive definite: untouched; zero matrix: all eigenvalues clamped to eps
+    A = torch.eye(12, dtype=torch.float64, device="cuda").repeat(3, 1, 1)
+    A[1] *= 5.0
+    A[2].zero_()
+    ref = A.clone()
+    sg.project_pd(A)
+    assert torch.equal(A[0], ref[0]) and torch.equal(A[1], ref[1])
+    assert torch.allclose(A[2], 1e-10 * torch.eye(12, dtype=torch.float64, device="cuda"))
+    # empty batch
+    E = torch.zeros((0, 12, 12), dtype=torch.float32, device="cuda")
+    sg.project_pd(E)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_bcsr_spmv_kernel(sg, dtype):
+    import torch
+
+    from oracle import oracle as O
+    from symx_gb300 import problems
+
+    p = problems.step_problem("tet4_6p")
+    ref = O.Problem(p, 1)
+    rp, cols, vals, _ = ref.assemble(True)
+    A = O.bcsr_to_scipy(rp, cols, vals)
+    x = problems.normal(5, A.shape[0])
+    t = getattr(torch, dtype)
+    y = torch.zeros(A.shape[0], dtype=t, device="cuda")
+    sg.bcsr_spmv(torch.tensor(rp, device="cuda"), torch.tensor(cols, device="cuda"),
+                 torch.tensor(vals, dtype=t, device="cuda"), torch.tensor(x, dtype=t, device="cuda"), y)
+    tol = 1e-12 if dtype == "float64" else 1e-5
+    yr = A @ x
+    assert np.max(np.abs(y.double().cpu().numpy() - yr)) <= tol * np.max(np.abs(yr))
+
+
+def test_deterministic_repeat(sg):
+    p, s = make(sg, "tet4_6p", precision="mixed")
+    s.solve()
+    x1 = s.get_positions()
+    s.set_state(p["x_init"], p["x0"], p["v0"])
+    s.solve()
+    assert np.array_equal(x1, s.get_positions())
+
+
+def test_failure_modes_return_codes(sg):
+    # PCG capped at one iteration cannot reach the forcing tolerance: linear-solve failure
+    p, s = make(sg, "tet4_10")
+    s.set_settings(cg_max_iterations=1)
+    st = s.solve()
+    assert st["solver_return_name"] == "LinearSystemSolveFailure"
+    # an unreachable Armijo condition exhausts the backtracking budget
+    p, s = make(sg, "tet4_3")
+    s.set_settings(line_search_armijo_beta=1e6, max_backtracking_armijo_iterations=3)
+    st = s.solve()
+    assert st["solver_return_name"] == "TooManyArmijoIterations"
+    # max_iterations without success flag
+    p, s = make(sg, "tet4_3")
+    s.set_settings(max_iterations=1)
+    st = s.solve()
+    assert st["solver_return_name"] == "TooManyIterations"
+
+
+def test_inverted_initial_element_is_rejected_by_line_search(sg):
+    # an inverted element makes E = +inf (log guard): the first evaluation is not finite and
+    # the solver reports failure instead of returning garbage
+    p, s = make(sg, "tet4_3")
+    x = p["x_init"].copy()
+    t = p["conn"][5]
+    x[t[0]], x[t[1]] = x[t[1]].copy(), x[t[0]].copy()
+    s.set_state(x, p["x0"], p["v0"])
+    E, _ = s.evaluate()
+    assert np.isinf(E) and E > 0
+    st = s.solve()
+    assert st["solver_return"] != 0
