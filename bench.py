@@ -275,6 +275,31 @@ def cpu_baseline(p, args):
                                                             "t_line_search")}}
 
 
+def run_profile(args):
+    """Setup + one warm-up and one timed solve of the workload in one precision (the command
+    the ncu captures wrap).  Prints the stage times of the timed solve."""
+    import torch
+
+    import symx_gb300 as sg
+    from symx_gb300 import problems
+
+    p = problems.step_problem(args.config)
+    solver = sg.ElasticSolver(p)
+    solver.set_settings(cg_rel_tolerance=1e-3, precision=args.profile_solve)
+    out = None
+    for i in range(2):
+        solver.set_state(p["x_init"], p["x0"], p["v0"])
+        solver.upload()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = solver.solve_device()
+        torch.cuda.synchronize()
+        out = {"profile_solve": args.profile_solve, "config": args.config, "wall_ms": (time.perf_counter() - t0) * 1e3,
+               **{k: st[k] for k in st}}
+    print(json.dumps(out))
+    return None
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -316,6 +341,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-newton-iterations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--profile-solve", choices=["mixed", "fp64"], default=None)
     args = ap.parse_args()
     rank, world, _ = dist_env()
     if world > 1 and args.impl == "ours":
@@ -324,6 +350,9 @@ def main():
 
         torch.cuda.set_device(dist_env()[2])
         dist.init_process_group("nccl")
+    if args.profile_solve:
+        run_profile(args)
+        return
     if args.impl == "reference":
         out = run_reference(args)
     else:

@@ -64,9 +64,10 @@ template <typename T>
 static int project_impl(T* m, int32_t n, int64_t count, T eps, int32_t mirroring, int32_t* nc, void* stream)
 {
     return guarded([&] {
-        if (!m || !nc) throw std::invalid_argument("null device pointer");
         if (n <= 0 || n % 3 != 0 || n > 24) throw std::invalid_argument("n must be a multiple of 3 up to 24");
         if (count < 0) throw std::invalid_argument("negative count");
+        if (count == 0) return SYMXG_OK;
+        if (!m || !nc) throw std::invalid_argument("null device pointer");
         symxg::launch_project_pd<T>(m, n, count, eps, mirroring != 0, nc, (cudaStream_t)stream);
         return SYMXG_OK;
     });

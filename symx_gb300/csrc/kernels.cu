@@ -279,14 +279,16 @@ __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ d
 constexpr int kSpmvThreads = 256;  // 16 rows per block, 16 lanes per row
 
 // Partial product of one block row over the lanes of a 16-lane group, reduced across the
-// group in a fixed butterfly order.  Valid in every lane of the group.
+// group in a fixed butterfly order.  Every lane of the warp must call it (rows past the end
+// pass valid = false and contribute zeros), so the full-mask shuffles are always converged.
 template <typename T>
-__device__ __forceinline__ void row_product(int row, int lane16, const int32_t* __restrict__ row_ptr,
+__device__ __forceinline__ void row_product(bool valid, int row, int lane16, const int32_t* __restrict__ row_ptr,
                                             const int32_t* __restrict__ cols, const T* __restrict__ vals,
                                             const T* __restrict__ x, T& s0, T& s1, T& s2)
 {
     s0 = s1 = s2 = T(0);
-    const int kb = row_ptr[row], ke = row_ptr[row + 1];
+    const int kb = valid ? row_ptr[row] : 0;
+    const int ke = valid ? row_ptr[row + 1] : 0;
     for (int k = kb + lane16; k < ke; k += 16) {
         const T* b = vals + (int64_t)k * 9;
         const int c = cols[k];
@@ -310,10 +312,10 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const 
 {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
     const int lane16 = threadIdx.x & 15;
-    if (row >= n_blocks) return;  // whole 16-lane groups exit together
+    const bool valid = row < n_blocks;
     T s0, s1, s2;
-    row_product<T>(row, lane16, row_ptr, cols, vals, x, s0, s1, s2);
-    if (lane16 == 0) {
+    row_product<T>(valid, row, lane16, row_ptr, cols, vals, x, s0, s1, s2);
+    if (valid && lane16 == 0) {
         y[3 * row] = s0;
         y[3 * row + 1] = s1;
         y[3 * row + 2] = s2;
@@ -327,10 +329,11 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B)
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
     const int lane16 = threadIdx.x & 15;
     double pq = 0.0;
-    if (row < B.n_blocks) {
-        T s0, s1, s2;
-        row_product<T>(row, lane16, B.row_ptr, B.cols, B.vals, B.p, s0, s1, s2);
-        if (lane16 == 0) {
+    const bool valid = row < B.n_blocks;
+    T s0, s1, s2;
+    row_product<T>(valid, row, lane16, B.row_ptr, B.cols, B.vals, B.p, s0, s1, s2);
+    {
+        if (valid && lane16 == 0) {
             B.q[3 * row] = s0;
             B.q[3 * row + 1] = s1;
             B.q[3 * row + 2] = s2;
@@ -555,6 +558,7 @@ template <typename T>
 void launch_pcg_iteration(const PcgBuffers<T>& B, cudaStream_t s)
 {
     const unsigned gs = blocks_for((int64_t)B.n_blocks * 16, kSpmvThreads);
+    if (gs > (unsigned)kPcgMaxPartials) throw std::runtime_error("symx_gb300: system too large for the PCG partials");
     k_pcg_spmv<T><<<gs, kSpmvThreads, 0, s>>>(B);
     k_pcg_update<T><<<blocks_for(B.n_blocks, 256), 256, 0, s>>>(B);
     k_pcg_direction<T><<<blocks_for(3 * (int64_t)B.n_blocks, 256), 256, 0, s>>>(B);

@@ -35,14 +35,16 @@ SYMXG_DEVICE constexpr int tri(int i, int j)
 
 template <typename T>
 struct JacobiTol;
+// Stop when the off-diagonal Frobenius norm is below 32 ulp of the matrix norm: rotations
+// leave rounding-level off-diagonal entries behind, so a tighter test would never pass.
 template <>
 struct JacobiTol<float> {
-    static SYMXG_DEVICE float rel2() { return 1.4210855e-14f; }  // (2^-23)^2
-    static constexpr int max_sweeps = 12;
+    static SYMXG_DEVICE float rel2() { return 1.4551915e-11f; }  // (32 * 2^-23)^2
+    static constexpr int max_sweeps = 15;
 };
 template <>
 struct JacobiTol<double> {
-    static SYMXG_DEVICE double rel2() { return 4.930380657631324e-32; }  // (2^-52)^2
+    static SYMXG_DEVICE double rel2() { return 5.048709793414476e-29; }  // (32 * 2^-52)^2
     static constexpr int max_sweeps = 20;
 };
 
