@@ -18,8 +18,9 @@
 //       (examples/rubber_extrusion.cpp:94-107) potentials.
 //   * project_to_PD_inplace (symx/src/solver/second_order/project_to_PD.cpp:12-32):
 //       eigenvalues < eps become eps (or -lambda when mirroring), A = V diag V^T only if
-//       something changed.  The eigen-decomposition here is cyclic Jacobi (Golub & Van Loan,
-//       Matrix Computations, 8.5) instead of Eigen's tridiagonal QL.
+//       something changed.  The eigen-decomposition here is Householder tridiagonalization +
+//       implicit symmetric QR (Golub & Van Loan, Matrix Computations, 8.3), the algorithm class
+//       of the reference's Eigen::SelfAdjointEigenSolver, written out here.
 //   * Assembly of all element blocks, both triangles (ElementHessians.cpp:224-256).
 //   * Block-Jacobi preconditioner: symmetric 3x3 inverse of the diagonal blocks
 //       (BlockedSparseMatrix.h:1146-1278) and its application (:1280-1361).
@@ -226,21 +227,117 @@ void jacobi_eig(int n, double* A, double* V)
     }
 }
 
+// Symmetric eigen-decomposition by Householder tridiagonalization (Golub & Van Loan,
+// Matrix Computations, Alg. 8.3.1) followed by implicit symmetric QR steps with the
+// Wilkinson shift (Alg. 8.3.2), accumulating all transformations.  The same algorithm class
+// as the reference's Eigen::SelfAdjointEigenSolver.  On return lam holds the eigenvalues and
+// Q (row-major) the eigenvectors as columns.  Returns false if the QR iteration did not
+// converge.
+bool symmetric_eig(int n, const double* A_in, double* lam, double* Q)
+{
+    std::vector<double> A(A_in, A_in + n * n), v(n), p(n), w(n);
+    for (int i = 0; i < n * n; ++i) Q[i] = 0.0;
+    for (int i = 0; i < n; ++i) Q[i * n + i] = 1.0;
+    for (int k = 0; k + 2 < n; ++k) {
+        // Householder vector for x = A[k+1:n, k]
+        double alpha = 0.0;
+        for (int i = k + 1; i < n; ++i) alpha += A[i * n + k] * A[i * n + k];
+        alpha = std::sqrt(alpha);
+        if (alpha == 0.0) continue;
+        const double x0 = A[(k + 1) * n + k];
+        const double r = x0 >= 0.0 ? -alpha : alpha;  // reflect x onto r e1
+        for (int i = 0; i < n; ++i) v[i] = 0.0;
+        v[k + 1] = x0 - r;
+        for (int i = k + 2; i < n; ++i) v[i] = A[i * n + k];
+        double vv = 0.0;
+        for (int i = k + 1; i < n; ++i) vv += v[i] * v[i];
+        if (vv == 0.0) continue;
+        const double beta = 2.0 / vv;
+        // p = beta A v, w = p - (beta p.v / 2) v, A -= v w^T + w v^T (trailing block incl. column k)
+        for (int i = k; i < n; ++i) {
+            double s = 0.0;
+            for (int j = k + 1; j < n; ++j) s += A[i * n + j] * v[j];
+            p[i] = beta * s;
+        }
+        double pv = 0.0;
+        for (int i = k + 1; i < n; ++i) pv += p[i] * v[i];
+        for (int i = k; i < n; ++i) w[i] = p[i] - 0.5 * beta * pv * v[i];
+        for (int i = k + 1; i < n; ++i)
+            for (int j = k + 1; j < n; ++j) A[i * n + j] -= v[i] * w[j] + w[i] * v[j];
+        A[(k + 1) * n + k] = A[k * n + k + 1] = r;
+        for (int i = k + 2; i < n; ++i) A[i * n + k] = A[k * n + i] = 0.0;
+        // Q = Q (I - beta v v^T)
+        for (int i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int j = k + 1; j < n; ++j) s += Q[i * n + j] * v[j];
+            s *= beta;
+            for (int j = k + 1; j < n; ++j) Q[i * n + j] -= s * v[j];
+        }
+    }
+    std::vector<double> d(n), e(n, 0.0);
+    for (int i = 0; i < n; ++i) d[i] = A[i * n + i];
+    for (int i = 0; i + 1 < n; ++i) e[i] = A[i * n + i + 1];
+    const double eps = std::numeric_limits<double>::epsilon();
+    int hi = n - 1, guard = 0;
+    while (hi > 0) {
+        if (++guard > 60 * n) return false;
+        // deflate converged trailing off-diagonals
+        if (std::fabs(e[hi - 1]) <= eps * (std::fabs(d[hi - 1]) + std::fabs(d[hi]))) {
+            e[hi - 1] = 0.0;
+            --hi;
+            continue;
+        }
+        int lo = hi - 1;
+        while (lo > 0 && std::fabs(e[lo - 1]) > eps * (std::fabs(d[lo - 1]) + std::fabs(d[lo]))) --lo;
+        // Wilkinson shift from the trailing 2x2 block
+        const double dd = 0.5 * (d[hi - 1] - d[hi]);
+        const double b2 = e[hi - 1] * e[hi - 1];
+        const double mu = d[hi] - b2 / (dd + (dd >= 0.0 ? 1.0 : -1.0) * std::sqrt(dd * dd + b2));
+        // implicit QR step on rows/cols lo..hi (bulge chase with Givens rotations)
+        double x = d[lo] - mu, z = e[lo];
+        for (int k = lo; k < hi; ++k) {
+            const double rr = std::hypot(x, z);
+            const double c = x / rr, sn = -z / rr;
+            if (k > lo) e[k - 1] = rr;
+            const double a11 = d[k], a22 = d[k + 1], a12 = e[k];
+            d[k] = c * c * a11 - 2.0 * c * sn * a12 + sn * sn * a22;
+            d[k + 1] = sn * sn * a11 + 2.0 * c * sn * a12 + c * c * a22;
+            e[k] = c * sn * (a11 - a22) + (c * c - sn * sn) * a12;
+            if (k + 1 < hi) {
+                x = e[k];
+                z = -sn * e[k + 1];
+                e[k + 1] = c * e[k + 1];
+            }
+            for (int i = 0; i < n; ++i) {
+                const double qk = Q[i * n + k], qk1 = Q[i * n + k + 1];
+                Q[i * n + k] = c * qk - sn * qk1;
+                Q[i * n + k + 1] = sn * qk + c * qk1;
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) lam[i] = d[i];
+    return true;
+}
+
 bool project_pd(int n, double* M, double eps, bool mirroring)
 {
-    std::vector<double> A(M, M + n * n), V(n * n), lam(n);
-    jacobi_eig(n, A.data(), V.data());
+    std::vector<double> V(n * n), lam(n);
+    if (!symmetric_eig(n, M, lam.data(), V.data())) {
+        // fall back to Jacobi for the (never observed) non-converging case
+        std::vector<double> A(M, M + n * n);
+        jacobi_eig(n, A.data(), V.data());
+        for (int i = 0; i < n; ++i) lam[i] = A[i * n + i];
+    }
     bool changed = false;
     for (int i = 0; i < n; ++i) {
-        lam[i] = A[i * n + i];
         if (lam[i] < eps) { changed = true; lam[i] = mirroring ? -lam[i] : eps; }
     }
     if (!changed) return false;
     for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) {
+        for (int j = i; j < n; ++j) {
             double s = 0;
             for (int k = 0; k < n; ++k) s += V[i * n + k] * lam[k] * V[j * n + k];
-            M[i * n + j] = s;
+            M[i * n + j] = M[j * n + i] = s;
         }
     return true;
 }

@@ -60,14 +60,16 @@ __device__ __forceinline__ T symxg_powi(T x, int n)
 }
 
 std::string emit_device_function(const Expressions& g, const std::vector<int32_t>& outputs, const std::string& name,
-                                 const std::string& T, bool accumulate, OpCount* count)
+                                 const std::string& T, bool accumulate, OpCount* count,
+                                 const std::unordered_map<int32_t, int32_t>* external)
 {
+    auto is_external = [&](int32_t i) { return external && external->count(i) > 0; };
     int32_t top = 0;
     for (int32_t o : outputs) top = std::max(top, o);
     std::vector<uint8_t> need(top + 1, 0);
     for (int32_t o : outputs) need[o] = 1;
     for (int32_t i = top; i >= 0; --i) {
-        if (!need[i]) continue;
+        if (!need[i] || is_external(i)) continue;
         const Node& n = g[i];
         switch (n.op) {
             case Op::Zero: case Op::One: case Op::Const: case Op::Symbol: break;
@@ -78,6 +80,7 @@ std::string emit_device_function(const Expressions& g, const std::vector<int32_t
         }
     }
     auto ref = [&](int32_t i) -> std::string {
+        if (is_external(i)) return "c[" + std::to_string(external->at(i)) + "]";
         const Node& n = g[i];
         switch (n.op) {
             case Op::Zero: return "(" + T + ")0";
@@ -89,10 +92,10 @@ std::string emit_device_function(const Expressions& g, const std::vector<int32_t
     };
     OpCount oc;
     std::ostringstream s;
-    s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, " << T
-      << "* __restrict__ out)\n{\n";
+    s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, const " << T
+      << "* __restrict__ c, " << T << "* __restrict__ out)\n{\n";
     for (int32_t i = 0; i <= top; ++i) {
-        if (!need[i]) continue;
+        if (!need[i] || is_external(i)) continue;
         const Node& n = g[i];
         std::string e;
         switch (n.op) {

@@ -9,6 +9,7 @@
 
 #include <cstdint>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "symbolic.h"
@@ -20,11 +21,14 @@ struct OpCount {
     int64_t total() const { return add + sub + mul + div + neg + transcendental + branch + pow; }
 };
 
-// Emit `__device__ __forceinline__ void <name>(const T* __restrict__ in, T* __restrict__ out)`
-// computing every expression of `outputs` (node ids) in type `T` ("double" or "float").
-// If `accumulate` is set, outputs are added to `out` instead of assigned (summations).
+// Emit `__device__ __forceinline__ void <name>(const T* __restrict__ in, const T* __restrict__ c,
+// T* __restrict__ out)` computing every expression of `outputs` (node ids) in type `T`
+// ("double" or "float").  Nodes listed in `external` are not computed: they are read as
+// c[slot] (values hoisted out of the kernel).  If `accumulate` is set, outputs are added to
+// `out` instead of assigned (summations).
 std::string emit_device_function(const Expressions& g, const std::vector<int32_t>& outputs, const std::string& name,
-                                 const std::string& T, bool accumulate, OpCount* count = nullptr);
+                                 const std::string& T, bool accumulate, OpCount* count = nullptr,
+                                 const std::unordered_map<int32_t, int32_t>* external = nullptr);
 
 // Prelude shared by all generated sources: guarded log, integer powers, infinities.
 std::string codegen_prelude();

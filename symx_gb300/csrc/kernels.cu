@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <stdexcept>
 #include <string>
@@ -166,7 +167,7 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
             fro2 += v * v;
         }
     int sweep = 0;
-    for (; sweep < symxg_dev::JacobiTol<T>::max_sweeps; ++sweep) {
+    for (; sweep < (2 * symxg_dev::JacobiTol<T>::max_double_sweeps); ++sweep) {
         T off = T(0);
         for (int p = 0; p < N; ++p)
             for (int q = p + 1; q < N; ++q) off += T(2) * A[p * NMAX + q] * A[p * NMAX + q];
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
                 }
             }
     }
-    if (sweep == symxg_dev::JacobiTol<T>::max_sweeps) *not_converged = 1;
+    if (sweep == (2 * symxg_dev::JacobiTol<T>::max_double_sweeps)) *not_converged = 1;
     bool changed = false;
     for (int i = 0; i < N; ++i) {
         T l = A[i * NMAX + i];
@@ -322,27 +323,155 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const 
     }
 }
 
+// ---- float-float (double-single) accumulation for the FP32 PCG's dot products.
+// Error-free transformations on the FP32 pipe (TwoSum, FMA-based TwoProd); the __f*_rn
+// intrinsics keep the compiler from contracting or reordering them.  Relative accuracy is
+// about 2^-44, with no FP64 instruction per vector entry (FP64 is 1/64 rate on this part).
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float h = __fadd_rn(s, e);
+    return FF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ FF ff_prod(float x, float y)
+{
+    const float p = __fmul_rn(x, y);
+    return FF{p, fmaf(x, y, -p)};
+}
+__device__ __forceinline__ FF ff_shfl_down(FF a, int o)
+{
+    return FF{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+}
+
+// Accumulator of the PCG dot products: float-float for the FP32 PCG, double for FP64.
 template <typename T>
-__global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B)
+struct DotAcc;
+template <>
+struct DotAcc<float> {
+    FF v{0.f, 0.f};
+    __device__ __forceinline__ void add_prod(float x, float y) { v = ff_add(v, ff_prod(x, y)); }
+    // block-wide sum in fixed order; the result (as double) is valid in thread 0
+    __device__ double block_sum(double* sh)
+    {
+        FF a = v;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        __syncthreads();
+        float* shf = reinterpret_cast<float*>(sh);
+        if (lane == 0) { shf[2 * warp] = a.hi; shf[2 * warp + 1] = a.lo; }
+        __syncthreads();
+        if (warp == 0) {
+            a = lane < nw ? FF{shf[2 * lane], shf[2 * lane + 1]} : FF{0.f, 0.f};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
+        }
+        return (double)a.hi + (double)a.lo;
+    }
+};
+template <>
+struct DotAcc<double> {
+    double v = 0.0;
+    __device__ __forceinline__ void add_prod(double x, double y) { v = fma(x, y, v); }
+    __device__ double block_sum(double* sh) { return block_reduce<false>(v, sh); }
+};
+
+// Publish per-block partial sums (valid in thread 0) and let the last block combine them in
+// index order (double).  Returns true in the threads of the last block.
+template <int NPARTS>
+__device__ bool publish_and_combine(const double (&blockv)[NPARTS], double* partials, unsigned* ticket,
+                                    double (&result)[NPARTS])
+{
+    __shared__ double sh[32];
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NPARTS; ++k) partials[k * gridDim.x + blockIdx.x] = blockv[k];
+        __threadfence();
+        is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NPARTS; ++k) {
+        double acc = 0.0;
+        for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) acc += __ldcg(&partials[k * gridDim.x + i]);
+        result[k] = block_reduce<false>(acc, sh);
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+// p_new = z + beta * p_old (p_new = z on the first iteration); one helper so every thread
+// computing a given entry gets the same bits.
+template <typename T>
+__device__ __forceinline__ T direction(const T* __restrict__ z, const T* __restrict__ p_old, T beta, bool first, int i)
+{
+    return first ? z[i] : fma(beta, p_old[i], z[i]);
+}
+
+// PCG step 1: p = z + beta p_old (fused), q = A p, p.q.  Fixed grid, 16 lanes per block row,
+// a warp takes two rows per pass.
+template <typename T>
+__global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, const T* __restrict__ p_old,
+                                                           T* __restrict__ p_new, int first)
 {
     if (B.state->done) return;
-    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    __shared__ double sh[32];
+    const T beta = first ? T(0) : (T)B.state->beta;
+    const bool f = first != 0;
     const int lane16 = threadIdx.x & 15;
-    double pq = 0.0;
-    const bool valid = row < B.n_blocks;
-    T s0, s1, s2;
-    row_product<T>(valid, row, lane16, B.row_ptr, B.cols, B.vals, B.p, s0, s1, s2);
-    {
+    const int half = (threadIdx.x >> 4) & 1;
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warps_total = (gridDim.x * blockDim.x) >> 5;
+    DotAcc<T> pq;
+    for (int base = 2 * warp_global; base < B.n_blocks; base += 2 * warps_total) {
+        const int row = base + half;
+        const bool valid = row < B.n_blocks;
+        T s0 = T(0), s1 = T(0), s2 = T(0);
+        const int kb = valid ? B.row_ptr[row] : 0;
+        const int ke = valid ? B.row_ptr[row + 1] : 0;
+        for (int k = kb + lane16; k < ke; k += 16) {
+            const T* b = B.vals + (int64_t)k * 9;
+            const int c = B.cols[k];
+            const T x0 = direction(B.z, p_old, beta, f, 3 * c);
+            const T x1 = direction(B.z, p_old, beta, f, 3 * c + 1);
+            const T x2 = direction(B.z, p_old, beta, f, 3 * c + 2);
+            s0 += b[0] * x0 + b[1] * x1 + b[2] * x2;
+            s1 += b[3] * x0 + b[4] * x1 + b[5] * x2;
+            s2 += b[6] * x0 + b[7] * x1 + b[8] * x2;
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o, 16);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o, 16);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o, 16);
+        }
         if (valid && lane16 == 0) {
+            const T p0 = direction(B.z, p_old, beta, f, 3 * row);
+            const T p1 = direction(B.z, p_old, beta, f, 3 * row + 1);
+            const T p2 = direction(B.z, p_old, beta, f, 3 * row + 2);
+            p_new[3 * row] = p0;
+            p_new[3 * row + 1] = p1;
+            p_new[3 * row + 2] = p2;
             B.q[3 * row] = s0;
             B.q[3 * row + 1] = s1;
             B.q[3 * row + 2] = s2;
-            pq = (double)B.p[3 * row] * (double)s0 + (double)B.p[3 * row + 1] * (double)s1 +
-                 (double)B.p[3 * row + 2] * (double)s2;
+            pq.add_prod(p0, s0);
+            pq.add_prod(p1, s1);
+            pq.add_prod(p2, s2);
         }
     }
-    double mine[1] = {pq}, res[1];
-    if (last_block_combine<false, 1>(mine, B.partials, B.tickets, res) && threadIdx.x == 0) {
+    const double bpq[1] = {pq.block_sum(sh)};
+    double res[1];
+    if (publish_and_combine<1>(bpq, B.partials, B.tickets, res) && threadIdx.x == 0) {
         PcgState* st = B.state;
         st->pAp = res[0];
         if (!(res[0] > 0.0)) {  // indefinite (or NaN): stop as the reference does
@@ -356,20 +485,21 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B)
     }
 }
 
+// PCG step 2: x += alpha p, r -= alpha q, z = M^-1 r, r.r and r.z; convergence test and beta.
 template <typename T>
-__global__ void k_pcg_update(PcgBuffers<T> B)
+__global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __restrict__ p)
 {
     if (B.state->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double rr = 0.0, rz = 0.0;
-    if (i < B.n_blocks) {
-        const double alpha = B.state->alpha;
+    __shared__ double sh[32];
+    const T alpha = (T)B.state->alpha;
+    DotAcc<T> rr, rz;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_blocks; i += gridDim.x * blockDim.x) {
         T r[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int k = 3 * i + d;
-            B.x[k] = (T)((double)B.x[k] + alpha * (double)B.p[k]);
-            r[d] = (T)((double)B.r[k] - alpha * (double)B.q[k]);
+            B.x[k] = fma(alpha, p[k], B.x[k]);
+            r[d] = fma(-alpha, B.q[k], B.r[k]);
             B.r[k] = r[d];
         }
         const T* m = B.Dinv + (int64_t)i * 9;
@@ -377,12 +507,13 @@ __global__ void k_pcg_update(PcgBuffers<T> B)
         for (int d = 0; d < 3; ++d) {
             const T z = m[3 * d] * r[0] + m[3 * d + 1] * r[1] + m[3 * d + 2] * r[2];
             B.z[3 * i + d] = z;
-            rr += (double)r[d] * (double)r[d];
-            rz += (double)r[d] * (double)z;
+            rr.add_prod(r[d], r[d]);
+            rz.add_prod(r[d], z);
         }
     }
-    double mine[2] = {rr, rz}, res[2];
-    if (last_block_combine<false, 2>(mine, B.partials, B.tickets + 1, res) && threadIdx.x == 0) {
+    const double bv[2] = {rr.block_sum(sh), rz.block_sum(sh)};
+    double res[2];
+    if (publish_and_combine<2>(bv, B.partials, B.tickets + 1, res) && threadIdx.x == 0) {
         PcgState* st = B.state;
         st->iteration += 1;
         st->rr = res[0];
@@ -400,22 +531,14 @@ __global__ void k_pcg_update(PcgBuffers<T> B)
     }
 }
 
+// r = b = -grad (as T), x = 0, z = M^-1 r; b.b (double, from the FP64 gradient) and r.z.
 template <typename T>
-__global__ void k_pcg_direction(PcgBuffers<T> B)
+__global__ void __launch_bounds__(256) k_pcg_init(PcgBuffers<T> B, const double* __restrict__ grad)
 {
-    if (B.state->done) return;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= 3 * (int64_t)B.n_blocks) return;
-    const double beta = B.state->beta;
-    B.p[k] = (T)((double)B.z[k] + beta * (double)B.p[k]);
-}
-
-template <typename T>
-__global__ void k_pcg_init(PcgBuffers<T> B, const double* __restrict__ grad)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double bb = 0.0, rz = 0.0;
-    if (i < B.n_blocks) {
+    __shared__ double sh[32];
+    double bb = 0.0;
+    DotAcc<T> rz;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_blocks; i += gridDim.x * blockDim.x) {
         T r[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -423,19 +546,19 @@ __global__ void k_pcg_init(PcgBuffers<T> B, const double* __restrict__ grad)
             r[d] = (T)b;
             B.r[3 * i + d] = r[d];
             B.x[3 * i + d] = T(0);
-            bb += b * b;
+            bb = fma(b, b, bb);
         }
         const T* m = B.Dinv + (int64_t)i * 9;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const T z = m[3 * d] * r[0] + m[3 * d + 1] * r[1] + m[3 * d + 2] * r[2];
             B.z[3 * i + d] = z;
-            B.p[3 * i + d] = z;
-            rz += (double)r[d] * (double)z;
+            rz.add_prod(r[d], z);
         }
     }
-    double mine[2] = {bb, rz}, res[2];
-    if (last_block_combine<false, 2>(mine, B.partials, B.tickets + 2, res) && threadIdx.x == 0) {
+    const double bv[2] = {block_reduce<false>(bb, sh), rz.block_sum(sh)};
+    double res[2];
+    if (publish_and_combine<2>(bv, B.partials, B.tickets + 2, res) && threadIdx.x == 0) {
         PcgState* st = B.state;
         st->bb = res[0];
         st->rz = res[1];
@@ -545,24 +668,26 @@ void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* 
     check_launch("block_jacobi_setup");
 }
 
+constexpr unsigned kMaxPcgGrid = 152 * 8;
+
 template <typename T>
 void launch_pcg_init(const PcgBuffers<T>& B, const double* grad, cudaStream_t s)
 {
-    const unsigned g = blocks_for(B.n_blocks, 256);
-    if (g > (unsigned)kPcgMaxPartials) throw std::runtime_error("symx_gb300: system too large for the PCG partials");
+    const unsigned g = std::min<unsigned>(blocks_for(B.n_blocks, 256), kMaxPcgGrid);
     k_pcg_init<T><<<g, 256, 0, s>>>(B, grad);
     check_launch("pcg_init");
 }
 
 template <typename T>
-void launch_pcg_iteration(const PcgBuffers<T>& B, cudaStream_t s)
+void launch_pcg_iteration(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 {
-    const unsigned gs = blocks_for((int64_t)B.n_blocks * 16, kSpmvThreads);
-    if (gs > (unsigned)kPcgMaxPartials) throw std::runtime_error("symx_gb300: system too large for the PCG partials");
-    k_pcg_spmv<T><<<gs, kSpmvThreads, 0, s>>>(B);
-    k_pcg_update<T><<<blocks_for(B.n_blocks, 256), 256, 0, s>>>(B);
-    k_pcg_direction<T><<<blocks_for(3 * (int64_t)B.n_blocks, 256), 256, 0, s>>>(B);
-    count_launch(2);
+    const unsigned gs = std::min<unsigned>(blocks_for((int64_t)B.n_blocks * 16, kSpmvThreads), kMaxPcgGrid);
+    const unsigned gu = std::min<unsigned>(blocks_for(B.n_blocks, 256), kMaxPcgGrid);
+    T* p_old = (iteration & 1) ? B.p : B.p2;
+    T* p_new = (iteration & 1) ? B.p2 : B.p;
+    k_pcg_spmv<T><<<gs, kSpmvThreads, 0, s>>>(B, p_old, p_new, iteration == 0 ? 1 : 0);
+    k_pcg_update<T><<<gu, 256, 0, s>>>(B, p_new);
+    count_launch(1);
     check_launch("pcg_iteration");
 }
 
@@ -595,7 +720,7 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
     template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, cudaStream_t);      \
     template void launch_block_jacobi_setup<T>(int, const int32_t*, const T*, T*, cudaStream_t);                       \
     template void launch_pcg_init<T>(const PcgBuffers<T>&, const double*, cudaStream_t);                               \
-    template void launch_pcg_iteration<T>(const PcgBuffers<T>&, cudaStream_t);                                        \
+    template void launch_pcg_iteration<T>(const PcgBuffers<T>&, int, cudaStream_t);                                   \
     template void launch_bcsr_spmv<T>(int, const int32_t*, const int32_t*, const T*, const T*, T*, cudaStream_t);      \
     template void launch_axpy_to<T>(int64_t, const double*, double, const T*, double*, cudaStream_t);                  \
     template void launch_convert_to_double<T>(int64_t, const T*, double*, cudaStream_t);

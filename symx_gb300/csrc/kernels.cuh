@@ -74,7 +74,8 @@ struct PcgBuffers {
     T* x;
     T* r;
     T* z;
-    T* p;
+    T* p;               // search directions, ping-pong between p and p2 across iterations
+    T* p2;
     T* q;
     double* partials;   // kPcgPartials doubles x 2
     unsigned* tickets;  // 4 counters
@@ -82,13 +83,14 @@ struct PcgBuffers {
 };
 constexpr int kPcgMaxPartials = 1 << 16;
 
-// Set x = 0, r = b (b = -grad converted to T), z = M^-1 r, p = z, bb, rz, error0.
+// Set x = 0, r = b (b = -grad converted to T), z = M^-1 r, bb, rz, error0.
 template <typename T>
 void launch_pcg_init(const PcgBuffers<T>& B, const double* neg_rhs_source, cudaStream_t s);
-// One PCG iteration (SpMV + p.Ap, update + dots, direction update), each a no-op once
-// state->done is set.
+// PCG iteration number `iteration` (0-based, counted on the host): the SpMV kernel forms the
+// direction p = z + beta p_old in the ping-pong buffer and q = A p with p.q, the update kernel
+// x, r, z with r.r and r.z.  Both are no-ops once state->done is set.
 template <typename T>
-void launch_pcg_iteration(const PcgBuffers<T>& B, cudaStream_t s);
+void launch_pcg_iteration(const PcgBuffers<T>& B, int iteration, cudaStream_t s);
 
 // y = A x over a 3x3-block CSR matrix (standalone SpMV, used by tests and benchmarks).
 template <typename T>

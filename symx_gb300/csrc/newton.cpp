@@ -113,12 +113,20 @@ struct CompiledPotential {
     OpCount ops_eg, ops_h, ops_e;
     DevBuf<int32_t> conn;
     DevBuf<const double*> map_ptrs;
+    int n_cache = 0, n_qp = 1;      // hoisted values per element and quadrature point
+    DevBuf<double> cache;
     int64_t e_off = 0, g_off = 0, h_off = 0;  // offsets: elements, gradient blocks, Hessian blocks
 };
 
-std::string build_source(const CompiledPotential& cp, const Expressions& g, const std::vector<int32_t>& eg,
+// Generated source of one potential.  Besides the element kernels it contains a precompute
+// kernel: every subexpression that does not depend on a DoF (rest shape, material, the
+// quadrature point) and feeds a DoF-dependent one is evaluated once per upload into a
+// per-element cache (`n_cache` doubles per element and quadrature point), and the element
+// kernels read it instead of recomputing it at every Newton and line-search evaluation.
+std::string build_source(CompiledPotential& cp, const Expressions& g, const std::vector<int32_t>& eg,
                          const std::vector<int32_t>& h_bm, const std::vector<int32_t>& e_only, int32_t cond,
-                         const Summation& sum, OpCount* oeg, OpCount* oh, OpCount* oe)
+                         const Summation& sum, const std::vector<uint8_t>& is_dof_symbol, OpCount* oeg, OpCount* oh,
+                         OpCount* oe)
 {
     const MappedWorkspace<double>& mws = *cp.pot->mws;
     const int NS = g.n_symbols();
@@ -126,90 +134,191 @@ std::string build_source(const CompiledPotential& cp, const Expressions& g, cons
     const int NH = (int)h_bm.size();
     const int NQ = std::max(1, sum.n_iterations);
     const bool acc = sum.n_iterations > 1;
+
+    // ---- hoisting plan
+    std::vector<int32_t> roots(eg);
+    roots.insert(roots.end(), h_bm.begin(), h_bm.end());
+    roots.insert(roots.end(), e_only.begin(), e_only.end());
+    if (cond >= 0) roots.push_back(cond);
+    int32_t top = 0;
+    for (int32_t r : roots) top = std::max(top, r);
+    auto is_leaf = [&](int32_t i) {
+        const Op o = g[i].op;
+        return o == Op::Zero || o == Op::One || o == Op::Const || o == Op::Symbol;
+    };
+    std::vector<uint8_t> variant(top + 1, 0);
+    for (int32_t i = 0; i <= top; ++i) {
+        const Node& n = g[i];
+        if (n.op == Op::Symbol) variant[i] = is_dof_symbol[(int32_t)n.v];
+        else if (!is_leaf(i))
+            variant[i] = (n.a >= 0 && variant[n.a]) || (n.b >= 0 && n.op != Op::PowN && variant[n.b]) ||
+                         (n.c >= 0 && variant[n.c]);
+    }
+    std::vector<uint8_t> seen(top + 1, 0), main_symbol(NS, 0), pre_symbol(NS, 0);
+    std::vector<int32_t> frontier, stack(roots.begin(), roots.end());
+    while (!stack.empty()) {
+        const int32_t i = stack.back();
+        stack.pop_back();
+        if (seen[i]) continue;
+        seen[i] = 1;
+        const Node& n = g[i];
+        if (n.op == Op::Symbol) { main_symbol[(int32_t)n.v] = 1; continue; }
+        if (is_leaf(i)) continue;
+        if (!variant[i]) { frontier.push_back(i); continue; }
+        if (n.a >= 0) stack.push_back(n.a);
+        if (n.b >= 0 && n.op != Op::PowN) stack.push_back(n.b);
+        if (n.c >= 0) stack.push_back(n.c);
+    }
+    std::sort(frontier.begin(), frontier.end());
+    std::unordered_map<int32_t, int32_t> ext;
+    for (size_t k = 0; k < frontier.size(); ++k) ext[frontier[k]] = (int32_t)k;
+    const int K = (int)frontier.size();
+    cp.n_cache = K;
+    cp.n_qp = NQ;
+    // symbols the precompute kernel reads
+    {
+        std::vector<uint8_t> need(top + 1, 0);
+        for (int32_t f : frontier) need[f] = 1;
+        for (int32_t i = top; i >= 0; --i) {
+            if (!need[i]) continue;
+            const Node& n = g[i];
+            if (n.op == Op::Symbol) { pre_symbol[(int32_t)n.v] = 1; continue; }
+            if (is_leaf(i)) continue;
+            if (n.a >= 0) need[n.a] = 1;
+            if (n.b >= 0 && n.op != Op::PowN) need[n.b] = 1;
+            if (n.c >= 0) need[n.c] = 1;
+        }
+    }
+    auto map_used = [&](const DataMap& m, const std::vector<uint8_t>& used) {
+        for (int j = 0; j < m.stride; ++j)
+            if (used[m.first_symbol + j]) return true;
+        return false;
+    };
+    auto sum_used = [&](const std::vector<uint8_t>& used) {
+        for (int j = 0; j < sum.stride; ++j)
+            if (used[sum.first_symbol + j]) return true;
+        return false;
+    };
+
     std::ostringstream s;
     s << "// generated element kernels for potential '" << cp.name << "'\n";
+    s << "// " << K << " hoisted values per element and quadrature point\n";
     s << codegen_prelude();
-    s << emit_device_function(g, eg, "symxg_eval_eg", "double", acc, oeg);
-    s << emit_device_function(g, h_bm, "symxg_eval_h_f64", "double", acc, oh);
-    s << emit_device_function(g, h_bm, "symxg_eval_h_f32", "float", acc, nullptr);
-    s << emit_device_function(g, e_only, "symxg_eval_e", "double", acc, oe);
-    if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond", "double", false, nullptr);
+    s << emit_device_function(g, eg, "symxg_eval_eg", "double", acc, oeg, &ext);
+    s << emit_device_function(g, h_bm, "symxg_eval_h_f64", "double", acc, oh, &ext);
+    s << emit_device_function(g, h_bm, "symxg_eval_h_f32", "float", acc, nullptr, &ext);
+    s << emit_device_function(g, e_only, "symxg_eval_e", "double", acc, oe, &ext);
+    if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond", "double", false, nullptr, &ext);
+    if (K > 0) s << emit_device_function(g, frontier, "symxg_eval_pre", "double", false, nullptr, nullptr);
     if (sum.n_iterations > 0) {
         s << "static __device__ const double symxg_sum_data[" << sum.data.size() << "] = {";
         for (size_t i = 0; i < sum.data.size(); ++i) s << (i ? ", " : "") << double_literal(sum.data[i]);
         s << "};\n";
     }
-    // gather of all bound data for element e
-    s << "__device__ __forceinline__ void symxg_gather(long long e, const int* __restrict__ conn, "
-         "const double* const* __restrict__ maps, double* in)\n{\n";
-    s << "    const int* __restrict__ ce = conn + e * " << cp.conn_stride << "LL;\n";
-    for (size_t k = 0; k < mws.maps.size(); ++k) {
-        const DataMap& m = mws.maps[k];
-        s << "    { const double* __restrict__ m = maps[" << k << "]";
-        if (m.conn_column >= 0) s << " + (long long)ce[" << m.conn_column << "] * " << m.stride << "LL";
-        s << ";";
-        for (int j = 0; j < m.stride; ++j) s << " in[" << (m.first_symbol + j) << "] = m[" << j << "];";
-        s << " }\n";
-    }
-    s << "}\n";
-    auto set_sum = [&](const std::string& q) {
+    // gathers of the bound data for element e: all maps a kernel family reads
+    auto gather = [&](const std::string& fname, const std::vector<uint8_t>& used) {
+        s << "__device__ __forceinline__ void " << fname
+          << "(long long e, const int* __restrict__ conn, const double* const* __restrict__ maps, double* in)\n{\n";
+        s << "    const int* __restrict__ ce = conn + e * " << cp.conn_stride << "LL;\n    (void)ce;\n";
+        for (size_t k = 0; k < mws.maps.size(); ++k) {
+            const DataMap& m = mws.maps[k];
+            if (!map_used(m, used)) continue;
+            s << "    { const double* __restrict__ m = maps[" << k << "]";
+            if (m.conn_column >= 0) s << " + (long long)ce[" << m.conn_column << "] * " << m.stride << "LL";
+            s << ";";
+            for (int j = 0; j < m.stride; ++j) s << " in[" << (m.first_symbol + j) << "] = m[" << j << "];";
+            s << " }\n";
+        }
+        s << "}\n";
+    };
+    gather("symxg_gather", main_symbol);
+    gather("symxg_gather_pre", pre_symbol);
+    auto set_sum = [&](const std::string& q, const std::vector<uint8_t>& used) {
         std::ostringstream t;
+        if (sum.n_iterations == 0 || !sum_used(used)) return t.str();
         for (int j = 0; j < sum.stride; ++j)
             t << "        in[" << (sum.first_symbol + j) << "] = symxg_sum_data[" << q << " * " << sum.stride << " + " << j
               << "];\n";
         return t.str();
     };
+    auto load_cache = [&](const std::string& q, const std::string& T) {
+        std::ostringstream t;
+        t << "        " << T << " c[" << std::max(1, K) << "];\n";
+        if (K > 0)
+            t << "        for (int k = 0; k < " << K << "; ++k) c[k] = (" << T << ")cache[(e * " << NQ << "LL + " << q
+              << ") * " << K << "LL + k];\n";
+        else
+            t << "        c[0] = (" << T << ")0;\n";
+        return t.str();
+    };
     auto cond_check = [&](const std::string& zero_writes) {
         if (cond < 0) return std::string();
         std::ostringstream t;
-        t << "    { double c[1]; symxg_eval_cond(in, c); if (!(c[0] > 0.0)) {\n" << zero_writes << "        return; } }\n";
+        t << "    {\n" << set_sum("0", main_symbol) << load_cache("0", "double")
+          << "        double cv[1]; symxg_eval_cond(in, c, cv);\n        if (!(cv[0] > 0.0)) {\n"
+          << zero_writes << "            return;\n        }\n    }\n";
         return t.str();
     };
+    const std::string sig_common =
+        "(long long n, const int* __restrict__ conn, const double* const* __restrict__ maps, "
+        "const double* __restrict__ cache, double* __restrict__ E";
+
+    // precompute kernel
+    s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_pre(long long n, const int* __restrict__ conn, "
+         "const double* const* __restrict__ maps, double* __restrict__ cache)\n{\n";
+    s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
+    if (K > 0) {
+        s << "    double in[" << NS << "];\n    symxg_gather_pre(e, conn, maps, in);\n";
+        s << "    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q", pre_symbol);
+        s << "        symxg_eval_pre(in, nullptr, cache + (e * " << NQ << "LL + q) * " << K << "LL);\n    }\n";
+    }
+    s << "}\n";
+
     // E + g + H kernels, H in double or float
     for (int prec = 0; prec < 2; ++prec) {
         const std::string TH = prec == 0 ? "double" : "float";
         const std::string kname = prec == 0 ? "symxg_egh_f64" : "symxg_egh_f32";
-        s << "extern \"C\" __global__ void __launch_bounds__(128) " << kname
-          << "(long long n, const int* __restrict__ conn, const double* const* __restrict__ maps, "
-             "double* __restrict__ E, double* __restrict__ G, "
-          << TH << "* __restrict__ H)\n{\n";
+        s << "extern \"C\" __global__ void __launch_bounds__(128) " << kname << sig_common
+          << ", double* __restrict__ G, " << TH << "* __restrict__ H)\n{\n";
         s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
         s << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
         std::ostringstream zw;
-        zw << "        E[e] = 0.0;\n        for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = 0.0;\n"
-           << "        for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = (" << TH << ")0;\n";
-        if (sum.n_iterations > 0) s << set_sum("0");
+        zw << "            E[e] = 0.0;\n            for (int i = 0; i < " << NG << "; ++i) G[e * " << NG
+           << "LL + i] = 0.0;\n"
+           << "            for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = (" << TH << ")0;\n";
         s << cond_check(zw.str());
         s << "    double eg[" << (NG + 1) << "];\n    " << TH << " h[" << NH << "];\n";
         if (acc) {
             s << "    for (int i = 0; i < " << NG + 1 << "; ++i) eg[i] = 0.0;\n";
             s << "    for (int i = 0; i < " << NH << "; ++i) h[i] = (" << TH << ")0;\n";
-            s << "    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q");
+            s << "    for (int q = 0; q < " << NQ << "; ++q) {\n";
         } else {
-            s << "    {\n";
+            s << "    { const int q = 0; (void)q;\n";
         }
-        s << "        symxg_eval_eg(in, eg);\n";
+        s << set_sum("q", main_symbol) << load_cache("q", "double");
+        s << "        symxg_eval_eg(in, c, eg);\n";
         if (prec == 0) {
-            s << "        symxg_eval_h_f64(in, h);\n";
+            s << "        symxg_eval_h_f64(in, c, h);\n";
         } else {
-            s << "        float inf32[" << NS << "];\n        for (int i = 0; i < " << NS << "; ++i) inf32[i] = (float)in[i];\n";
-            s << "        symxg_eval_h_f32(inf32, h);\n";
+            s << "        float in32[" << NS << "], c32[" << std::max(1, K) << "];\n";
+            s << "        for (int i = 0; i < " << NS << "; ++i) in32[i] = (float)in[i];\n";
+            s << "        for (int i = 0; i < " << std::max(1, K) << "; ++i) c32[i] = (float)c[i];\n";
+            s << "        symxg_eval_h_f32(in32, c32, h);\n";
         }
         s << "    }\n";
         s << "    E[e] = eg[0];\n    for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = eg[1 + i];\n";
         s << "    for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = h[i];\n}\n";
     }
     // energy-only kernel (line search)
-    s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_e(long long n, const int* __restrict__ conn, "
-         "const double* const* __restrict__ maps, double* __restrict__ E)\n{\n";
+    s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_e" << sig_common << ")\n{\n";
     s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
     s << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
-    if (sum.n_iterations > 0) s << set_sum("0");
-    s << cond_check("        E[e] = 0.0;\n");
+    s << cond_check("            E[e] = 0.0;\n");
     s << "    double ev[1];\n";
-    if (acc) s << "    ev[0] = 0.0;\n    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q");
-    else s << "    {\n";
-    s << "        symxg_eval_e(in, ev);\n    }\n    E[e] = ev[0];\n}\n";
+    if (acc) s << "    ev[0] = 0.0;\n    for (int q = 0; q < " << NQ << "; ++q) {\n";
+    else s << "    { const int q = 0; (void)q;\n";
+    s << set_sum("q", main_symbol) << load_cache("q", "double");
+    s << "        symxg_eval_e(in, c, ev);\n    }\n    E[e] = ev[0];\n}\n";
     return s.str();
 }
 
@@ -250,8 +359,10 @@ CompiledPotential prepare_potential(const Potential& pot, const GlobalPotential&
         for (int j = 0; j < n; ++j)
             h_bm[(((i / 3) * cp.nb + (j / 3)) * 3 + (i % 3)) * 3 + (j % 3)] = hess(i, j).expr_id;
     const int32_t cond = pot.has_condition ? pot.condition.expr_id : -1;
-    cp.source = build_source(cp, g, eg, h_bm, {pot.expression.expr_id}, cond, mws.summation, &cp.ops_eg, &cp.ops_h,
-                             &cp.ops_e);
+    std::vector<uint8_t> is_dof(g.n_symbols(), 0);
+    for (const Scalar& w : wrt) is_dof[w.get_symbol_idx()] = 1;
+    cp.source = build_source(cp, g, eg, h_bm, {pot.expression.expr_id}, cond, mws.summation, is_dof, &cp.ops_eg,
+                             &cp.ops_h, &cp.ops_e);
     return cp;
 }
 
@@ -275,8 +386,8 @@ struct SolverImpl {
     int64_t nnzb = 0;
     DevBuf<float> vals32, Dinv32;
     DevBuf<double> vals64, Dinv64;
-    DevBuf<float> v32[5];
-    DevBuf<double> v64[5];
+    DevBuf<float> v32[6];
+    DevBuf<double> v64[6];
     DevBuf<double> partials, scalars;
     DevBuf<unsigned> tickets;
     DevBuf<PcgState> pcg_state;
@@ -330,15 +441,16 @@ struct SolverImpl {
             long long n = cp.n_elements;
             const int32_t* conn = cp.conn.p;
             const double* const* maps = cp.map_ptrs.p;
+            const double* cache = cp.cache.p;
             double* E = E_el.p + cp.e_off;
             const unsigned grid = (unsigned)((n + 127) / 128);
             if (mode == 2) {
-                void* args[] = {&n, &conn, &maps, &E};
+                void* args[] = {&n, &conn, &maps, &cache, &E};
                 cp.module->launch("symxg_e", dim3(grid), dim3(128), 0, stream, args);
             } else {
                 double* G = g_el.p + cp.g_off * 3;
                 void* H = mode == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
-                void* args[] = {&n, &conn, &maps, &E, &G, &H};
+                void* args[] = {&n, &conn, &maps, &cache, &E, &G, &H};
                 cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_f32", dim3(grid), dim3(128), 0, stream, args);
             }
         }
@@ -536,6 +648,7 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
         if (cp.conn.n)
             ck(cudaMemcpy(cp.conn.p, conn, sizeof(int32_t) * cp.conn.n, cudaMemcpyHostToDevice), "upload connectivity");
         cp.map_ptrs.alloc(cp.pot->mws->maps.size());
+        cp.cache.alloc(std::max<size_t>(1, (size_t)cp.n_elements * cp.n_qp * cp.n_cache));
         cp.pot->mws->verify_no_out_of_bounds();
     }
 }
@@ -598,6 +711,16 @@ void NewtonsMethod::upload()
     for (auto& a : I.arrays) {
         ck(cudaMemcpyAsync(a.dev.p, a.host, sizeof(double) * a.n, cudaMemcpyHostToDevice, I.stream), "upload data");
         bytes += (int64_t)sizeof(double) * a.n;
+    }
+    // values that depend only on the uploaded data are computed once here
+    for (auto& cp : I.pots) {
+        if (cp.n_cache == 0 || cp.n_elements == 0) continue;
+        long long n = cp.n_elements;
+        const int32_t* conn = cp.conn.p;
+        const double* const* maps = cp.map_ptrs.p;
+        double* cache = cp.cache.p;
+        void* args[] = {&n, &conn, &maps, &cache};
+        cp.module->launch("symxg_pre", dim3((unsigned)((n + 127) / 128)), dim3(128), 0, I.stream, args);
     }
     ck(cudaStreamSynchronize(I.stream), "synchronize");
     h2d_bytes_ = bytes;
@@ -735,6 +858,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     B.z = V[2].p;
     B.p = V[3].p;
     B.q = V[4].p;
+    B.p2 = V[5].p;
     B.partials = I.partials.p;
     B.tickets = I.tickets.p;
     B.state = I.pcg_state.p;
@@ -797,7 +921,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         symxg::launch_pcg_init<T>(B, I.grad.p, s);
         int launched = 0, chunk = 4;
         while (true) {
-            for (int k = 0; k < chunk; ++k) symxg::launch_pcg_iteration<T>(B, s);
+            for (int k = 0; k < chunk; ++k) symxg::launch_pcg_iteration<T>(B, launched + k, s);
             launched += chunk;
             ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
             ck(cudaStreamSynchronize(s), "synchronize");

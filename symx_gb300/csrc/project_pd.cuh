@@ -5,11 +5,14 @@
 // replaced by `eps` (or by their negation when mirroring), and the matrix is rebuilt as
 // V diag(lambda) V^T only if some eigenvalue changed.
 //
-// The eigen-decomposition is cyclic Jacobi (Golub & Van Loan, Matrix Computations,
-// Sec. 8.5) on the upper triangle, one thread per matrix, every index known at compile
-// time so that A (N(N+1)/2 values) and V (N*N values) live in registers for N = 12.
-// The number of sweeps is capped; a matrix that has not converged by then is still
-// rebuilt from the current rotation and flagged in `status`.
+// Eigen-decomposition: cyclic Jacobi (Golub & Van Loan, Matrix Computations, Sec. 8.5),
+// one thread per matrix with A (upper triangle) and V in registers.  To keep the code small
+// enough for the instruction cache while every register index stays a compile-time
+// constant, one "step" rotates the pairs (0, q), q = 1..N-1 (unrolled), and then relabels
+// the indices cyclically (i -> i-1 mod N) by register moves.  N steps bring the labels back
+// and rotate every pair twice, i.e. they are two cyclic sweeps.  Convergence is tested
+// before each such double sweep; the number of double sweeps is capped and a matrix that
+// reaches the cap is still rebuilt from the current rotation and flagged.
 //
 // Element Hessians are stored block-major: the 3x3 block (a, b) of an N x N matrix
 // (N = 3 * nb) starts at ((a * nb + b) * 9) and is row-major inside.
@@ -33,23 +36,133 @@ SYMXG_DEVICE constexpr int tri(int i, int j)
     return (i <= j) ? (i * N - (i * (i - 1)) / 2 + (j - i)) : (j * N - (j * (j - 1)) / 2 + (i - j));
 }
 
-template <typename T>
-struct JacobiTol;
 // Stop when the off-diagonal Frobenius norm is below 32 ulp of the matrix norm: rotations
 // leave rounding-level off-diagonal entries behind, so a tighter test would never pass.
+template <typename T>
+struct JacobiTol;
 template <>
 struct JacobiTol<float> {
     static SYMXG_DEVICE float rel2() { return 1.4551915e-11f; }  // (32 * 2^-23)^2
-    static constexpr int max_sweeps = 15;
+    static constexpr int max_double_sweeps = 8;
 };
 template <>
 struct JacobiTol<double> {
     static SYMXG_DEVICE double rel2() { return 5.048709793414476e-29; }  // (32 * 2^-52)^2
-    static constexpr int max_sweeps = 20;
+    static constexpr int max_double_sweeps = 10;
 };
 
 template <typename T>
 SYMXG_DEVICE T sq(T x) { return x * x; }
+
+// tan of the Jacobi angle that zeroes a_pq: t = 2 a_pq sgn(d) / (|d| + sqrt(d^2 + 4 a_pq^2)),
+// d = a_qq - a_pp; t = 0 when a_pq = 0.  This form cannot overflow.
+SYMXG_DEVICE float jacobi_t(float app, float aqq, float apq)
+{
+    const float d = aqq - app;
+    const float r = d * d + 4.0f * apq * apq;
+    const float den = fabsf(d) + (r > 0.0f ? r * rsqrtf(r) : 0.0f);
+    const float num = 2.0f * apq * (d >= 0.0f ? 1.0f : -1.0f);
+    return den > 0.0f ? num * __frcp_rn(den) : 0.0f;
+}
+SYMXG_DEVICE double jacobi_t(double app, double aqq, double apq)
+{
+    const double d = aqq - app;
+    const double r = d * d + 4.0 * apq * apq;
+    const double den = fabs(d) + sqrt(r);
+    const double num = 2.0 * apq * (d >= 0.0 ? 1.0 : -1.0);
+    return den > 0.0 ? num / den : 0.0;
+}
+SYMXG_DEVICE float inv_hypot1(float t) { return rsqrtf(1.0f + t * t); }
+SYMXG_DEVICE double inv_hypot1(double t) { return 1.0 / sqrt(1.0 + t * t); }
+
+// Rotate the pairs (0, q), q = 1..N-1, then relabel i -> i-1 (mod N).
+template <typename T, int N>
+SYMXG_DEVICE void jacobi_step(T (&a)[N * (N + 1) / 2], T (&v)[N * N])
+{
+#pragma unroll
+    for (int q = 1; q < N; ++q) {
+        const T apq = a[tri<N>(0, q)];
+        const T app = a[tri<N>(0, 0)];
+        const T aqq = a[tri<N>(q, q)];
+        const T t = jacobi_t(app, aqq, apq);
+        const T c = inv_hypot1(t);
+        const T s = t * c;
+        a[tri<N>(0, 0)] = app - t * apq;
+        a[tri<N>(q, q)] = aqq + t * apq;
+        a[tri<N>(0, q)] = T(0);
+#pragma unroll
+        for (int k = 1; k < N; ++k) {
+            if (k == q) continue;
+            const T akp = a[tri<N>(k, 0)];
+            const T akq = a[tri<N>(k, q)];
+            a[tri<N>(k, 0)] = c * akp - s * akq;
+            a[tri<N>(k, q)] = s * akp + c * akq;
+        }
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const T vkp = v[k * N + 0];
+            const T vkq = v[k * N + q];
+            v[k * N + 0] = c * vkp - s * vkq;
+            v[k * N + q] = s * vkp + c * vkq;
+        }
+    }
+    // relabel: new index i is old index i+1 (mod N)
+    T na[N * (N + 1) / 2];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) na[tri<N>(i, j)] = a[tri<N>((i + 1) % N, (j + 1) % N)];
+#pragma unroll
+    for (int k = 0; k < N * (N + 1) / 2; ++k) a[k] = na[k];
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+        const T first = v[r * N + 0];
+#pragma unroll
+        for (int j = 0; j + 1 < N; ++j) v[r * N + j] = v[r * N + j + 1];
+        v[r * N + N - 1] = first;
+    }
+}
+
+// One classic cyclic sweep over all pairs (p, q), p < q, fully unrolled.  Used for double,
+// where the FP64 pipe, not instruction fetch, bounds the kernel and the relabeling moves of
+// jacobi_step would only add spills.
+template <typename T, int N>
+SYMXG_DEVICE void jacobi_double_sweep_cyclic(T (&a)[N * (N + 1) / 2], T (&v)[N * N])
+{
+#pragma unroll 1
+    for (int rep = 0; rep < 2; ++rep) {
+#pragma unroll
+        for (int p = 0; p < N - 1; ++p) {
+#pragma unroll
+            for (int q = p + 1; q < N; ++q) {
+                const T apq = a[tri<N>(p, q)];
+                const T app = a[tri<N>(p, p)];
+                const T aqq = a[tri<N>(q, q)];
+                const T t = jacobi_t(app, aqq, apq);
+                const T c = inv_hypot1(t);
+                const T s = t * c;
+                a[tri<N>(p, p)] = app - t * apq;
+                a[tri<N>(q, q)] = aqq + t * apq;
+                a[tri<N>(p, q)] = T(0);
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    if (k == p || k == q) continue;
+                    const T akp = a[tri<N>(k, p)];
+                    const T akq = a[tri<N>(k, q)];
+                    a[tri<N>(k, p)] = c * akp - s * akq;
+                    a[tri<N>(k, q)] = s * akp + c * akq;
+                }
+#pragma unroll
+                for (int k = 0; k < N; ++k) {
+                    const T vkp = v[k * N + p];
+                    const T vkq = v[k * N + q];
+                    v[k * N + p] = c * vkp - s * vkq;
+                    v[k * N + q] = s * vkp + c * vkq;
+                }
+            }
+        }
+    }
+}
 
 // Project the matrix H (block-major, N x N) in place.  Returns 1 if the matrix changed,
 // and sets *not_converged when the sweep cap was reached.
@@ -74,48 +187,22 @@ SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, in
 #pragma unroll
         for (int j = i; j < N; ++j) fro2 += (i == j ? T(1) : T(2)) * sq(a[tri<N>(i, j)]);
 
-    int sweep = 0;
-    for (; sweep < JacobiTol<T>::max_sweeps; ++sweep) {
+    int ds = 0;
+    for (; ds < JacobiTol<T>::max_double_sweeps; ++ds) {
         T off = T(0);
 #pragma unroll
         for (int p = 0; p < N; ++p)
 #pragma unroll
             for (int q = p + 1; q < N; ++q) off += sq(a[tri<N>(p, q)]);
         if (!(off > JacobiTol<T>::rel2() * fro2)) break;
-#pragma unroll
-        for (int p = 0; p < N - 1; ++p) {
-#pragma unroll
-            for (int q = p + 1; q < N; ++q) {
-                const T apq = a[tri<N>(p, q)];
-                const T app = a[tri<N>(p, p)];
-                const T aqq = a[tri<N>(q, q)];
-                const T tau = (aqq - app) / (T(2) * apq);
-                T t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
-                t = (apq != T(0)) ? t : T(0);
-                const T c = T(1) / sqrt(T(1) + t * t);
-                const T s = t * c;
-                a[tri<N>(p, p)] = app - t * apq;
-                a[tri<N>(q, q)] = aqq + t * apq;
-                a[tri<N>(p, q)] = T(0);
-#pragma unroll
-                for (int k = 0; k < N; ++k) {
-                    if (k == p || k == q) continue;
-                    const T akp = a[tri<N>(k, p)];
-                    const T akq = a[tri<N>(k, q)];
-                    a[tri<N>(k, p)] = c * akp - s * akq;
-                    a[tri<N>(k, q)] = s * akp + c * akq;
-                }
-#pragma unroll
-                for (int k = 0; k < N; ++k) {
-                    const T vkp = v[k * N + p];
-                    const T vkq = v[k * N + q];
-                    v[k * N + p] = c * vkp - s * vkq;
-                    v[k * N + q] = s * vkp + c * vkq;
-                }
-            }
+        if (sizeof(T) == 4) {
+#pragma unroll 1
+            for (int step = 0; step < N; ++step) jacobi_step<T, N>(a, v);
+        } else {
+            jacobi_double_sweep_cyclic<T, N>(a, v);
         }
     }
-    if (sweep == JacobiTol<T>::max_sweeps && not_converged) *not_converged = 1;
+    if (ds == JacobiTol<T>::max_double_sweeps && not_converged) *not_converged = 1;
 
     bool changed = false;
     T lam[N];

@@ -69,6 +69,8 @@ int32_t Expressions::add(Op op, int32_t a, int32_t b, int32_t c, double v)
             if (a == 0) return b;
             if (b == 0) return a;
             if (is_const(a) && is_const(b)) return constant(cv(a) + cv(b));
+            if (nodes_[b].op == Op::Neg) return add(Op::Sub, a, nodes_[b].a);
+            if (nodes_[a].op == Op::Neg) return add(Op::Sub, b, nodes_[a].a);
             break;
         case Op::Sub:
             if (b == 0) return a;
@@ -81,11 +83,16 @@ int32_t Expressions::add(Op op, int32_t a, int32_t b, int32_t c, double v)
             if (a == 1) return b;
             if (b == 1) return a;
             if (is_const(a) && is_const(b)) return constant(cv(a) * cv(b));
+            if (is_const(a) && cv(a) == -1.0) return add(Op::Neg, b);
+            if (is_const(b) && cv(b) == -1.0) return add(Op::Neg, a);
             break;
         case Op::Div:
             if (b == 1) return a;
             if (a == 0) return 0;
             if (is_const(a) && is_const(b)) return constant(cv(a) / cv(b));
+            // a / b with a non-constant denominator becomes a * (1 / b): every quotient by the
+            // same b then shares one reciprocal (divisions are the costliest FP64 operation).
+            if (!is_const(b) && a != 1) return add(Op::Mul, a, add(Op::Div, 1, b));
             break;
         case Op::Neg:
             if (a == 0) return 0;
@@ -607,9 +614,10 @@ int32_t d_node(Expressions& g, int32_t f, int32_t wrt, DiffCache& cache)
         case Op::Neg: r = g.add(Op::Neg, D(n.a)); break;
         case Op::Mul: r = add(mul(D(n.a), n.b), mul(n.a, D(n.b))); break;
         case Op::Div: {
-            // d(a/b) = (da - (a/b) db) / b
+            // d(a/b) = (da - (a/b) db) / b; for the shared reciprocal f = 1/b: -f f db
             const int32_t da = D(n.a), db = D(n.b);
-            r = div(sub(da, mul(f, db)), n.b);
+            if (n.a == 1) r = g.add(Op::Neg, mul(mul(f, f), db));
+            else r = div(sub(da, mul(f, db)), n.b);
             break;
         }
         case Op::PowN: {
