@@ -111,13 +111,13 @@ def spmv_roofline(solver, torch, sg, n_rep=30):
     dev = torch.device("cuda")
     rp_t = torch.tensor(rp, device=dev)
     cols_t = torch.tensor(cols, device=dev)
-    vals_t = torch.tensor(vals, dtype=torch.float32, device=dev)
+    vals_t = sg.component_major(torch.tensor(vals, dtype=torch.float32, device=dev))
     n = 3 * (rp.size - 1)
     x = torch.randn(n, dtype=torch.float32, device=dev)
     y = torch.zeros_like(x)
     stream = torch.cuda.current_stream()
     for _ in range(3):
-        sg.bcsr_spmv(rp_t, cols_t, vals_t, x, y)
+        sg.bcsr_spmv(rp_t, cols_t, vals_t, x, y)  # warm-up
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2
     times = []
     for _ in range(n_rep):
@@ -129,7 +129,7 @@ def spmv_roofline(solver, torch, sg, n_rep=30):
         b.record(stream)
         torch.cuda.synchronize()
         times.append(a.elapsed_time(b) * 1e-3)
-    nnzb, nb = cols.size, rp.size - 1
+    nnzb, nb = cols.size, rp.size - 1  # vals_t is (9, nnzb): component-major
     algo_bytes = nnzb * (9 * 4 + 4) + (nb + 1) * 4 + n * 4 + n * 4
     t = statistics.median(times)
     return {"nnzb": int(nnzb), "n_block_rows": int(nb), "algorithmic_bytes": int(algo_bytes), "seconds": t}
@@ -145,7 +145,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     p = problems.step_problem(args.config)
     solver = sg.ElasticSolver(p)
-    solver.set_settings(cg_rel_tolerance=1e-3, precision="mixed")
+    # time_kernels: CUDA events around every PCG SpMV / projection launch (roofline, live)
+    solver.set_settings(cg_rel_tolerance=1e-3, precision="mixed", time_kernels=1)
 
     def device_solve(precision):
         solver.set_settings(precision=precision)
@@ -213,7 +214,22 @@ def run_ours(args):
 
     peak, peak_kind = measured_peaks()
     rf = spmv_roofline(solver, torch, sg)
-    achieved = rf["algorithmic_bytes"] / rf["seconds"] / 1e9
+    achieved_standalone = rf["algorithmic_bytes"] / rf["seconds"] / 1e9
+    # live PCG SpMV launches of the timed solves: p = z + beta p_old fused, so z and p_old are
+    # read and p_new and q written (4 vectors) besides the matrix
+    n3 = 3 * rf["n_block_rows"]
+    spmv_bytes = rf["nnzb"] * (9 * 4 + 4) + (rf["n_block_rows"] + 1) * 4 + 4 * n3 * 4
+    n_spmv = sum(x["spmv_launches"] for x in stats)
+    t_spmv = sum(x["spmv_seconds"] for x in stats) / max(1, n_spmv)
+    achieved = spmv_bytes / t_spmv / 1e9 if n_spmv else achieved_standalone
+    n_proj = sum(x["project_launches"] for x in stats)
+    t_proj = sum(x["project_seconds"] for x in stats) / max(1, n_proj)
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            traffic = json.load(f).get("k_pcg_spmv<float>", {}).get(args.config)
+    except (OSError, ValueError):
+        traffic = None
     rel_vs_fp64 = float(np.linalg.norm(x_mixed - x_fp64) / np.linalg.norm(x_fp64))
     out = {
         "metric": METRIC,
@@ -245,10 +261,17 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(e2e_st["h2d_bytes"]), "d2h_bytes_per_step": int(e2e_st["d2h_bytes"])},
         "gpu_launches": int((lc1 - lc0) / max(1, args.steps)),
         "gpu_launches_total": int(lc1 - lc0),
-        "roofline": {"kernel": "k_bcsr_spmv<float> (PCG SpMV, standalone launch on the assembled Hessian)",
+        "roofline": {"kernel": "k_pcg_spmv<float> (PCG SpMV with fused direction update, live in the timed solves)",
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "algorithmic_bytes": rf["algorithmic_bytes"], "launch_seconds": rf["seconds"], "traffic": None},
+                     "algorithmic_bytes": int(spmv_bytes), "launch_seconds": t_spmv, "launches": int(n_spmv),
+                     "traffic": traffic},
+        "spmv_standalone": {"kernel": "k_bcsr_spmv<float>", "algorithmic_bytes": rf["algorithmic_bytes"],
+                            "launch_seconds": rf["seconds"], "achieved_gbs": round(achieved_standalone, 1),
+                            "frac": round(achieved_standalone / peak, 4)},
+        "projection": {"kernel": "k_project_pd_unrolled<float,12>", "launch_seconds": t_proj, "launches": int(n_proj),
+                       "matrices_per_launch": int(p["conn"].shape[0]),
+                       "ns_per_matrix": round(t_proj / p["conn"].shape[0] * 1e9, 3) if n_proj else None},
         "clocks": clocks.summary(),
     }
     if args.cpu_baseline:
@@ -256,21 +279,29 @@ def run_ours(args):
     return out
 
 
+def oracle_settings(O, n_newton):
+    kw = dict(cg_rel_tolerance=1e-3)
+    if n_newton > 0:
+        kw.update(max_iterations=n_newton, max_iterations_as_success=1)
+    return O.default_settings(**kw)
+
+
 def cpu_baseline(p, args):
-    """The oracle restatement of the reference's CPU path on this host's cores, on a bounded
-    sample of the same workload: the first `n` Newton iterations of the same solve."""
+    """The oracle restatement of the reference's CPU path on this host's cores, on the same
+    solve (all Newton iterations unless --cpu-newton-iterations bounds it)."""
     from oracle import oracle as O
 
     n = args.cpu_newton_iterations
     P = O.Problem(p, 0)
     threads = O.lib().oracle_num_threads()
     P.set_x(p["x_init"])
-    st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, max_iterations=n, max_iterations_as_success=1))
+    st = P.solve(oracle_settings(O, n))
     its = max(1, st["newton_iterations"])
+    what = "the complete" if n <= 0 else f"the first {its} Newton iterations of the"
     return {"value": round(st["t_total"] * 1e3 / its, 3), "unit": UNIT + " per Newton step", "cores": threads,
             "kind": "port",
-            "sample": f"first {its} Newton iterations of the same tet4_64 solve (oracle port, OpenMP), "
-                      f"{st['t_total']:.1f} s; cg {st['cg_iterations']}",
+            "sample": f"{what} tet4_64 solve (oracle port, OpenMP): {its} Newton / {st['cg_iterations']} CG "
+                      f"iterations in {st['t_total']:.1f} s",
             "stage_seconds": {k: round(st[k], 3) for k in ("t_eval", "t_project", "t_assembly", "t_linear_solve",
                                                             "t_line_search")}}
 
@@ -311,22 +342,26 @@ def run_reference(args):
     P = O.Problem(p, 0)
     threads = O.lib().oracle_num_threads()
     n = args.cpu_newton_iterations
-    per_step = []
+    per_step, per_solve, its = [], [], 1
     for i in range(args.warmup + args.steps):
         P.set_x(p["x_init"])
-        st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, max_iterations=n, max_iterations_as_success=1))
+        # warm-up steps run a single Newton iteration (they only touch the memory)
+        st = P.solve(oracle_settings(O, 1 if i < args.warmup else n))
         if i >= args.warmup:
-            per_step.append(st["t_total"] * 1e3 / max(1, st["newton_iterations"]))
+            its = max(1, st["newton_iterations"])
+            per_step.append(st["t_total"] * 1e3 / its)
+            per_solve.append(st["t_total"] * 1e3)
     v = statistics.mean(per_step)
     return {
         "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT + " per Newton step",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v * n, 3),
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(per_solve), 3),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded 64^3 Tet4 cube)",
         "config": {"workload": "Neo-Hookean Tet4 implicit-Euler step, 64^3 cells (274,625 vertices, 1,572,864 tets)",
                    "name": args.config},
         "cpu_baseline": {"value": round(v, 3), "unit": UNIT + " per Newton step", "cores": threads, "kind": "port",
-                         "sample": f"each step: the first {n} Newton iterations of the same solve, from the same state"},
+                         "sample": ("each step: the complete solve" if n <= 0 else f"each step: the first {n} Newton "
+                                    f"iterations of the solve") + f" from the same state ({its} Newton iterations)"},
         "e2e": {"value": round(v, 3), "unit": UNIT + " per Newton step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -339,7 +374,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="tet4_64")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--cpu-newton-iterations", type=int, default=2)
+    ap.add_argument("--cpu-newton-iterations", type=int, default=0, help="0: the complete solve")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--profile-solve", choices=["mixed", "fp64"], default=None)
     args = ap.parse_args()

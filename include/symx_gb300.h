@@ -89,6 +89,7 @@ typedef struct symxg_newton_settings {
     double cg_rel_tolerance;
     double bailout_residual;
     int32_t precision;               /* SYMXG_PRECISION_* */
+    int32_t time_kernels;            /* 1: record CUDA events around PCG SpMV and projection launches */
 } symxg_newton_settings;
 
 typedef struct symxg_solve_stats {
@@ -106,6 +107,10 @@ typedef struct symxg_solve_stats {
     double t_evaluate_P;
     int64_t h2d_bytes;               /* host->device bytes of the last upload */
     int64_t d2h_bytes;               /* device->host bytes of the last download */
+    int64_t spmv_launches;           /* with time_kernels: PCG SpMV launches that did work ... */
+    double spmv_seconds;             /* ... and their summed device time */
+    int64_t project_launches;        /* with time_kernels: 12x12 projection launches ... */
+    double project_seconds;          /* ... and their summed device time */
 } symxg_solve_stats;
 
 /* message of the last failing call on this thread ("" if none) */
@@ -161,12 +166,14 @@ int symxg_project_pd_f32(float* matrices, int32_t n, int64_t count, float eps, i
                          int32_t* not_converged, void* stream);
 int symxg_project_pd_f64(double* matrices, int32_t n, int64_t count, double eps, int32_t mirroring,
                          int32_t* not_converged, void* stream);
-/* y = A x for a 3x3-block CSR matrix (row_ptr n_blocks+1, cols nnzb, vals nnzb*9 row-major
- * blocks).  Replaces BlockedSparseMatrix::spmxv_from_ptr (BlockedSparseMatrix.h:986-1138). */
+/* y = A x for a 3x3-block CSR matrix: row_ptr (n_blocks+1), cols (nnzb) and values stored
+ * component-major, i.e. component m (row-major inside the 3x3 block) of block k at
+ * vals[m * vals_stride + k], vals_stride >= nnzb (the layout the solver's PCG uses).
+ * Replaces BlockedSparseMatrix::spmxv_from_ptr (BlockedSparseMatrix.h:986-1138). */
 int symxg_bcsr_spmv_f32(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
-                        const float* x, float* y, void* stream);
+                        int64_t vals_stride, const float* x, float* y, void* stream);
 int symxg_bcsr_spmv_f64(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const double* vals,
-                        const double* x, double* y, void* stream);
+                        int64_t vals_stride, const double* x, double* y, void* stream);
 
 #ifdef __cplusplus
 }

@@ -13,7 +13,7 @@ import numpy as np
 from . import capi
 from .capi import PRECISION_FP64, PRECISION_MIXED, SOLVER_RETURN, SymxgError, check, load
 
-__all__ = ["ElasticSolver", "load", "check", "SymxgError", "PRECISION_FP64", "PRECISION_MIXED",
+__all__ = ["ElasticSolver", "load", "check", "SymxgError", "PRECISION_FP64", "PRECISION_MIXED", "component_major",
            "SOLVER_RETURN", "project_pd", "bcsr_spmv"]
 
 
@@ -180,12 +180,18 @@ def project_pd(H, eps=1e-10, mirroring=False, stream=None):
     return bool(flag.item())
 
 
-def bcsr_spmv(row_ptr, cols, vals, x, y, stream=None):
-    """y = A x on CUDA torch tensors (row_ptr int32, cols int32, vals (nnzb,3,3), x/y (3*nb,))."""
+def component_major(vals):
+    """(nnzb, 3, 3) block values -> the (9, nnzb) component-major layout of the BCSR kernels."""
+    return vals.reshape(vals.shape[0], 9).t().contiguous()
+
+
+def bcsr_spmv(row_ptr, cols, vals_cm, x, y, stream=None):
+    """y = A x on CUDA torch tensors: row_ptr/cols int32, vals_cm (9, nnzb) component-major
+    (see component_major), x/y (3 * n_block_rows,)."""
     import torch
 
     L = load()
     s = C.c_void_p(stream if stream is not None else torch.cuda.current_stream(x.device).cuda_stream)
-    f = L.symxg_bcsr_spmv_f32 if vals.dtype == torch.float32 else L.symxg_bcsr_spmv_f64
+    f = L.symxg_bcsr_spmv_f32 if vals_cm.dtype == torch.float32 else L.symxg_bcsr_spmv_f64
     check(f(row_ptr.numel() - 1, C.c_void_p(row_ptr.data_ptr()), C.c_void_p(cols.data_ptr()),
-            C.c_void_p(vals.data_ptr()), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), s))
+            C.c_void_p(vals_cm.data_ptr()), vals_cm.stride(0), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), s))

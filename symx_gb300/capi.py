@@ -50,7 +50,7 @@ class NewtonSettings(C.Structure):
         ("project_to_pd", C.c_int32), ("projection_eps", C.c_double),
         ("project_to_pd_use_mirroring", C.c_int32), ("cg_max_iterations", C.c_int32),
         ("cg_abs_tolerance", C.c_double), ("cg_rel_tolerance", C.c_double),
-        ("bailout_residual", C.c_double), ("precision", C.c_int32),
+        ("bailout_residual", C.c_double), ("precision", C.c_int32), ("time_kernels", C.c_int32),
     ]
 
 
@@ -62,6 +62,8 @@ class SolveStats(C.Structure):
         ("t_project_to_PD", C.c_double), ("t_assembly", C.c_double),
         ("t_linear_system_solve", C.c_double), ("t_evaluate_P", C.c_double),
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+        ("spmv_launches", C.c_int64), ("spmv_seconds", C.c_double),
+        ("project_launches", C.c_int64), ("project_seconds", C.c_double),
     ]
 
     def as_dict(self):
@@ -109,8 +111,8 @@ def load(path: str | None = None):
         "symxg_op_counts": ([P, I32, P], C.c_int),
         "symxg_project_pd_f32": ([P, I32, I64, C.c_float, I32, P, P], C.c_int),
         "symxg_project_pd_f64": ([P, I32, I64, D, I32, P, P], C.c_int),
-        "symxg_bcsr_spmv_f32": ([I32, P, P, P, P, P, P], C.c_int),
-        "symxg_bcsr_spmv_f64": ([I32, P, P, P, P, P, P], C.c_int),
+        "symxg_bcsr_spmv_f32": ([I32, P, P, P, I64, P, P, P], C.c_int),
+        "symxg_bcsr_spmv_f64": ([I32, P, P, P, I64, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -74,12 +74,13 @@ static int project_impl(T* m, int32_t n, int64_t count, T eps, int32_t mirroring
 }
 
 template <typename T>
-static int spmv_impl(int32_t nb, const int32_t* rp, const int32_t* cols, const T* vals, const T* x, T* y, void* stream)
+static int spmv_impl(int32_t nb, const int32_t* rp, const int32_t* cols, const T* vals, int64_t vs, const T* x, T* y,
+                     void* stream)
 {
     return guarded([&] {
-        if (nb < 0) throw std::invalid_argument("negative size");
+        if (nb < 0 || vs < 0) throw std::invalid_argument("negative size");
         if (nb > 0 && (!rp || !cols || !vals || !x || !y)) throw std::invalid_argument("null device pointer");
-        if (nb > 0) symxg::launch_bcsr_spmv<T>(nb, rp, cols, vals, x, y, (cudaStream_t)stream);
+        if (nb > 0) symxg::launch_bcsr_spmv<T>(nb, rp, cols, vals, vs, x, y, (cudaStream_t)stream);
         return SYMXG_OK;
     });
 }
@@ -106,6 +107,15 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
     o->t_evaluate_P = get("evaluate_P");
     o->h2d_bytes = st.h2d_bytes;
     o->d2h_bytes = st.d2h_bytes;
+    for (const auto& kv : st.kernels) {
+        if (kv.first.rfind("pcg_spmv", 0) == 0) {
+            o->spmv_launches += kv.second.first;
+            o->spmv_seconds += kv.second.second;
+        } else if (kv.first.rfind("project_pd", 0) == 0) {
+            o->project_launches += kv.second.first;
+            o->project_seconds += kv.second.second;
+        }
+    }
 }
 
 extern "C" {
@@ -135,6 +145,7 @@ void symxg_default_settings(symxg_newton_settings* s)
     s->cg_rel_tolerance = d.cg_rel_tolerance;
     s->bailout_residual = d.bailout_residual;
     s->precision = SYMXG_PRECISION_FP64;
+    s->time_kernels = 0;
 }
 
 int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, symxg_solver** out)
@@ -262,6 +273,7 @@ int symxg_set_settings(symxg_solver* s, const symxg_newton_settings* c)
         t.cg_rel_tolerance = c->cg_rel_tolerance;
         t.bailout_residual = c->bailout_residual;
         t.precision = c->precision == SYMXG_PRECISION_MIXED ? symx::Precision::Mixed : symx::Precision::FP64;
+        t.time_kernels = c->time_kernels != 0;
         return SYMXG_OK;
     });
 }
@@ -390,15 +402,15 @@ int symxg_project_pd_f64(double* m, int32_t n, int64_t count, double eps, int32_
     return project_impl<double>(m, n, count, eps, mirroring, nc, stream);
 }
 
-int symxg_bcsr_spmv_f32(int32_t nb, const int32_t* rp, const int32_t* cols, const float* vals, const float* x, float* y,
-                        void* stream)
+int symxg_bcsr_spmv_f32(int32_t nb, const int32_t* rp, const int32_t* cols, const float* vals, int64_t vs, const float* x,
+                        float* y, void* stream)
 {
-    return spmv_impl<float>(nb, rp, cols, vals, x, y, stream);
+    return spmv_impl<float>(nb, rp, cols, vals, vs, x, y, stream);
 }
-int symxg_bcsr_spmv_f64(int32_t nb, const int32_t* rp, const int32_t* cols, const double* vals, const double* x,
-                        double* y, void* stream)
+int symxg_bcsr_spmv_f64(int32_t nb, const int32_t* rp, const int32_t* cols, const double* vals, int64_t vs,
+                        const double* x, double* y, void* stream)
 {
-    return spmv_impl<double>(nb, rp, cols, vals, x, y, stream);
+    return spmv_impl<double>(nb, rp, cols, vals, vs, x, y, stream);
 }
 
 }  // extern "C"

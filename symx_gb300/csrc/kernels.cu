@@ -17,6 +17,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
+#include <type_traits>
+#include <unordered_map>
 #include <stdexcept>
 #include <string>
 
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
 // ---------------------------------------------------------------- assembly
 template <typename T>
 __global__ void k_assemble_blocks(int64_t nnzb, const int64_t* __restrict__ slot_ptr, const int32_t* __restrict__ contrib,
-                                  const T* __restrict__ blocks, T* __restrict__ vals)
+                                  const T* __restrict__ blocks, T* __restrict__ vals, int64_t vstride)
 {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nnzb) return;
@@ -231,7 +234,7 @@ __global__ void k_assemble_blocks(int64_t nnzb, const int64_t* __restrict__ slot
         for (int k = 0; k < 9; ++k) acc[k] += b[k];
     }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) vals[s * 9 + k] = acc[k];
+    for (int k = 0; k < 9; ++k) vals[k * vstride + s] = acc[k];
 }
 
 __global__ void k_gather_gradient(int n_blocks, const int64_t* __restrict__ ptr, const int32_t* __restrict__ contrib,
@@ -254,13 +257,14 @@ __global__ void k_gather_gradient(int n_blocks, const int64_t* __restrict__ ptr,
 // ---------------------------------------------------------------- block Jacobi
 template <typename T>
 __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ diag_slot, const T* __restrict__ vals,
-                                     T* __restrict__ Dinv)
+                                     int64_t vstride, T* __restrict__ Dinv)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_blocks) return;
-    const T* m = vals + (int64_t)diag_slot[r] * 9;
+    const int64_t k = diag_slot[r];
     // symmetric 3x3 inverse from the upper triangle (cofactors / determinant)
-    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[8];
+    const double a = vals[k], b = vals[vstride + k], c = vals[2 * vstride + k], d = vals[4 * vstride + k],
+                 e = vals[5 * vstride + k], f = vals[8 * vstride + k];
     const double c00 = d * f - e * e, c01 = c * e - b * f, c02 = b * e - c * d;
     const double det = a * c00 + b * c01 + c * c02;
     const double id = 1.0 / det;
@@ -279,47 +283,72 @@ __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ d
 // ---------------------------------------------------------------- SpMV / PCG
 constexpr int kSpmvThreads = 256;  // 16 rows per block, 16 lanes per row
 
-// Partial product of one block row over the lanes of a 16-lane group, reduced across the
-// group in a fixed butterfly order.  Every lane of the warp must call it (rows past the end
-// pass valid = false and contribute zeros), so the full-mask shuffles are always converged.
-template <typename T>
-__device__ __forceinline__ void row_product(bool valid, int row, int lane16, const int32_t* __restrict__ row_ptr,
-                                            const int32_t* __restrict__ cols, const T* __restrict__ vals,
-                                            const T* __restrict__ x, T& s0, T& s1, T& s2)
+// BCSR storage: the nine components of 3x3 block k (row-major inside the block) are
+// vals[m * vstride + k], m = 0..8 (component-major), so each load of a half-warp reads 16
+// consecutive values.
+//
+// Products of two block rows at once, each over the 16 lanes of its half-warp, lane-strided
+// over the row's blocks; both rows' loads are in flight together.  xv(c, d) is component d of
+// the multiplied vector at block column c.  The sums are reduced across the 16 lanes in a
+// fixed butterfly order; every lane of the warp must call this (rows past the end pass
+// valid = false), so the full-mask shuffles are converged.
+template <typename T, typename XV>
+__device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bool vB, int lane16,
+                                                 const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                                                 const T* __restrict__ vals, int64_t vs, XV xv, T (&a)[3], T (&b)[3])
 {
-    s0 = s1 = s2 = T(0);
-    const int kb = valid ? row_ptr[row] : 0;
-    const int ke = valid ? row_ptr[row + 1] : 0;
-    for (int k = kb + lane16; k < ke; k += 16) {
-        const T* b = vals + (int64_t)k * 9;
-        const int c = cols[k];
-        const T x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
-        s0 += b[0] * x0 + b[1] * x1 + b[2] * x2;
-        s1 += b[3] * x0 + b[4] * x1 + b[5] * x2;
-        s2 += b[6] * x0 + b[7] * x1 + b[8] * x2;
+    a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = T(0);
+    const int kbA = vA ? row_ptr[rowA] : 0, keA = vA ? row_ptr[rowA + 1] : 0;
+    const int kbB = vB ? row_ptr[rowB] : 0, keB = vB ? row_ptr[rowB + 1] : 0;
+    for (int i = lane16;; i += 16) {
+        const int kA = kbA + i, kB = kbB + i;
+        const bool hA = kA < keA, hB = kB < keB;
+        if (!hA && !hB) break;
+        if (hA) {
+            const int c = cols[kA];
+            const T x0 = xv(c, 0), x1 = xv(c, 1), x2 = xv(c, 2);
+            a[0] += vals[kA] * x0 + vals[vs + kA] * x1 + vals[2 * vs + kA] * x2;
+            a[1] += vals[3 * vs + kA] * x0 + vals[4 * vs + kA] * x1 + vals[5 * vs + kA] * x2;
+            a[2] += vals[6 * vs + kA] * x0 + vals[7 * vs + kA] * x1 + vals[8 * vs + kA] * x2;
+        }
+        if (hB) {
+            const int c = cols[kB];
+            const T x0 = xv(c, 0), x1 = xv(c, 1), x2 = xv(c, 2);
+            b[0] += vals[kB] * x0 + vals[vs + kB] * x1 + vals[2 * vs + kB] * x2;
+            b[1] += vals[3 * vs + kB] * x0 + vals[4 * vs + kB] * x1 + vals[5 * vs + kB] * x2;
+            b[2] += vals[6 * vs + kB] * x0 + vals[7 * vs + kB] * x1 + vals[8 * vs + kB] * x2;
+        }
     }
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o, 16);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o, 16);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o, 16);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            a[d] += __shfl_xor_sync(0xffffffffu, a[d], o, 16);
+            b[d] += __shfl_xor_sync(0xffffffffu, b[d], o, 16);
+        }
     }
 }
 
+// y = A x; each warp takes four block rows per pass (two per half-warp).
 template <typename T>
 __global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const int32_t* __restrict__ row_ptr,
                                                             const int32_t* __restrict__ cols, const T* __restrict__ vals,
-                                                            const T* __restrict__ x, T* __restrict__ y)
+                                                            int64_t vs, const T* __restrict__ x, T* __restrict__ y)
 {
-    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
     const int lane16 = threadIdx.x & 15;
-    const bool valid = row < n_blocks;
-    T s0, s1, s2;
-    row_product<T>(valid, row, lane16, row_ptr, cols, vals, x, s0, s1, s2);
-    if (valid && lane16 == 0) {
-        y[3 * row] = s0;
-        y[3 * row + 1] = s1;
-        y[3 * row + 2] = s2;
+    const int half = (threadIdx.x >> 4) & 1;
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warps_total = (gridDim.x * blockDim.x) >> 5;
+    auto xv = [x](int c, int d) { return x[3 * c + d]; };
+    for (int base = 4 * warp_global; base < n_blocks; base += 4 * warps_total) {
+        const int rowA = base + half, rowB = base + 2 + half;
+        const bool vA = rowA < n_blocks, vB = rowB < n_blocks;
+        T a[3], b[3];
+        two_row_products<T>(rowA, vA, rowB, vB, lane16, row_ptr, cols, vals, vs, xv, a, b);
+        if (lane16 == 0) {
+            if (vA) { y[3 * rowA] = a[0]; y[3 * rowA + 1] = a[1]; y[3 * rowA + 2] = a[2]; }
+            if (vB) { y[3 * rowB] = b[0]; y[3 * rowB + 1] = b[1]; y[3 * rowB + 2] = b[2]; }
+        }
     }
 }
 
@@ -417,8 +446,8 @@ __device__ __forceinline__ T direction(const T* __restrict__ z, const T* __restr
     return first ? z[i] : fma(beta, p_old[i], z[i]);
 }
 
-// PCG step 1: p = z + beta p_old (fused), q = A p, p.q.  Fixed grid, 16 lanes per block row,
-// a warp takes two rows per pass.
+// PCG step 1: p = z + beta p_old (fused), q = A p, p.q.  Grid sized to the resident
+// blocks; each warp takes four block rows per pass.
 template <typename T>
 __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, const T* __restrict__ p_old,
                                                            T* __restrict__ p_new, int first)
@@ -431,42 +460,28 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, cons
     const int half = (threadIdx.x >> 4) & 1;
     const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int warps_total = (gridDim.x * blockDim.x) >> 5;
+    const T* __restrict__ z = B.z;
+    auto pv = [z, p_old, beta, f](int c, int d) { return direction(z, p_old, beta, f, 3 * c + d); };
     DotAcc<T> pq;
-    for (int base = 2 * warp_global; base < B.n_blocks; base += 2 * warps_total) {
-        const int row = base + half;
-        const bool valid = row < B.n_blocks;
-        T s0 = T(0), s1 = T(0), s2 = T(0);
-        const int kb = valid ? B.row_ptr[row] : 0;
-        const int ke = valid ? B.row_ptr[row + 1] : 0;
-        for (int k = kb + lane16; k < ke; k += 16) {
-            const T* b = B.vals + (int64_t)k * 9;
-            const int c = B.cols[k];
-            const T x0 = direction(B.z, p_old, beta, f, 3 * c);
-            const T x1 = direction(B.z, p_old, beta, f, 3 * c + 1);
-            const T x2 = direction(B.z, p_old, beta, f, 3 * c + 2);
-            s0 += b[0] * x0 + b[1] * x1 + b[2] * x2;
-            s1 += b[3] * x0 + b[4] * x1 + b[5] * x2;
-            s2 += b[6] * x0 + b[7] * x1 + b[8] * x2;
-        }
+    for (int base = 4 * warp_global; base < B.n_blocks; base += 4 * warps_total) {
+        const int rowA = base + half, rowB = base + 2 + half;
+        const bool vA = rowA < B.n_blocks, vB = rowB < B.n_blocks;
+        T a[3], b[3];
+        two_row_products<T>(rowA, vA, rowB, vB, lane16, B.row_ptr, B.cols, B.vals, B.vals_stride, pv, a, b);
+        if (lane16 == 0) {
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) {
-            s0 += __shfl_xor_sync(0xffffffffu, s0, o, 16);
-            s1 += __shfl_xor_sync(0xffffffffu, s1, o, 16);
-            s2 += __shfl_xor_sync(0xffffffffu, s2, o, 16);
-        }
-        if (valid && lane16 == 0) {
-            const T p0 = direction(B.z, p_old, beta, f, 3 * row);
-            const T p1 = direction(B.z, p_old, beta, f, 3 * row + 1);
-            const T p2 = direction(B.z, p_old, beta, f, 3 * row + 2);
-            p_new[3 * row] = p0;
-            p_new[3 * row + 1] = p1;
-            p_new[3 * row + 2] = p2;
-            B.q[3 * row] = s0;
-            B.q[3 * row + 1] = s1;
-            B.q[3 * row + 2] = s2;
-            pq.add_prod(p0, s0);
-            pq.add_prod(p1, s1);
-            pq.add_prod(p2, s2);
+            for (int rr = 0; rr < 2; ++rr) {
+                const int row = rr ? rowB : rowA;
+                if (!(rr ? vB : vA)) continue;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const T pd = pv(row, d);
+                    const T qd = rr ? b[d] : a[d];
+                    p_new[3 * row + d] = pd;
+                    B.q[3 * row + d] = qd;
+                    pq.add_prod(pd, qd);
+                }
+            }
         }
     }
     const double bpq[1] = {pq.block_sum(sh)};
@@ -509,6 +524,83 @@ __global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __
             B.z[3 * i + d] = z;
             rr.add_prod(r[d], r[d]);
             rz.add_prod(r[d], z);
+        }
+    }
+    const double bv[2] = {rr.block_sum(sh), rz.block_sum(sh)};
+    double res[2];
+    if (publish_and_combine<2>(bv, B.partials, B.tickets + 1, res) && threadIdx.x == 0) {
+        PcgState* st = B.state;
+        st->iteration += 1;
+        st->rr = res[0];
+        st->error = sqrt(res[0] / st->bb);
+        if (st->error < st->abs_tol || st->error / st->error0 < st->rel_tol) {
+            st->converged = 1;
+            st->done = 1;
+        } else if (st->iteration >= st->max_iterations) {
+            st->converged = 0;
+            st->done = 1;
+        } else {
+            st->beta = res[1] / st->rz;
+            st->rz = res[1];
+        }
+    }
+}
+
+// Float PCG step 2 on four block rows per thread with 16-byte loads: the vectors are padded
+// to a multiple of four block rows (zero tails), so rows 4t..4t+3 are 12 consecutive floats
+// (three float4) and their preconditioner blocks 36 floats (nine float4).
+__global__ void __launch_bounds__(256) k_pcg_update_f32x4(PcgBuffers<float> B, const float* __restrict__ p)
+{
+    if (B.state->done) return;
+    __shared__ double sh[32];
+    const float alpha = (float)B.state->alpha;
+    DotAcc<float> rr, rz;
+    const int groups = B.n_pad / 4;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < groups; t += gridDim.x * blockDim.x) {
+        float xs[12], ps[12], rs[12], qs[12], zs[12], m[36];
+        const float4* X4 = reinterpret_cast<const float4*>(B.x) + 3 * t;
+        const float4* P4 = reinterpret_cast<const float4*>(p) + 3 * t;
+        const float4* R4 = reinterpret_cast<const float4*>(B.r) + 3 * t;
+        const float4* Q4 = reinterpret_cast<const float4*>(B.q) + 3 * t;
+        const float4* M4 = reinterpret_cast<const float4*>(B.Dinv) + 9 * t;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float4 a = X4[j], b = P4[j], c = R4[j], d = Q4[j];
+            xs[4 * j] = a.x; xs[4 * j + 1] = a.y; xs[4 * j + 2] = a.z; xs[4 * j + 3] = a.w;
+            ps[4 * j] = b.x; ps[4 * j + 1] = b.y; ps[4 * j + 2] = b.z; ps[4 * j + 3] = b.w;
+            rs[4 * j] = c.x; rs[4 * j + 1] = c.y; rs[4 * j + 2] = c.z; rs[4 * j + 3] = c.w;
+            qs[4 * j] = d.x; qs[4 * j + 1] = d.y; qs[4 * j + 2] = d.z; qs[4 * j + 3] = d.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const float4 a = M4[j];
+            m[4 * j] = a.x; m[4 * j + 1] = a.y; m[4 * j + 2] = a.z; m[4 * j + 3] = a.w;
+        }
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+            xs[k] = fmaf(alpha, ps[k], xs[k]);
+            rs[k] = fmaf(-alpha, qs[k], rs[k]);
+        }
+#pragma unroll
+        for (int row = 0; row < 4; ++row)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float* mm = m + 9 * row + 3 * d;
+                zs[3 * row + d] = mm[0] * rs[3 * row] + mm[1] * rs[3 * row + 1] + mm[2] * rs[3 * row + 2];
+            }
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+            rr.add_prod(rs[k], rs[k]);
+            rz.add_prod(rs[k], zs[k]);
+        }
+        float4* Xo = reinterpret_cast<float4*>(B.x) + 3 * t;
+        float4* Ro = reinterpret_cast<float4*>(B.r) + 3 * t;
+        float4* Zo = reinterpret_cast<float4*>(B.z) + 3 * t;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            Xo[j] = make_float4(xs[4 * j], xs[4 * j + 1], xs[4 * j + 2], xs[4 * j + 3]);
+            Ro[j] = make_float4(rs[4 * j], rs[4 * j + 1], rs[4 * j + 2], rs[4 * j + 3]);
+            Zo[j] = make_float4(zs[4 * j], zs[4 * j + 1], zs[4 * j + 2], zs[4 * j + 3]);
         }
     }
     const double bv[2] = {rr.block_sum(sh), rz.block_sum(sh)};
@@ -647,10 +739,10 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
 
 template <typename T>
 void launch_assemble_blocks(int64_t nnzb, const int64_t* slot_ptr, const int32_t* contrib, const T* blocks, T* vals,
-                            cudaStream_t s)
+                            int64_t vstride, cudaStream_t s)
 {
     if (nnzb <= 0) return;
-    k_assemble_blocks<T><<<blocks_for(nnzb, 256), 256, 0, s>>>(nnzb, slot_ptr, contrib, blocks, vals);
+    k_assemble_blocks<T><<<blocks_for(nnzb, 256), 256, 0, s>>>(nnzb, slot_ptr, contrib, blocks, vals, vstride);
     check_launch("assemble");
 }
 
@@ -662,41 +754,79 @@ void launch_gather_gradient(int n_blocks, const int64_t* ptr, const int32_t* con
 }
 
 template <typename T>
-void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, T* Dinv, cudaStream_t s)
+void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, int64_t vstride, T* Dinv,
+                               cudaStream_t s)
 {
-    k_block_jacobi_setup<T><<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, diag_slot, vals, Dinv);
+    k_block_jacobi_setup<T><<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, diag_slot, vals, vstride, Dinv);
     check_launch("block_jacobi_setup");
 }
 
-constexpr unsigned kMaxPcgGrid = 152 * 8;
+// Blocks of `kernel` resident at once on the whole device (cached per kernel).
+template <typename K>
+unsigned resident_grid(K kernel, int threads)
+{
+    static std::mutex m;
+    static std::unordered_map<const void*, unsigned> cache;
+    std::lock_guard<std::mutex> lock(m);
+    auto it = cache.find((const void*)kernel);
+    if (it != cache.end()) return it->second;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    const unsigned g = (unsigned)std::max(1, sms * std::max(1, per_sm));
+    cache[(const void*)kernel] = g;
+    return g;
+}
 
 template <typename T>
 void launch_pcg_init(const PcgBuffers<T>& B, const double* grad, cudaStream_t s)
 {
-    const unsigned g = std::min<unsigned>(blocks_for(B.n_blocks, 256), kMaxPcgGrid);
+    const unsigned g = std::min<unsigned>(blocks_for(B.n_blocks, 256), resident_grid(k_pcg_init<T>, 256));
     k_pcg_init<T><<<g, 256, 0, s>>>(B, grad);
     check_launch("pcg_init");
 }
 
 template <typename T>
-void launch_pcg_iteration(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
+void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 {
-    const unsigned gs = std::min<unsigned>(blocks_for((int64_t)B.n_blocks * 16, kSpmvThreads), kMaxPcgGrid);
-    const unsigned gu = std::min<unsigned>(blocks_for(B.n_blocks, 256), kMaxPcgGrid);
+    const unsigned gs = std::min<unsigned>(blocks_for((int64_t)B.n_blocks * 8, kSpmvThreads),
+                                           resident_grid(k_pcg_spmv<T>, kSpmvThreads));
     T* p_old = (iteration & 1) ? B.p : B.p2;
     T* p_new = (iteration & 1) ? B.p2 : B.p;
     k_pcg_spmv<T><<<gs, kSpmvThreads, 0, s>>>(B, p_old, p_new, iteration == 0 ? 1 : 0);
-    k_pcg_update<T><<<gu, 256, 0, s>>>(B, p_new);
-    count_launch(1);
-    check_launch("pcg_iteration");
+    check_launch("pcg_spmv");
 }
 
 template <typename T>
-void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, const T* x, T* y,
-                      cudaStream_t s)
+void launch_pcg_update(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 {
-    k_bcsr_spmv<T><<<blocks_for((int64_t)n_blocks * 16, kSpmvThreads), kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols,
-                                                                                           vals, x, y);
+    T* p_new = (iteration & 1) ? B.p2 : B.p;
+    if constexpr (std::is_same<T, float>::value) {
+        const unsigned gu = std::min<unsigned>(blocks_for(B.n_pad / 4, 256), resident_grid(k_pcg_update_f32x4, 256));
+        k_pcg_update_f32x4<<<gu, 256, 0, s>>>(B, p_new);
+    } else {
+        const unsigned gu = std::min<unsigned>(blocks_for(B.n_blocks, 256), resident_grid(k_pcg_update<T>, 256));
+        k_pcg_update<T><<<gu, 256, 0, s>>>(B, p_new);
+    }
+    check_launch("pcg_update");
+}
+
+template <typename T>
+void launch_pcg_iteration(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
+{
+    launch_pcg_spmv<T>(B, iteration, s);
+    launch_pcg_update<T>(B, iteration, s);
+}
+
+template <typename T>
+void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, int64_t vstride,
+                      const T* x, T* y, cudaStream_t s)
+{
+    if (n_blocks <= 0) return;
+    const unsigned g = std::min<unsigned>(blocks_for((int64_t)n_blocks * 8, kSpmvThreads),
+                                          resident_grid(k_bcsr_spmv<T>, kSpmvThreads));
+    k_bcsr_spmv<T><<<g, kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols, vals, vstride, x, y);
     check_launch("bcsr_spmv");
 }
 
@@ -717,11 +847,13 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
 #define SYMXG_INSTANTIATE(T)                                                                                          \
     template void launch_dot_mixed<T>(const T*, const double*, int64_t, double*, unsigned*, double*, cudaStream_t);  \
     template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t);                                 \
-    template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, cudaStream_t);      \
-    template void launch_block_jacobi_setup<T>(int, const int32_t*, const T*, T*, cudaStream_t);                       \
+    template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, int64_t, cudaStream_t); \
+    template void launch_block_jacobi_setup<T>(int, const int32_t*, const T*, int64_t, T*, cudaStream_t);              \
     template void launch_pcg_init<T>(const PcgBuffers<T>&, const double*, cudaStream_t);                               \
     template void launch_pcg_iteration<T>(const PcgBuffers<T>&, int, cudaStream_t);                                   \
-    template void launch_bcsr_spmv<T>(int, const int32_t*, const int32_t*, const T*, const T*, T*, cudaStream_t);      \
+    template void launch_pcg_spmv<T>(const PcgBuffers<T>&, int, cudaStream_t);                                        \
+    template void launch_pcg_update<T>(const PcgBuffers<T>&, int, cudaStream_t);                                      \
+    template void launch_bcsr_spmv<T>(int, const int32_t*, const int32_t*, const T*, int64_t, const T*, T*, cudaStream_t); \
     template void launch_axpy_to<T>(int64_t, const double*, double, const T*, double*, cudaStream_t);                  \
     template void launch_convert_to_double<T>(int64_t, const T*, double*, cudaStream_t);
 SYMXG_INSTANTIATE(float)

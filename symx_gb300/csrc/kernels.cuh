@@ -48,11 +48,14 @@ void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, 
 template <typename T>
 void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s);
 
-// Assembly: vals[s] = sum over c in [slot_ptr[s], slot_ptr[s+1]) of blocks[contrib[c]],
-// in that fixed order (3x3 blocks, 9 values each).
+// BCSR values are stored component-major: component m (row-major inside the 3x3 block) of
+// block k is vals[m * vstride + k], vstride >= nnzb.
+//
+// Assembly: block s = sum over c in [slot_ptr[s], slot_ptr[s+1]) of blocks[contrib[c]]
+// (element blocks: 9 consecutive values, row-major), summed in that fixed order.
 template <typename T>
 void launch_assemble_blocks(int64_t nnzb, const int64_t* slot_ptr, const int32_t* contrib, const T* blocks, T* vals,
-                            cudaStream_t s);
+                            int64_t vstride, cudaStream_t s);
 // Gradient: g[3v+d] = sum over c in [ptr[v], ptr[v+1]) of gel[3*contrib[c]+d].
 void launch_gather_gradient(int n_blocks, const int64_t* ptr, const int32_t* contrib, const double* gel, double* g,
                             cudaStream_t s);
@@ -60,16 +63,19 @@ void launch_gather_gradient(int n_blocks, const int64_t* ptr, const int32_t* con
 // Block-Jacobi: Dinv[r] = inverse of the diagonal block vals[diag_slot[r]] (computed in
 // double, stored as T).
 template <typename T>
-void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, T* Dinv, cudaStream_t s);
+void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, int64_t vstride, T* Dinv,
+                               cudaStream_t s);
 
 // PCG over a 3x3-block CSR matrix (row_ptr/cols/vals), block-Jacobi preconditioner.
 // Vectors in T, dot products accumulated in double, scalars in `state`.
 template <typename T>
 struct PcgBuffers {
     int n_blocks;
+    int n_pad;          // n_blocks rounded up to a multiple of 4; vectors hold 3*n_pad (zero tails)
     const int32_t* row_ptr;
     const int32_t* cols;
-    const T* vals;
+    const T* vals;      // component-major, stride vals_stride
+    int64_t vals_stride;
     const T* Dinv;
     T* x;
     T* r;
@@ -91,11 +97,17 @@ void launch_pcg_init(const PcgBuffers<T>& B, const double* neg_rhs_source, cudaS
 // x, r, z with r.r and r.z.  Both are no-ops once state->done is set.
 template <typename T>
 void launch_pcg_iteration(const PcgBuffers<T>& B, int iteration, cudaStream_t s);
-
-// y = A x over a 3x3-block CSR matrix (standalone SpMV, used by tests and benchmarks).
+// The two launches of launch_pcg_iteration, separately (for per-kernel timing).
 template <typename T>
-void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, const T* x, T* y,
-                      cudaStream_t s);
+void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s);
+template <typename T>
+void launch_pcg_update(const PcgBuffers<T>& B, int iteration, cudaStream_t s);
+
+// y = A x over a 3x3-block CSR matrix with component-major values (the PCG's product, as a
+// stand-alone launch).
+template <typename T>
+void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, int64_t vstride,
+                      const T* x, T* y, cudaStream_t s);
 
 // x_out = x0 + step * du (du in T, x in double)
 template <typename T>

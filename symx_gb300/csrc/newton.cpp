@@ -121,8 +121,9 @@ struct CompiledPotential {
 // Generated source of one potential.  Besides the element kernels it contains a precompute
 // kernel: every subexpression that does not depend on a DoF (rest shape, material, the
 // quadrature point) and feeds a DoF-dependent one is evaluated once per upload into a
-// per-element cache (`n_cache` doubles per element and quadrature point), and the element
-// kernels read it instead of recomputing it at every Newton and line-search evaluation.
+// per-element cache (`n_cache` doubles per element and quadrature point, stored value-major
+// so that a warp's loads are coalesced), and the element kernels read it instead of
+// recomputing it at every Newton and line-search evaluation.
 std::string build_source(CompiledPotential& cp, const Expressions& g, const std::vector<int32_t>& eg,
                          const std::vector<int32_t>& h_bm, const std::vector<int32_t>& e_only, int32_t cond,
                          const Summation& sum, const std::vector<uint8_t>& is_dof_symbol, OpCount* oeg, OpCount* oh,
@@ -154,6 +155,9 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
             variant[i] = (n.a >= 0 && variant[n.a]) || (n.b >= 0 && n.op != Op::PowN && variant[n.b]) ||
                          (n.c >= 0 && variant[n.c]);
     }
+    // Every invariant node that feeds a DoF-dependent node (or an output) gets a cache slot: the
+    // topmost invariant subexpressions, so each cached value saves as many operations as
+    // possible.
     std::vector<uint8_t> seen(top + 1, 0), main_symbol(NS, 0), pre_symbol(NS, 0);
     std::vector<int32_t> frontier, stack(roots.begin(), roots.end());
     while (!stack.empty()) {
@@ -245,8 +249,8 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
         std::ostringstream t;
         t << "        " << T << " c[" << std::max(1, K) << "];\n";
         if (K > 0)
-            t << "        for (int k = 0; k < " << K << "; ++k) c[k] = (" << T << ")cache[(e * " << NQ << "LL + " << q
-              << ") * " << K << "LL + k];\n";
+            t << "        for (int k = 0; k < " << K << "; ++k) c[k] = (" << T << ")cache[((long long)" << q << " * " << K
+              << "LL + k) * n + e];\n";
         else
             t << "        c[0] = (" << T << ")0;\n";
         return t.str();
@@ -270,7 +274,8 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
     if (K > 0) {
         s << "    double in[" << NS << "];\n    symxg_gather_pre(e, conn, maps, in);\n";
         s << "    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q", pre_symbol);
-        s << "        symxg_eval_pre(in, nullptr, cache + (e * " << NQ << "LL + q) * " << K << "LL);\n    }\n";
+        s << "        double c[" << K << "];\n        symxg_eval_pre(in, nullptr, c);\n";
+        s << "        for (int k = 0; k < " << K << "; ++k) cache[((long long)q * " << K << "LL + k) * n + e] = c[k];\n    }\n";
     }
     s << "}\n";
 
@@ -372,7 +377,8 @@ struct SolverImpl {
     cudaStream_t stream = nullptr;
     std::vector<CompiledPotential> pots;
     std::vector<UploadedArray> arrays;
-    int n_dofs = 0, n_blocks = 0;
+    int n_dofs = 0, n_blocks = 0, n_pad = 0;  // n_pad: block rows rounded up to a multiple of 4
+    int64_t vstride = 0;                        // BCSR component stride (nnzb rounded up to 32)
     std::vector<int> dof_offsets;  // doubles, per DoF set (+ total)
 
     DevBuf<double> x, x_before, grad;
@@ -408,17 +414,25 @@ struct SolverImpl {
     {
         const int k = (int)p;
         if (precision_allocated[k]) return;
-        const size_t n = 3 * (size_t)n_blocks;
+        const size_t n = 3 * (size_t)n_pad;
         if (p == Precision::Mixed) {
             H32.alloc((size_t)n_hblocks * 9);
-            vals32.alloc((size_t)nnzb * 9);
-            Dinv32.alloc((size_t)n_blocks * 9);
-            for (auto& v : v32) v.alloc(n);
+            vals32.alloc((size_t)vstride * 9);
+            Dinv32.alloc((size_t)n_pad * 9);
+            ck(cudaMemset(Dinv32.p, 0, sizeof(float) * Dinv32.n), "memset");
+            for (auto& v : v32) {
+                v.alloc(n);
+                ck(cudaMemset(v.p, 0, sizeof(float) * n), "memset");
+            }
         } else {
             H64.alloc((size_t)n_hblocks * 9);
-            vals64.alloc((size_t)nnzb * 9);
-            Dinv64.alloc((size_t)n_blocks * 9);
-            for (auto& v : v64) v.alloc(n);
+            vals64.alloc((size_t)vstride * 9);
+            Dinv64.alloc((size_t)n_pad * 9);
+            ck(cudaMemset(Dinv64.p, 0, sizeof(double) * Dinv64.n), "memset");
+            for (auto& v : v64) {
+                v.alloc(n);
+                ck(cudaMemset(v.p, 0, sizeof(double) * n), "memset");
+            }
         }
         precision_allocated[k] = true;
     }
@@ -500,6 +514,7 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     I.n_dofs = I.dof_offsets.back();
     if (I.n_dofs <= 0 || I.n_dofs % 3 != 0) throw std::runtime_error("symx: number of DoFs must be a positive multiple of 3");
     I.n_blocks = I.n_dofs / 3;
+    I.n_pad = (I.n_blocks + 3) / 4 * 4;
     const std::string cache_dir =
         context->compilation_directory.empty() ? symxg::default_cache_dir() : context->compilation_directory;
 
@@ -576,6 +591,7 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     }
     std::vector<int32_t>().swap(raw);
     I.nnzb = (int64_t)cols.size();
+    I.vstride = (I.nnzb + 31) / 32 * 32;
     auto slot_of = [&](int64_t r, int64_t c) -> int64_t {
         auto b = cols.begin() + row_ptr[r], e = cols.begin() + row_ptr[r + 1];
         return std::lower_bound(b, e, (int32_t)c) - cols.begin();
@@ -781,7 +797,7 @@ void assemble_t(SolverImpl& I, bool project, const NewtonSettings& s, int mode)
             symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)s.projection_eps,
                                         s.project_to_pd_use_mirroring, I.flags.p, I.stream);
     }
-    symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.stream);
+    symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.vstride, I.stream);
 }
 }  // namespace
 
@@ -792,18 +808,20 @@ void NewtonsMethod::assembled_hessian(bool project, int32_t* n_blocks, int64_t* 
     *n_blocks = I.n_blocks;
     *nnzb = I.nnzb;
     if (!vals) return;
+    std::vector<double> soa((size_t)I.vstride * 9);
     if (settings.precision == Precision::Mixed) {
         assemble_t<float>(I, project, settings, 1);
-        DevBuf<double> tmp;
-        tmp.alloc((size_t)I.nnzb * 9);
-        symxg::launch_convert_to_double<float>((int64_t)I.nnzb * 9, I.vals32.p, tmp.p, I.stream);
+        std::vector<float> f(soa.size());
         ck(cudaStreamSynchronize(I.stream), "synchronize");
-        ck(cudaMemcpy(vals, tmp.p, sizeof(double) * I.nnzb * 9, cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(f.data(), I.vals32.p, sizeof(float) * f.size(), cudaMemcpyDeviceToHost), "download");
+        std::copy(f.begin(), f.end(), soa.begin());
     } else {
         assemble_t<double>(I, project, settings, 0);
         ck(cudaStreamSynchronize(I.stream), "synchronize");
-        ck(cudaMemcpy(vals, I.vals64.p, sizeof(double) * I.nnzb * 9, cudaMemcpyDeviceToHost), "download");
+        ck(cudaMemcpy(soa.data(), I.vals64.p, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost), "download");
     }
+    for (int64_t k = 0; k < I.nnzb; ++k)
+        for (int m = 0; m < 9; ++m) vals[k * 9 + m] = soa[(size_t)m * I.vstride + k];
     ck(cudaMemcpy(row_ptr, I.row_ptr.p, sizeof(int32_t) * (I.n_blocks + 1), cudaMemcpyDeviceToHost), "download");
     ck(cudaMemcpy(cols, I.cols.p, sizeof(int32_t) * I.nnzb, cudaMemcpyDeviceToHost), "download");
 }
@@ -849,9 +867,11 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     DevBuf<T>* V = I.vecs<T>();
     PcgBuffers<T> B;
     B.n_blocks = I.n_blocks;
+    B.n_pad = I.n_pad;
     B.row_ptr = I.row_ptr.p;
     B.cols = I.cols.p;
     B.vals = I.vals<T>();
+    B.vals_stride = I.vstride;
     B.Dinv = I.Dinv<T>();
     B.x = V[0].p;
     B.r = V[1].p;
@@ -871,6 +891,8 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     double res0 = std::numeric_limits<double>::max();
     double E0 = 0.0, residual = 0.0;
     SolverReturn result = SolverReturn::Running;
+    struct PendingEvent { std::string name; cudaEvent_t a, b; };
+    std::vector<PendingEvent> pending_kernel_events;
     int it = -1;
     ck(cudaMemsetAsync(I.flags.p, 0, sizeof(int), s), "memset");
     while (result == SolverReturn::Running) {
@@ -899,16 +921,28 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         // projection and assembly
         if (S.projection_mode == ProjectionToPD::ProjectedNewton) {
             timer.start("project_to_PD");
-            for (auto& cp : I.pots)
+            for (auto& cp : I.pots) {
+                cudaEvent_t a = nullptr, b = nullptr;
+                const bool timed = S.time_kernels && cp.nb * 3 == 12;
+                if (timed) {
+                    cudaEventCreate(&a);
+                    cudaEventCreate(&b);
+                    cudaEventRecord(a, s);
+                }
                 symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)S.projection_eps,
                                             S.project_to_pd_use_mirroring, I.flags.p, s);
+                if (timed) {
+                    cudaEventRecord(b, s);
+                    pending_kernel_events.push_back({std::string("project_pd_12_") + (sizeof(T) == 4 ? "f32" : "f64"), a, b});
+                }
+            }
             timer.stop();
             st.n_projected_hessians += (uint64_t)I.n_elements_total;
         }
         st.n_hessians += (uint64_t)I.n_elements_total;
         timer.start("assembly");
-        symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), s);
-        symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.Dinv<T>(), s);
+        symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.vstride, s);
+        symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.vstride, I.Dinv<T>(), s);
         timer.stop();
         // linear solve: block-Jacobi PCG with the reference's forcing sequence
         timer.start("linear_system_solve");
@@ -919,9 +953,23 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         init.max_iterations = S.cg_max_iterations;
         ck(cudaMemcpyAsync(I.pcg_state.p, &init, sizeof(PcgState), cudaMemcpyHostToDevice, s), "pcg state");
         symxg::launch_pcg_init<T>(B, I.grad.p, s);
-        int launched = 0, chunk = 4;
+        int launched = 0, chunk = 8;
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spmv_ev;
         while (true) {
-            for (int k = 0; k < chunk; ++k) symxg::launch_pcg_iteration<T>(B, launched + k, s);
+            for (int k = 0; k < chunk; ++k) {
+                if (S.time_kernels) {
+                    cudaEvent_t a, b;
+                    cudaEventCreate(&a);
+                    cudaEventCreate(&b);
+                    cudaEventRecord(a, s);
+                    symxg::launch_pcg_spmv<T>(B, launched + k, s);
+                    cudaEventRecord(b, s);
+                    spmv_ev.push_back({a, b});
+                    symxg::launch_pcg_update<T>(B, launched + k, s);
+                } else {
+                    symxg::launch_pcg_iteration<T>(B, launched + k, s);
+                }
+            }
             launched += chunk;
             ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
             ck(cudaStreamSynchronize(s), "synchronize");
@@ -930,6 +978,19 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         }
         timer.stop();
         const PcgState ps = *I.h_state;
+        if (S.time_kernels) {
+            auto& kt = st.kernels[std::string("pcg_spmv_") + (sizeof(T) == 4 ? "f32" : "f64")];
+            for (size_t k = 0; k < spmv_ev.size(); ++k) {
+                if ((int)k < ps.iteration) {  // launches after convergence returned at once
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, spmv_ev[k].first, spmv_ev[k].second);
+                    kt.first += 1;
+                    kt.second += ms * 1e-3;
+                }
+                cudaEventDestroy(spmv_ev[k].first);
+                cudaEventDestroy(spmv_ev[k].second);
+            }
+        }
         st.cg_iterations += ps.iteration;
         if (verbosity > 0) std::printf("#CG: %4d | ", ps.iteration);
         if (!ps.converged) {
@@ -994,6 +1055,15 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     ck(cudaMemcpy(&nc, I.flags.p, sizeof(int), cudaMemcpyDeviceToHost), "flags");
     st.projection_not_converged = nc;
     timer.flush(st.timers);
+    for (auto& pe : pending_kernel_events) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pe.a, pe.b);
+        auto& kt = st.kernels[pe.name];
+        kt.first += 1;
+        kt.second += ms * 1e-3;
+        cudaEventDestroy(pe.a);
+        cudaEventDestroy(pe.b);
+    }
     st.newton_iterations = it;
     st.final_residual = residual;
     st.final_energy = E0;

@@ -63,6 +63,8 @@ struct NewtonSettings {
     bool cg_stop_on_indefiniteness = true;
     double bailout_residual = 1e-10;
     Precision precision = Precision::FP64;
+    // Record CUDA events around every PCG SpMV and PD-projection launch (SolveStats::kernels).
+    bool time_kernels = false;
 };
 
 struct Context {
@@ -90,6 +92,8 @@ struct SolveStats {
     int64_t d2h_bytes = 0;  // device->host bytes of the last download()
     // Device time per stage in seconds (CUDA events), with the reference's timer labels.
     std::map<std::string, double> timers;
+    // With time_kernels: per kernel name, {launches that did work, total seconds}.
+    std::map<std::string, std::pair<int64_t, double>> kernels;
 };
 
 struct SolverImpl;

@@ -10,9 +10,9 @@
 // enough for the instruction cache while every register index stays a compile-time
 // constant, one "step" rotates the pairs (0, q), q = 1..N-1 (unrolled), and then relabels
 // the indices cyclically (i -> i-1 mod N) by register moves.  N steps bring the labels back
-// and rotate every pair twice, i.e. they are two cyclic sweeps.  Convergence is tested
-// before each such double sweep; the number of double sweeps is capped and a matrix that
-// reaches the cap is still rebuilt from the current rotation and flagged.
+// and rotate every pair twice, i.e. they are two cyclic sweeps.  Convergence is tested every
+// few steps; the number of steps is capped and a matrix that reaches the cap is still rebuilt
+// from the current rotation and flagged.
 //
 // Element Hessians are stored block-major: the 3x3 block (a, b) of an N x N matrix
 // (N = 3 * nb) starts at ((a * nb + b) * 9) and is row-major inside.
@@ -187,8 +187,13 @@ SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, in
 #pragma unroll
         for (int j = i; j < N; ++j) fro2 += (i == j ? T(1) : T(2)) * sq(a[tri<N>(i, j)]);
 
-    int ds = 0;
-    for (; ds < JacobiTol<T>::max_double_sweeps; ++ds) {
+    // Convergence is tested every kGroup relabel steps (float) or every double sweep (double).
+    // The off-diagonal norm and the final V diag(lambda) V^T do not depend on the labelling,
+    // so stopping between full double sweeps is exact.
+    constexpr int kGroup = (sizeof(T) == 4) ? (N < 4 ? N : 4) : N;
+    constexpr int kMaxGroups = JacobiTol<T>::max_double_sweeps * ((N + kGroup - 1) / kGroup);
+    int grp = 0;
+    for (; grp < kMaxGroups; ++grp) {
         T off = T(0);
 #pragma unroll
         for (int p = 0; p < N; ++p)
@@ -197,12 +202,12 @@ SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, in
         if (!(off > JacobiTol<T>::rel2() * fro2)) break;
         if (sizeof(T) == 4) {
 #pragma unroll 1
-            for (int step = 0; step < N; ++step) jacobi_step<T, N>(a, v);
+            for (int step = 0; step < kGroup; ++step) jacobi_step<T, N>(a, v);
         } else {
             jacobi_double_sweep_cyclic<T, N>(a, v);
         }
     }
-    if (ds == JacobiTol<T>::max_double_sweeps && not_converged) *not_converged = 1;
+    if (grp == kMaxGroups && not_converged) *not_converged = 1;
 
     bool changed = false;
     T lam[N];

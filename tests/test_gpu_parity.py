@@ -181,7 +181,7 @@ def test_bcsr_spmv_kernel(sg, dtype):
     t = getattr(torch, dtype)
     y = torch.zeros(A.shape[0], dtype=t, device="cuda")
     sg.bcsr_spmv(torch.tensor(rp, device="cuda"), torch.tensor(cols, device="cuda"),
-                 torch.tensor(vals, dtype=t, device="cuda"), torch.tensor(x, dtype=t, device="cuda"), y)
+                 sg.component_major(torch.tensor(vals, dtype=t, device="cuda")), torch.tensor(x, dtype=t, device="cuda"), y)
     tol = 1e-12 if dtype == "float64" else 1e-5
     yr = A @ x
     assert np.max(np.abs(y.double().cpu().numpy() - yr)) <= tol * np.max(np.abs(yr))
