@@ -145,7 +145,10 @@ __global__ void __launch_bounds__(128) k_project_pd_unrolled(T* __restrict__ H, 
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= count) return;
     int nc = 0;
-    symxg_dev::project_pd_inplace<T, N>(H + m * (N * N), eps, mirroring != 0, &nc);
+    if constexpr (std::is_same<T, float>::value && N % 2 == 0)
+        symxg_dev::project_pd_inplace_packed<N>(H + m * (N * N), eps, mirroring != 0, &nc);
+    else
+        symxg_dev::project_pd_inplace<T, N>(H + m * (N * N), eps, mirroring != 0, &nc);
     if (nc) *not_converged = 1;
 }
 
@@ -255,6 +258,8 @@ __global__ void k_gather_gradient(int n_blocks, const int64_t* __restrict__ ptr,
 }
 
 // ---------------------------------------------------------------- block Jacobi
+// Dinv holds, per block row, the inverse diagonal block as three rows of four (the fourth
+// entry zero), so the preconditioner is applied with three 16-byte (float) loads.
 template <typename T>
 __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ diag_slot, const T* __restrict__ vals,
                                      int64_t vstride, T* __restrict__ Dinv)
@@ -268,30 +273,52 @@ __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ d
     const double c00 = d * f - e * e, c01 = c * e - b * f, c02 = b * e - c * d;
     const double det = a * c00 + b * c01 + c * c02;
     const double id = 1.0 / det;
-    T* o = Dinv + (int64_t)r * 9;
-    o[0] = (T)(c00 * id);
-    o[1] = (T)(c01 * id);
-    o[2] = (T)(c02 * id);
-    o[3] = o[1];
-    o[4] = (T)((a * f - c * c) * id);
-    o[5] = (T)((b * c - a * e) * id);
-    o[6] = o[2];
-    o[7] = o[5];
-    o[8] = (T)((a * d - b * b) * id);
+    const double i00 = c00 * id, i01 = c01 * id, i02 = c02 * id;
+    const double i11 = (a * f - c * c) * id, i12 = (b * c - a * e) * id, i22 = (a * d - b * b) * id;
+    T* o = Dinv + (int64_t)r * 12;
+    o[0] = (T)i00; o[1] = (T)i01; o[2] = (T)i02; o[3] = T(0);
+    o[4] = (T)i01; o[5] = (T)i11; o[6] = (T)i12; o[7] = T(0);
+    o[8] = (T)i02; o[9] = (T)i12; o[10] = (T)i22; o[11] = T(0);
 }
 
 // ---------------------------------------------------------------- SpMV / PCG
 constexpr int kSpmvThreads = 256;  // 16 rows per block, 16 lanes per row
+
+// PCG vectors hold one block row as four values (x, y, z, 0): a gathered block column is
+// one 16-byte load (float) instead of three 4-byte loads spread over 12 bytes.
+template <typename T>
+struct Row4 {
+    T x, y, z, w;
+};
+__device__ __forceinline__ Row4<float> ld4(const float* __restrict__ p)
+{
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    return Row4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Row4<double> ld4(const double* __restrict__ p)
+{
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    return Row4<double>{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, const Row4<float>& v)
+{
+    *reinterpret_cast<float4*>(p) = make_float4(v.x, v.y, v.z, v.w);
+}
+__device__ __forceinline__ void st4(double* __restrict__ p, const Row4<double>& v)
+{
+    reinterpret_cast<double2*>(p)[0] = make_double2(v.x, v.y);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v.z, v.w);
+}
 
 // BCSR storage: the nine components of 3x3 block k (row-major inside the block) are
 // vals[m * vstride + k], m = 0..8 (component-major), so each load of a half-warp reads 16
 // consecutive values.
 //
 // Products of two block rows at once, each over the 16 lanes of its half-warp, lane-strided
-// over the row's blocks; both rows' loads are in flight together.  xv(c, d) is component d of
-// the multiplied vector at block column c.  The sums are reduced across the 16 lanes in a
-// fixed butterfly order; every lane of the warp must call this (rows past the end pass
-// valid = false), so the full-mask shuffles are converged.
+// over the row's blocks; both rows' loads are in flight together.  xv(c) is the multiplied
+// vector's block row c.  The sums are reduced across the 16 lanes in a fixed butterfly order;
+// every lane of the warp must call this (rows past the end pass valid = false), so the
+// full-mask shuffles are converged.
 template <typename T, typename XV>
 __device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bool vB, int lane16,
                                                  const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
@@ -305,18 +332,16 @@ __device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bo
         const bool hA = kA < keA, hB = kB < keB;
         if (!hA && !hB) break;
         if (hA) {
-            const int c = cols[kA];
-            const T x0 = xv(c, 0), x1 = xv(c, 1), x2 = xv(c, 2);
-            a[0] += vals[kA] * x0 + vals[vs + kA] * x1 + vals[2 * vs + kA] * x2;
-            a[1] += vals[3 * vs + kA] * x0 + vals[4 * vs + kA] * x1 + vals[5 * vs + kA] * x2;
-            a[2] += vals[6 * vs + kA] * x0 + vals[7 * vs + kA] * x1 + vals[8 * vs + kA] * x2;
+            const Row4<T> v = xv(cols[kA]);
+            a[0] += vals[kA] * v.x + vals[vs + kA] * v.y + vals[2 * vs + kA] * v.z;
+            a[1] += vals[3 * vs + kA] * v.x + vals[4 * vs + kA] * v.y + vals[5 * vs + kA] * v.z;
+            a[2] += vals[6 * vs + kA] * v.x + vals[7 * vs + kA] * v.y + vals[8 * vs + kA] * v.z;
         }
         if (hB) {
-            const int c = cols[kB];
-            const T x0 = xv(c, 0), x1 = xv(c, 1), x2 = xv(c, 2);
-            b[0] += vals[kB] * x0 + vals[vs + kB] * x1 + vals[2 * vs + kB] * x2;
-            b[1] += vals[3 * vs + kB] * x0 + vals[4 * vs + kB] * x1 + vals[5 * vs + kB] * x2;
-            b[2] += vals[6 * vs + kB] * x0 + vals[7 * vs + kB] * x1 + vals[8 * vs + kB] * x2;
+            const Row4<T> v = xv(cols[kB]);
+            b[0] += vals[kB] * v.x + vals[vs + kB] * v.y + vals[2 * vs + kB] * v.z;
+            b[1] += vals[3 * vs + kB] * v.x + vals[4 * vs + kB] * v.y + vals[5 * vs + kB] * v.z;
+            b[2] += vals[6 * vs + kB] * v.x + vals[7 * vs + kB] * v.y + vals[8 * vs + kB] * v.z;
         }
     }
 #pragma unroll
@@ -329,7 +354,8 @@ __device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bo
     }
 }
 
-// y = A x; each warp takes four block rows per pass (two per half-warp).
+// y = A x (x and y with 3 values per block row, the C ABI layout); each warp takes four
+// block rows per pass (two per half-warp).
 template <typename T>
 __global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const int32_t* __restrict__ row_ptr,
                                                             const int32_t* __restrict__ cols, const T* __restrict__ vals,
@@ -339,7 +365,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const 
     const int half = (threadIdx.x >> 4) & 1;
     const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int warps_total = (gridDim.x * blockDim.x) >> 5;
-    auto xv = [x](int c, int d) { return x[3 * c + d]; };
+    auto xv = [x](int c) { return Row4<T>{x[3 * c], x[3 * c + 1], x[3 * c + 2], T(0)}; };
     for (int base = 4 * warp_global; base < n_blocks; base += 4 * warps_total) {
         const int rowA = base + half, rowB = base + 2 + half;
         const bool vA = rowA < n_blocks, vB = rowB < n_blocks;
@@ -438,12 +464,16 @@ __device__ bool publish_and_combine(const double (&blockv)[NPARTS], double* part
     return true;
 }
 
-// p_new = z + beta * p_old (p_new = z on the first iteration); one helper so every thread
-// computing a given entry gets the same bits.
+// Direction of block row i: z + beta p_old (z on the first iteration); one helper so every
+// thread computing a given row gets the same bits.
 template <typename T>
-__device__ __forceinline__ T direction(const T* __restrict__ z, const T* __restrict__ p_old, T beta, bool first, int i)
+__device__ __forceinline__ Row4<T> direction(const T* __restrict__ z, const T* __restrict__ p_old, T beta, bool first,
+                                             int i)
 {
-    return first ? z[i] : fma(beta, p_old[i], z[i]);
+    const Row4<T> zz = ld4(z + 4 * i);
+    if (first) return zz;
+    const Row4<T> pp = ld4(p_old + 4 * i);
+    return Row4<T>{fma(beta, pp.x, zz.x), fma(beta, pp.y, zz.y), fma(beta, pp.z, zz.z), T(0)};
 }
 
 // PCG step 1: p = z + beta p_old (fused), q = A p, p.q.  Grid sized to the resident
@@ -461,7 +491,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, cons
     const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int warps_total = (gridDim.x * blockDim.x) >> 5;
     const T* __restrict__ z = B.z;
-    auto pv = [z, p_old, beta, f](int c, int d) { return direction(z, p_old, beta, f, 3 * c + d); };
+    auto pv = [z, p_old, beta, f](int c) { return direction(z, p_old, beta, f, c); };
     DotAcc<T> pq;
     for (int base = 4 * warp_global; base < B.n_blocks; base += 4 * warps_total) {
         const int rowA = base + half, rowB = base + 2 + half;
@@ -473,14 +503,13 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, cons
             for (int rr = 0; rr < 2; ++rr) {
                 const int row = rr ? rowB : rowA;
                 if (!(rr ? vB : vA)) continue;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const T pd = pv(row, d);
-                    const T qd = rr ? b[d] : a[d];
-                    p_new[3 * row + d] = pd;
-                    B.q[3 * row + d] = qd;
-                    pq.add_prod(pd, qd);
-                }
+                const Row4<T> pd = pv(row);
+                const T* qd = rr ? b : a;
+                st4(p_new + 4 * row, pd);
+                st4(B.q + 4 * row, Row4<T>{qd[0], qd[1], qd[2], T(0)});
+                pq.add_prod(pd.x, qd[0]);
+                pq.add_prod(pd.y, qd[1]);
+                pq.add_prod(pd.z, qd[2]);
             }
         }
     }
@@ -500,6 +529,16 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, cons
     }
 }
 
+// z = M^-1 r for one block row
+template <typename T>
+__device__ __forceinline__ Row4<T> apply_block_jacobi(const T* __restrict__ Dinv, int i, const Row4<T>& r)
+{
+    const Row4<T> m0 = ld4(Dinv + 12 * (int64_t)i), m1 = ld4(Dinv + 12 * (int64_t)i + 4),
+                  m2 = ld4(Dinv + 12 * (int64_t)i + 8);
+    return Row4<T>{m0.x * r.x + m0.y * r.y + m0.z * r.z, m1.x * r.x + m1.y * r.y + m1.z * r.z,
+                   m2.x * r.x + m2.y * r.y + m2.z * r.z, T(0)};
+}
+
 // PCG step 2: x += alpha p, r -= alpha q, z = M^-1 r, r.r and r.z; convergence test and beta.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __restrict__ p)
@@ -509,99 +548,24 @@ __global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __
     const T alpha = (T)B.state->alpha;
     DotAcc<T> rr, rz;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_blocks; i += gridDim.x * blockDim.x) {
-        T r[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const int k = 3 * i + d;
-            B.x[k] = fma(alpha, p[k], B.x[k]);
-            r[d] = fma(-alpha, B.q[k], B.r[k]);
-            B.r[k] = r[d];
-        }
-        const T* m = B.Dinv + (int64_t)i * 9;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const T z = m[3 * d] * r[0] + m[3 * d + 1] * r[1] + m[3 * d + 2] * r[2];
-            B.z[3 * i + d] = z;
-            rr.add_prod(r[d], r[d]);
-            rz.add_prod(r[d], z);
-        }
-    }
-    const double bv[2] = {rr.block_sum(sh), rz.block_sum(sh)};
-    double res[2];
-    if (publish_and_combine<2>(bv, B.partials, B.tickets + 1, res) && threadIdx.x == 0) {
-        PcgState* st = B.state;
-        st->iteration += 1;
-        st->rr = res[0];
-        st->error = sqrt(res[0] / st->bb);
-        if (st->error < st->abs_tol || st->error / st->error0 < st->rel_tol) {
-            st->converged = 1;
-            st->done = 1;
-        } else if (st->iteration >= st->max_iterations) {
-            st->converged = 0;
-            st->done = 1;
-        } else {
-            st->beta = res[1] / st->rz;
-            st->rz = res[1];
-        }
-    }
-}
-
-// Float PCG step 2 on four block rows per thread with 16-byte loads: the vectors are padded
-// to a multiple of four block rows (zero tails), so rows 4t..4t+3 are 12 consecutive floats
-// (three float4) and their preconditioner blocks 36 floats (nine float4).
-__global__ void __launch_bounds__(256) k_pcg_update_f32x4(PcgBuffers<float> B, const float* __restrict__ p)
-{
-    if (B.state->done) return;
-    __shared__ double sh[32];
-    const float alpha = (float)B.state->alpha;
-    DotAcc<float> rr, rz;
-    const int groups = B.n_pad / 4;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < groups; t += gridDim.x * blockDim.x) {
-        float xs[12], ps[12], rs[12], qs[12], zs[12], m[36];
-        const float4* X4 = reinterpret_cast<const float4*>(B.x) + 3 * t;
-        const float4* P4 = reinterpret_cast<const float4*>(p) + 3 * t;
-        const float4* R4 = reinterpret_cast<const float4*>(B.r) + 3 * t;
-        const float4* Q4 = reinterpret_cast<const float4*>(B.q) + 3 * t;
-        const float4* M4 = reinterpret_cast<const float4*>(B.Dinv) + 9 * t;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const float4 a = X4[j], b = P4[j], c = R4[j], d = Q4[j];
-            xs[4 * j] = a.x; xs[4 * j + 1] = a.y; xs[4 * j + 2] = a.z; xs[4 * j + 3] = a.w;
-            ps[4 * j] = b.x; ps[4 * j + 1] = b.y; ps[4 * j + 2] = b.z; ps[4 * j + 3] = b.w;
-            rs[4 * j] = c.x; rs[4 * j + 1] = c.y; rs[4 * j + 2] = c.z; rs[4 * j + 3] = c.w;
-            qs[4 * j] = d.x; qs[4 * j + 1] = d.y; qs[4 * j + 2] = d.z; qs[4 * j + 3] = d.w;
-        }
-#pragma unroll
-        for (int j = 0; j < 9; ++j) {
-            const float4 a = M4[j];
-            m[4 * j] = a.x; m[4 * j + 1] = a.y; m[4 * j + 2] = a.z; m[4 * j + 3] = a.w;
-        }
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-            xs[k] = fmaf(alpha, ps[k], xs[k]);
-            rs[k] = fmaf(-alpha, qs[k], rs[k]);
-        }
-#pragma unroll
-        for (int row = 0; row < 4; ++row)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const float* mm = m + 9 * row + 3 * d;
-                zs[3 * row + d] = mm[0] * rs[3 * row] + mm[1] * rs[3 * row + 1] + mm[2] * rs[3 * row + 2];
-            }
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-            rr.add_prod(rs[k], rs[k]);
-            rz.add_prod(rs[k], zs[k]);
-        }
-        float4* Xo = reinterpret_cast<float4*>(B.x) + 3 * t;
-        float4* Ro = reinterpret_cast<float4*>(B.r) + 3 * t;
-        float4* Zo = reinterpret_cast<float4*>(B.z) + 3 * t;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            Xo[j] = make_float4(xs[4 * j], xs[4 * j + 1], xs[4 * j + 2], xs[4 * j + 3]);
-            Ro[j] = make_float4(rs[4 * j], rs[4 * j + 1], rs[4 * j + 2], rs[4 * j + 3]);
-            Zo[j] = make_float4(zs[4 * j], zs[4 * j + 1], zs[4 * j + 2], zs[4 * j + 3]);
-        }
+        Row4<T> x = ld4(B.x + 4 * i), r = ld4(B.r + 4 * i);
+        const Row4<T> pp = ld4(p + 4 * i), q = ld4(B.q + 4 * i);
+        x.x = fma(alpha, pp.x, x.x);
+        x.y = fma(alpha, pp.y, x.y);
+        x.z = fma(alpha, pp.z, x.z);
+        r.x = fma(-alpha, q.x, r.x);
+        r.y = fma(-alpha, q.y, r.y);
+        r.z = fma(-alpha, q.z, r.z);
+        const Row4<T> z = apply_block_jacobi(B.Dinv, i, r);
+        st4(B.x + 4 * i, x);
+        st4(B.r + 4 * i, r);
+        st4(B.z + 4 * i, z);
+        rr.add_prod(r.x, r.x);
+        rr.add_prod(r.y, r.y);
+        rr.add_prod(r.z, r.z);
+        rz.add_prod(r.x, z.x);
+        rz.add_prod(r.y, z.y);
+        rz.add_prod(r.z, z.z);
     }
     const double bv[2] = {rr.block_sum(sh), rz.block_sum(sh)};
     double res[2];
@@ -631,22 +595,16 @@ __global__ void __launch_bounds__(256) k_pcg_init(PcgBuffers<T> B, const double*
     double bb = 0.0;
     DotAcc<T> rz;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_blocks; i += gridDim.x * blockDim.x) {
-        T r[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const double b = -grad[3 * i + d];
-            r[d] = (T)b;
-            B.r[3 * i + d] = r[d];
-            B.x[3 * i + d] = T(0);
-            bb = fma(b, b, bb);
-        }
-        const T* m = B.Dinv + (int64_t)i * 9;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const T z = m[3 * d] * r[0] + m[3 * d + 1] * r[1] + m[3 * d + 2] * r[2];
-            B.z[3 * i + d] = z;
-            rz.add_prod(r[d], z);
-        }
+        const double b0 = -grad[3 * i], b1 = -grad[3 * i + 1], b2 = -grad[3 * i + 2];
+        bb = fma(b0, b0, fma(b1, b1, fma(b2, b2, bb)));
+        const Row4<T> r{(T)b0, (T)b1, (T)b2, T(0)};
+        const Row4<T> z = apply_block_jacobi(B.Dinv, i, r);
+        st4(B.r + 4 * i, r);
+        st4(B.x + 4 * i, Row4<T>{T(0), T(0), T(0), T(0)});
+        st4(B.z + 4 * i, z);
+        rz.add_prod(r.x, z.x);
+        rz.add_prod(r.y, z.y);
+        rz.add_prod(r.z, z.z);
     }
     const double bv[2] = {block_reduce<false>(bb, sh), rz.block_sum(sh)};
     double res[2];
@@ -668,6 +626,45 @@ __global__ void __launch_bounds__(256) k_pcg_init(PcgBuffers<T> B, const double*
             if (st->error < st->abs_tol) { st->converged = 1; st->done = 1; }
         }
     }
+}
+
+// ---- Newton helpers on the PCG solution (4 values per block row)
+template <typename T>
+__global__ void k_dot_rows4(const T* __restrict__ du, const double* __restrict__ g, int n_rows, double* partials,
+                            unsigned* ticket, double* out)
+{
+    int64_t b, e;
+    chunk_range(n_rows, b, e);
+    double acc = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x)
+        acc += (double)du[4 * i] * g[3 * i] + (double)du[4 * i + 1] * g[3 * i + 1] + (double)du[4 * i + 2] * g[3 * i + 2];
+    double mine[1] = {acc}, res[1];
+    if (last_block_combine<false, 1>(mine, partials, ticket, res) && threadIdx.x == 0) out[0] = res[0];
+}
+
+template <typename T>
+__global__ void k_max_abs_rows4(const T* __restrict__ du, int n_rows, double* partials, unsigned* ticket, double* out)
+{
+    int64_t b, e;
+    chunk_range(n_rows, b, e);
+    float acc = 0.f;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            const float v = (float)du[4 * i + d];
+            acc = fmaxf(acc, isnan(v) ? __int_as_float(0x7f800000) : fabsf(v));
+        }
+    double mine[1] = {(double)acc}, res[1];
+    if (last_block_combine<true, 1>(mine, partials, ticket, res) && threadIdx.x == 0) out[0] = res[0];
+}
+
+template <typename T>
+__global__ void k_axpy_rows4(int n_rows, const double* __restrict__ x0, double step, const T* __restrict__ du,
+                             double* __restrict__ x)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 3 * (int64_t)n_rows) return;
+    const int64_t i = k / 3, d = k - 3 * i;
+    x[k] = x0[k] + step * (double)du[4 * i + d];
 }
 
 template <typename T>
@@ -802,13 +799,8 @@ template <typename T>
 void launch_pcg_update(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 {
     T* p_new = (iteration & 1) ? B.p2 : B.p;
-    if constexpr (std::is_same<T, float>::value) {
-        const unsigned gu = std::min<unsigned>(blocks_for(B.n_pad / 4, 256), resident_grid(k_pcg_update_f32x4, 256));
-        k_pcg_update_f32x4<<<gu, 256, 0, s>>>(B, p_new);
-    } else {
-        const unsigned gu = std::min<unsigned>(blocks_for(B.n_blocks, 256), resident_grid(k_pcg_update<T>, 256));
-        k_pcg_update<T><<<gu, 256, 0, s>>>(B, p_new);
-    }
+    const unsigned gu = std::min<unsigned>(blocks_for(B.n_blocks, 256), resident_grid(k_pcg_update<T>, 256));
+    k_pcg_update<T><<<gu, 256, 0, s>>>(B, p_new);
     check_launch("pcg_update");
 }
 
@@ -828,6 +820,28 @@ void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols,
                                           resident_grid(k_bcsr_spmv<T>, kSpmvThreads));
     k_bcsr_spmv<T><<<g, kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols, vals, vstride, x, y);
     check_launch("bcsr_spmv");
+}
+
+template <typename T>
+void launch_dot_rows4(const T* du, const double* g, int n_rows, double* partials, unsigned* ticket, double* out,
+                      cudaStream_t s)
+{
+    k_dot_rows4<T><<<kReduceBlocks, kReduceThreads, 0, s>>>(du, g, n_rows, partials, ticket, out);
+    check_launch("dot_rows4");
+}
+
+template <typename T>
+void launch_max_abs_rows4(const T* du, int n_rows, double* partials, unsigned* ticket, double* out, cudaStream_t s)
+{
+    k_max_abs_rows4<T><<<kReduceBlocks, kReduceThreads, 0, s>>>(du, n_rows, partials, ticket, out);
+    check_launch("max_abs_rows4");
+}
+
+template <typename T>
+void launch_axpy_rows4(int n_rows, const double* x0, double step, const T* du, double* x_out, cudaStream_t s)
+{
+    k_axpy_rows4<T><<<blocks_for(3 * (int64_t)n_rows, 256), 256, 0, s>>>(n_rows, x0, step, du, x_out);
+    check_launch("axpy_rows4");
 }
 
 template <typename T>
@@ -855,6 +869,9 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
     template void launch_pcg_update<T>(const PcgBuffers<T>&, int, cudaStream_t);                                      \
     template void launch_bcsr_spmv<T>(int, const int32_t*, const int32_t*, const T*, int64_t, const T*, T*, cudaStream_t); \
     template void launch_axpy_to<T>(int64_t, const double*, double, const T*, double*, cudaStream_t);                  \
+    template void launch_dot_rows4<T>(const T*, const double*, int, double*, unsigned*, double*, cudaStream_t);        \
+    template void launch_max_abs_rows4<T>(const T*, int, double*, unsigned*, double*, cudaStream_t);                   \
+    template void launch_axpy_rows4<T>(int, const double*, double, const T*, double*, cudaStream_t);                   \
     template void launch_convert_to_double<T>(int64_t, const T*, double*, cudaStream_t);
 SYMXG_INSTANTIATE(float)
 SYMXG_INSTANTIATE(double)

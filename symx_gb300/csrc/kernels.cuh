@@ -68,10 +68,11 @@ void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* 
 
 // PCG over a 3x3-block CSR matrix (row_ptr/cols/vals), block-Jacobi preconditioner.
 // Vectors in T, dot products accumulated in double, scalars in `state`.
+// PCG vectors (x, r, z, p, p2, q) hold 4 values per block row (x, y, z, 0); Dinv holds
+// the inverse diagonal blocks as 3 rows of 4 (12 values per block row).
 template <typename T>
 struct PcgBuffers {
     int n_blocks;
-    int n_pad;          // n_blocks rounded up to a multiple of 4; vectors hold 3*n_pad (zero tails)
     const int32_t* row_ptr;
     const int32_t* cols;
     const T* vals;      // component-major, stride vals_stride
@@ -109,6 +110,15 @@ template <typename T>
 void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, int64_t vstride,
                       const T* x, T* y, cudaStream_t s);
 
+// On the PCG solution du (4 values per block row) and double vectors with 3 per row:
+// out = du . g;  out = max |du|;  x_out = x0 + step * du.
+template <typename T>
+void launch_dot_rows4(const T* du, const double* g, int n_rows, double* partials, unsigned* ticket, double* out,
+                      cudaStream_t s);
+template <typename T>
+void launch_max_abs_rows4(const T* du, int n_rows, double* partials, unsigned* ticket, double* out, cudaStream_t s);
+template <typename T>
+void launch_axpy_rows4(int n_rows, const double* x0, double step, const T* du, double* x_out, cudaStream_t s);
 // x_out = x0 + step * du (du in T, x in double)
 template <typename T>
 void launch_axpy_to(int64_t n, const double* x0, double step, const T* du, double* x_out, cudaStream_t s);

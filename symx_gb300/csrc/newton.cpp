@@ -377,7 +377,7 @@ struct SolverImpl {
     cudaStream_t stream = nullptr;
     std::vector<CompiledPotential> pots;
     std::vector<UploadedArray> arrays;
-    int n_dofs = 0, n_blocks = 0, n_pad = 0;  // n_pad: block rows rounded up to a multiple of 4
+    int n_dofs = 0, n_blocks = 0;
     int64_t vstride = 0;                        // BCSR component stride (nnzb rounded up to 32)
     std::vector<int> dof_offsets;  // doubles, per DoF set (+ total)
 
@@ -414,11 +414,11 @@ struct SolverImpl {
     {
         const int k = (int)p;
         if (precision_allocated[k]) return;
-        const size_t n = 3 * (size_t)n_pad;
+        const size_t n = 4 * (size_t)n_blocks;
         if (p == Precision::Mixed) {
             H32.alloc((size_t)n_hblocks * 9);
             vals32.alloc((size_t)vstride * 9);
-            Dinv32.alloc((size_t)n_pad * 9);
+            Dinv32.alloc((size_t)n_blocks * 12);
             ck(cudaMemset(Dinv32.p, 0, sizeof(float) * Dinv32.n), "memset");
             for (auto& v : v32) {
                 v.alloc(n);
@@ -427,7 +427,7 @@ struct SolverImpl {
         } else {
             H64.alloc((size_t)n_hblocks * 9);
             vals64.alloc((size_t)vstride * 9);
-            Dinv64.alloc((size_t)n_pad * 9);
+            Dinv64.alloc((size_t)n_blocks * 12);
             ck(cudaMemset(Dinv64.p, 0, sizeof(double) * Dinv64.n), "memset");
             for (auto& v : v64) {
                 v.alloc(n);
@@ -514,7 +514,6 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     I.n_dofs = I.dof_offsets.back();
     if (I.n_dofs <= 0 || I.n_dofs % 3 != 0) throw std::runtime_error("symx: number of DoFs must be a positive multiple of 3");
     I.n_blocks = I.n_dofs / 3;
-    I.n_pad = (I.n_blocks + 3) / 4 * 4;
     const std::string cache_dir =
         context->compilation_directory.empty() ? symxg::default_cache_dir() : context->compilation_directory;
 
@@ -867,7 +866,6 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     DevBuf<T>* V = I.vecs<T>();
     PcgBuffers<T> B;
     B.n_blocks = I.n_blocks;
-    B.n_pad = I.n_pad;
     B.row_ptr = I.row_ptr.p;
     B.cols = I.cols.p;
     B.vals = I.vals<T>();
@@ -997,10 +995,8 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             result = SolverReturn::LinearSystemSolveFailure;
             break;
         }
-        symxg::launch_dot_mixed<T>(du, I.grad.p, n, I.partials.p, I.tickets.p + 4, I.scalars.p + 2, s);
-        // max |du|
-        symxg::launch_convert_to_double<T>(n, du, I.x_before.p, s);
-        symxg::launch_max_abs(I.x_before.p, n, I.partials.p, I.tickets.p + 4, I.scalars.p + 3, s);
+        symxg::launch_dot_rows4<T>(du, I.grad.p, I.n_blocks, I.partials.p, I.tickets.p + 4, I.scalars.p + 2, s);
+        symxg::launch_max_abs_rows4<T>(du, I.n_blocks, I.partials.p, I.tickets.p + 4, I.scalars.p + 3, s);
         I.read_scalars(4);
         const double du_dot_grad = I.h_scalars[2];
         double du_max = I.h_scalars[3];
@@ -1023,7 +1019,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         timer.start("evaluate_P");
         ck(cudaMemcpyAsync(I.x_before.p, I.x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy");
         double step = 1.0;
-        symxg::launch_axpy_to<T>(n, I.x_before.p, step * retraction, du, I.x.p, s);
+        symxg::launch_axpy_rows4<T>(I.n_blocks, I.x_before.p, step * retraction, du, I.x.p, s);
         if (S.enable_armijo_backtracking) {
             const double expected = S.line_search_armijo_beta * du_dot_grad * retraction;
             double E_thr = E0 + expected * step;
@@ -1035,7 +1031,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
                 const double E1 = I.h_scalars[0];
                 if (E1 < E_thr) break;
                 step *= 0.5;
-                symxg::launch_axpy_to<T>(n, I.x_before.p, step * retraction, du, I.x.p, s);
+                symxg::launch_axpy_rows4<T>(I.n_blocks, I.x_before.p, step * retraction, du, I.x.p, s);
                 E_thr = E0 + expected * step;
                 st.ls_bt_iterations++;
             }

@@ -164,6 +164,127 @@ SYMXG_DEVICE void jacobi_double_sweep_cyclic(T (&a)[N * (N + 1) / 2], T (&v)[N *
     }
 }
 
+#if defined(SYMXG_PACKED_FP32X2) || (defined(__CUDACC__) && (!defined(__CUDA_ARCH__) || __CUDA_ARCH__ >= 1000))
+#define SYMXG_HAVE_PACKED_PROJECTION 1
+// float, even N, on sm_100 and later: the eigenvector matrix is held as pairs of rows in
+// float2 registers, vv[kp * N + j] = (V[2kp][j], V[2kp+1][j]), and updated with the packed
+// FP32x2 instructions (__ffma2_rn / __fmul2_rn), two rows per instruction.  Same rotations,
+// same order as jacobi_step.
+template <int N>
+SYMXG_DEVICE void jacobi_step_packed(float (&a)[N * (N + 1) / 2], float2 (&vv)[(N / 2) * N])
+{
+#pragma unroll
+    for (int q = 1; q < N; ++q) {
+        const float apq = a[tri<N>(0, q)];
+        const float app = a[tri<N>(0, 0)];
+        const float aqq = a[tri<N>(q, q)];
+        const float t = jacobi_t(app, aqq, apq);
+        const float c = inv_hypot1(t);
+        const float s = t * c;
+        a[tri<N>(0, 0)] = app - t * apq;
+        a[tri<N>(q, q)] = aqq + t * apq;
+        a[tri<N>(0, q)] = 0.0f;
+#pragma unroll
+        for (int k = 1; k < N; ++k) {
+            if (k == q) continue;
+            const float akp = a[tri<N>(k, 0)];
+            const float akq = a[tri<N>(k, q)];
+            a[tri<N>(k, 0)] = c * akp - s * akq;
+            a[tri<N>(k, q)] = s * akp + c * akq;
+        }
+        const float2 c2 = make_float2(c, c), s2 = make_float2(s, s), ns2 = make_float2(-s, -s);
+#pragma unroll
+        for (int kp = 0; kp < N / 2; ++kp) {
+            const float2 P = vv[kp * N + 0];
+            const float2 Q = vv[kp * N + q];
+            vv[kp * N + 0] = __ffma2_rn(c2, P, __fmul2_rn(ns2, Q));
+            vv[kp * N + q] = __ffma2_rn(s2, P, __fmul2_rn(c2, Q));
+        }
+    }
+    float na[N * (N + 1) / 2];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) na[tri<N>(i, j)] = a[tri<N>((i + 1) % N, (j + 1) % N)];
+#pragma unroll
+    for (int k = 0; k < N * (N + 1) / 2; ++k) a[k] = na[k];
+#pragma unroll
+    for (int kp = 0; kp < N / 2; ++kp) {
+        const float2 first = vv[kp * N + 0];
+#pragma unroll
+        for (int j = 0; j + 1 < N; ++j) vv[kp * N + j] = vv[kp * N + j + 1];
+        vv[kp * N + N - 1] = first;
+    }
+}
+
+template <int N>
+SYMXG_DEVICE int project_pd_inplace_packed(float* __restrict__ H, float eps, bool mirroring, int* not_converged)
+{
+    constexpr int NT = N * (N + 1) / 2;
+    float a[NT];
+    float2 vv[(N / 2) * N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
+#pragma unroll
+    for (int kp = 0; kp < N / 2; ++kp)
+#pragma unroll
+        for (int j = 0; j < N; ++j) vv[kp * N + j] = make_float2(j == 2 * kp ? 1.0f : 0.0f, j == 2 * kp + 1 ? 1.0f : 0.0f);
+    float fro2 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) fro2 += (i == j ? 1.0f : 2.0f) * sq(a[tri<N>(i, j)]);
+    constexpr int kGroup = N < 4 ? N : 4;
+    constexpr int kMaxGroups = JacobiTol<float>::max_double_sweeps * ((N + kGroup - 1) / kGroup);
+    int grp = 0;
+    for (; grp < kMaxGroups; ++grp) {
+        float off = 0.0f;
+#pragma unroll
+        for (int p = 0; p < N; ++p)
+#pragma unroll
+            for (int q = p + 1; q < N; ++q) off += sq(a[tri<N>(p, q)]);
+        if (!(off > JacobiTol<float>::rel2() * fro2)) break;
+#pragma unroll 1
+        for (int step = 0; step < kGroup; ++step) jacobi_step_packed<N>(a, vv);
+    }
+    if (grp == kMaxGroups && not_converged) *not_converged = 1;
+    bool changed = false;
+    float lam[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        float l = a[tri<N>(i, i)];
+        if (l < eps) {
+            changed = true;
+            l = mirroring ? -l : eps;
+        }
+        lam[i] = l;
+    }
+    if (!changed) return 0;
+    // H = V diag(lam) V^T, two rows of H per packed accumulator
+#pragma unroll
+    for (int ip = 0; ip < N / 2; ++ip)
+#pragma unroll
+        for (int j = 2 * ip; j < N; ++j) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const float2 vj = vv[(j / 2) * N + k];
+                const float w = lam[k] * ((j & 1) ? vj.y : vj.x);
+                acc = __ffma2_rn(vv[ip * N + k], make_float2(w, w), acc);
+            }
+            H[bm_index<N>(2 * ip, j)] = acc.x;
+            H[bm_index<N>(j, 2 * ip)] = acc.x;
+            if (j >= 2 * ip + 1) {
+                H[bm_index<N>(2 * ip + 1, j)] = acc.y;
+                H[bm_index<N>(j, 2 * ip + 1)] = acc.y;
+            }
+        }
+    return 1;
+}
+#endif
+
 // Project the matrix H (block-major, N x N) in place.  Returns 1 if the matrix changed,
 // and sets *not_converged when the sweep cap was reached.
 template <typename T, int N>
