@@ -175,6 +175,30 @@ int symxg_bcsr_spmv_f32(int32_t n_blocks, const int32_t* row_ptr, const int32_t*
 int symxg_bcsr_spmv_f64(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const double* vals,
                         int64_t vals_stride, const double* x, double* y, void* stream);
 
+/* Outcome of a PCG solve: the fields of bsm::PCGInfo (solve_pcg.h:21-27), plus the number of
+ * block rows without a diagonal block (nonzero: the solve did not run, call fails). */
+typedef struct symxg_pcg_info {
+    int32_t converged;
+    int32_t n_iterations;
+    double error;                  /* sqrt(r.r / b.b) at exit */
+    int32_t found_indefiniteness;  /* p.Ap <= 0 met (the solve stops there) */
+    int32_t missing_diagonal;
+} symxg_pcg_info;
+
+/* Solve A x = b with block-Jacobi PCG on the device: A as for symxg_bcsr_spmv_*, b and x
+ * (3 * n_blocks) device arrays, x starting at zero.  Stops when sqrt(r.r/b.b) < abs_tol, when
+ * it falls below rel_tol times its initial value, on p.Ap <= 0, or after max_iterations.
+ * Every row must hold its diagonal block.  Allocates its workspace (about 150 bytes per block
+ * row in f32, 300 in f64) on each call and returns with `stream` synchronized.  Replaces
+ * BlockedSparseMatrix::prepare_preconditioning (BlockedSparseMatrix.h:1147) followed by
+ * bsm::solve_pcg (solve_pcg.h:83-232), as NewtonsMethod.cpp:427-446 calls them. */
+int symxg_bcsr_pcg_f32(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
+                       int64_t vals_stride, const float* b, float* x, double abs_tol, double rel_tol,
+                       int32_t max_iterations, symxg_pcg_info* info, void* stream);
+int symxg_bcsr_pcg_f64(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                       int64_t vals_stride, const double* b, double* x, double abs_tol, double rel_tol,
+                       int32_t max_iterations, symxg_pcg_info* info, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

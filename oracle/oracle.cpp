@@ -461,6 +461,24 @@ void project_all(Problem& P, double eps, bool mirroring, double* t)
     if (t) *t += seconds_since(t0);
 }
 
+// Block-Jacobi preconditioner (BlockedSparseMatrix.h:1146-1278): the symmetric 3x3
+// inverse of each diagonal block via the cofactors of its upper triangle.
+void block_jacobi_setup(Problem& P)
+{
+    P.Dinv.resize((size_t)P.nv * 9);
+    for (int v = 0; v < P.nv; ++v) {
+        const double* m = &P.vals[(size_t)P.diag_slot[v] * 9];
+        const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[8];
+        const double c00 = d * f - e * e, c01 = c * e - b * f, c02 = b * e - c * d;
+        const double det = a * c00 + b * c01 + c * c02;
+        const double id = 1.0 / det;
+        double* r = &P.Dinv[(size_t)v * 9];
+        r[0] = c00 * id; r[1] = c01 * id; r[2] = c02 * id;
+        r[3] = r[1]; r[4] = (a * f - c * c) * id; r[5] = (b * c - a * e) * id;
+        r[6] = r[2]; r[7] = r[5]; r[8] = (a * d - b * b) * id;
+    }
+}
+
 void assemble(Problem& P, double* t)
 {
     auto t0 = Clock::now();
@@ -483,19 +501,7 @@ void assemble(Problem& P, double* t)
         double* blk = &P.vals[(size_t)P.diag_slot[P.bc_idx[i]] * 9];
         for (int d = 0; d < 3; ++d) blk[4 * d] += P.k_bc;
     }
-    // block-Jacobi: symmetric 3x3 inverse via cofactors of the upper triangle
-    P.Dinv.resize((size_t)P.nv * 9);
-    for (int v = 0; v < P.nv; ++v) {
-        const double* m = &P.vals[(size_t)P.diag_slot[v] * 9];
-        const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[8];
-        const double c00 = d * f - e * e, c01 = c * e - b * f, c02 = b * e - c * d;
-        const double det = a * c00 + b * c01 + c * c02;
-        const double id = 1.0 / det;
-        double* r = &P.Dinv[(size_t)v * 9];
-        r[0] = c00 * id; r[1] = c01 * id; r[2] = c02 * id;
-        r[3] = r[1]; r[4] = (a * f - c * c) * id; r[5] = (b * c - a * e) * id;
-        r[6] = r[2]; r[7] = r[5]; r[8] = (a * d - b * b) * id;
-    }
+    block_jacobi_setup(P);
     if (t) *t += seconds_since(t0);
 }
 
@@ -782,6 +788,32 @@ int oracle_solve(void* h, const oracle_settings* s, oracle_stats* st)
     st->final_residual = residual;
     st->final_energy = E0;
     st->t_total = seconds_since(t_start);
+    return 0;
+}
+
+// bsm::solve_pcg (solve_pcg.h:82-232) with the block-diagonal preconditioner on a given
+// 3x3-block CSR matrix (row-major blocks); x0 = 0.  Every row must hold its diagonal block
+// (returns -1 otherwise).
+int oracle_bcsr_pcg(int32_t n_blocks, const int32_t* rowptr, const int32_t* cols, const double* vals, const double* b,
+                    double* x, double abs_tol, double rel_tol, int32_t max_iter, int32_t* iterations,
+                    int32_t* converged)
+{
+    Problem P;
+    P.nv = n_blocks;
+    P.n_threads = 1;
+    P.rowptr.assign(rowptr, rowptr + n_blocks + 1);
+    P.cols.assign(cols, cols + rowptr[n_blocks]);
+    P.vals.assign(vals, vals + (size_t)rowptr[n_blocks] * 9);
+    P.diag_slot.assign(n_blocks, -1);
+    for (int r = 0; r < n_blocks; ++r)
+        for (int k = rowptr[r]; k < rowptr[r + 1]; ++k)
+            if (cols[k] == r) { P.diag_slot[r] = k; break; }
+    for (int r = 0; r < n_blocks; ++r)
+        if (P.diag_slot[r] < 0) return -1;
+    block_jacobi_setup(P);
+    const PCGOut o = pcg(P, x, b, abs_tol, rel_tol, max_iter);
+    *iterations = o.iters;
+    *converged = o.converged ? 1 : 0;
     return 0;
 }
 

@@ -52,6 +52,7 @@ def lib():
         L.oracle_nh_element_batch.argtypes = [C.c_int, C.c_int, P, P, P, P, P, P, P]
         L.oracle_project_pd_batch.argtypes = [C.c_int, C.c_int, P, C.c_double, C.c_int, P]
         L.oracle_num_threads.restype = C.c_int
+        L.oracle_bcsr_pcg.argtypes = [C.c_int32, P, P, P, P, P, C.c_double, C.c_double, C.c_int32, P, P]
         _lib = L
     return _lib
 
@@ -140,6 +141,23 @@ class Problem:
         st = Stats()
         lib().oracle_solve(self.h, C.byref(s), C.byref(st))
         return st.as_dict()
+
+
+def bcsr_pcg(rowptr, cols, vals, b, abs_tol, rel_tol, max_iter):
+    """bsm::solve_pcg with the block-diagonal preconditioner on a 3x3-block CSR matrix
+    (vals (nnzb, 3, 3)), x0 = 0.  Returns (x, iterations, converged)."""
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    it = np.zeros(1, dtype=np.int32)
+    conv = np.zeros(1, dtype=np.int32)
+    rc = lib().oracle_bcsr_pcg(rowptr.size - 1, _p(rowptr), _p(cols), _p(vals), _p(b), _p(x), abs_tol, rel_tol,
+                               max_iter, _p(it), _p(conv))
+    if rc != 0:
+        raise ValueError("a block row has no diagonal block")
+    return x, int(it[0]), bool(conv[0])
 
 
 def bcsr_to_dense(rowptr, cols, vals):

@@ -14,7 +14,7 @@ from . import capi
 from .capi import PRECISION_FP64, PRECISION_MIXED, SOLVER_RETURN, SymxgError, check, load
 
 __all__ = ["ElasticSolver", "load", "check", "SymxgError", "PRECISION_FP64", "PRECISION_MIXED", "component_major",
-           "SOLVER_RETURN", "project_pd", "bcsr_spmv"]
+           "SOLVER_RETURN", "project_pd", "bcsr_spmv", "bcsr_pcg"]
 
 
 def _ptr(a):
@@ -195,3 +195,19 @@ def bcsr_spmv(row_ptr, cols, vals_cm, x, y, stream=None):
     f = L.symxg_bcsr_spmv_f32 if vals_cm.dtype == torch.float32 else L.symxg_bcsr_spmv_f64
     check(f(row_ptr.numel() - 1, C.c_void_p(row_ptr.data_ptr()), C.c_void_p(cols.data_ptr()),
             C.c_void_p(vals_cm.data_ptr()), vals_cm.stride(0), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), s))
+
+
+def bcsr_pcg(row_ptr, cols, vals_cm, b, x, abs_tol=1e-10, rel_tol=1e-6, max_iterations=1000, stream=None):
+    """Solve A x = b with block-Jacobi PCG (x starts at zero) on CUDA torch tensors: A as for
+    bcsr_spmv, b/x (3 * n_block_rows,) in the dtype of vals_cm.  Returns the PcgInfo fields
+    as a dict; raises SymxgError if a block row has no diagonal block."""
+    import torch
+
+    L = load()
+    s = C.c_void_p(stream if stream is not None else torch.cuda.current_stream(x.device).cuda_stream)
+    f = L.symxg_bcsr_pcg_f32 if vals_cm.dtype == torch.float32 else L.symxg_bcsr_pcg_f64
+    info = capi.PcgInfo()
+    check(f(row_ptr.numel() - 1, C.c_void_p(row_ptr.data_ptr()), C.c_void_p(cols.data_ptr()),
+            C.c_void_p(vals_cm.data_ptr()), vals_cm.stride(0), C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
+            float(abs_tol), float(rel_tol), int(max_iterations), C.byref(info), s))
+    return info.as_dict()

@@ -27,6 +27,7 @@ EXPORTS = [
     "symxg_upload", "symxg_solve_device", "symxg_download", "symxg_evaluate", "symxg_evaluate_energy",
     "symxg_assembled_hessian", "symxg_element_outputs", "symxg_op_counts", "symxg_project_pd_f32",
     "symxg_project_pd_f64", "symxg_bcsr_spmv_f32", "symxg_bcsr_spmv_f64", "symxg_launch_count",
+    "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64",
 ]
 
 
@@ -72,6 +73,16 @@ class SolveStats(C.Structure):
         return d
 
 
+class PcgInfo(C.Structure):
+    _fields_ = [
+        ("converged", C.c_int32), ("n_iterations", C.c_int32), ("error", C.c_double),
+        ("found_indefiniteness", C.c_int32), ("missing_diagonal", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -113,6 +124,8 @@ def load(path: str | None = None):
         "symxg_project_pd_f64": ([P, I32, I64, D, I32, P, P], C.c_int),
         "symxg_bcsr_spmv_f32": ([I32, P, P, P, I64, P, P, P], C.c_int),
         "symxg_bcsr_spmv_f64": ([I32, P, P, P, I64, P, P, P], C.c_int),
+        "symxg_bcsr_pcg_f32": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
+        "symxg_bcsr_pcg_f64": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

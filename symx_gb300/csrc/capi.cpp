@@ -14,6 +14,7 @@
 
 #include <cuda_runtime.h>
 
+#include "bcsr_pcg.h"
 #include "fem.h"
 #include "global_potential.h"
 #include "kernels.cuh"
@@ -81,6 +82,38 @@ static int spmv_impl(int32_t nb, const int32_t* rp, const int32_t* cols, const T
         if (nb < 0 || vs < 0) throw std::invalid_argument("negative size");
         if (nb > 0 && (!rp || !cols || !vals || !x || !y)) throw std::invalid_argument("null device pointer");
         if (nb > 0) symxg::launch_bcsr_spmv<T>(nb, rp, cols, vals, vs, x, y, (cudaStream_t)stream);
+        return SYMXG_OK;
+    });
+}
+
+template <typename T>
+static int pcg_impl(int32_t nb, const int32_t* rp, const int32_t* cols, const T* vals, int64_t vs, const T* b, T* x,
+                    double abs_tol, double rel_tol, int32_t max_it, symxg_pcg_info* info, void* stream)
+{
+    return guarded([&] {
+        if (!info) throw std::invalid_argument("null info");
+        std::memset(info, 0, sizeof(*info));
+        if (nb < 0 || vs < 0 || max_it < 0) throw std::invalid_argument("negative size");
+        if (nb > 0 && (!rp || !cols || !vals || !b || !x)) throw std::invalid_argument("null device pointer");
+        const unsigned parts = symxg::pcg_max_grid();
+        const size_t bytes = symxg::bcsr_pcg_workspace_bytes<T>(nb, parts);
+        void* ws = nullptr;
+        if (nb > 0) {
+            const cudaError_t e = cudaMalloc(&ws, bytes);
+            if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        struct Free {
+            void* p;
+            ~Free() { if (p) cudaFree(p); }
+        } guard{ws};
+        const symxg::BcsrPcgResult r = symxg::run_bcsr_pcg<T>(nb, rp, cols, vals, vs, b, x, abs_tol, rel_tol, max_it, ws,
+                                                               bytes, parts, (cudaStream_t)stream);
+        info->converged = r.converged;
+        info->n_iterations = r.iterations;
+        info->error = r.error;
+        info->found_indefiniteness = r.indefinite;
+        info->missing_diagonal = r.missing_diagonal;
+        if (r.missing_diagonal) throw std::invalid_argument("block rows without a diagonal block");
         return SYMXG_OK;
     });
 }
@@ -411,6 +444,18 @@ int symxg_bcsr_spmv_f64(int32_t nb, const int32_t* rp, const int32_t* cols, cons
                         const double* x, double* y, void* stream)
 {
     return spmv_impl<double>(nb, rp, cols, vals, vs, x, y, stream);
+}
+
+int symxg_bcsr_pcg_f32(int32_t nb, const int32_t* rp, const int32_t* cols, const float* vals, int64_t vs, const float* b,
+                       float* x, double abs_tol, double rel_tol, int32_t max_it, symxg_pcg_info* info, void* stream)
+{
+    return pcg_impl<float>(nb, rp, cols, vals, vs, b, x, abs_tol, rel_tol, max_it, info, stream);
+}
+int symxg_bcsr_pcg_f64(int32_t nb, const int32_t* rp, const int32_t* cols, const double* vals, int64_t vs,
+                       const double* b, double* x, double abs_tol, double rel_tol, int32_t max_it, symxg_pcg_info* info,
+                       void* stream)
+{
+    return pcg_impl<double>(nb, rp, cols, vals, vs, b, x, abs_tol, rel_tol, max_it, info, stream);
 }
 
 }  // extern "C"

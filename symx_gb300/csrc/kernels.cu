@@ -628,6 +628,55 @@ __global__ void __launch_bounds__(256) k_pcg_init(PcgBuffers<T> B, const double*
     }
 }
 
+// Same as k_pcg_init for a right-hand side b given in T with 3 values per block row.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_init_rhs(PcgBuffers<T> B, const T* __restrict__ b3)
+{
+    __shared__ double sh[32];
+    double bb = 0.0;
+    DotAcc<T> rz;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.n_blocks; i += gridDim.x * blockDim.x) {
+        const Row4<T> r{b3[3 * i], b3[3 * i + 1], b3[3 * i + 2], T(0)};
+        bb = fma((double)r.x, (double)r.x, fma((double)r.y, (double)r.y, fma((double)r.z, (double)r.z, bb)));
+        const Row4<T> z = apply_block_jacobi(B.Dinv, i, r);
+        st4(B.r + 4 * i, r);
+        st4(B.x + 4 * i, Row4<T>{T(0), T(0), T(0), T(0)});
+        st4(B.z + 4 * i, z);
+        rz.add_prod(r.x, z.x);
+        rz.add_prod(r.y, z.y);
+        rz.add_prod(r.z, z.z);
+    }
+    const double bv[2] = {block_reduce<false>(bb, sh), rz.block_sum(sh)};
+    double res[2];
+    if (publish_and_combine<2>(bv, B.partials, B.tickets + 2, res) && threadIdx.x == 0) {
+        PcgState* st = B.state;
+        st->bb = res[0];
+        st->rz = res[1];
+        st->iteration = 0;
+        st->indefinite = 0;
+        st->converged = 0;
+        st->done = 0;
+        if (res[0] < st->abs_tol * st->abs_tol) {
+            st->error = 0.0;
+            st->converged = 1;
+            st->done = 1;
+        } else {
+            st->error0 = 1.0;
+            st->error = 1.0;
+            if (st->error < st->abs_tol) { st->converged = 1; st->done = 1; }
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_rows4_to_vec3(int n_rows, const T* __restrict__ in4, T* __restrict__ out3)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 3 * (int64_t)n_rows) return;
+    const int64_t i = k / 3, d = k - 3 * i;
+    out3[k] = in4[4 * i + d];
+}
+
 // ---- Newton helpers on the PCG solution (4 values per block row)
 template <typename T>
 __global__ void k_dot_rows4(const T* __restrict__ du, const double* __restrict__ g, int n_rows, double* partials,
@@ -823,6 +872,29 @@ void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols,
 }
 
 template <typename T>
+void launch_pcg_init_rhs(const PcgBuffers<T>& B, const T* b3, cudaStream_t s)
+{
+    const unsigned g = std::min<unsigned>(blocks_for(B.n_blocks, 256), resident_grid(k_pcg_init_rhs<T>, 256));
+    k_pcg_init_rhs<T><<<g, 256, 0, s>>>(B, b3);
+    check_launch("pcg_init_rhs");
+}
+
+template <typename T>
+void launch_rows4_to_vec3(int n_rows, const T* in4, T* out3, cudaStream_t s)
+{
+    k_rows4_to_vec3<T><<<blocks_for(3 * (int64_t)n_rows, 256), 256, 0, s>>>(n_rows, in4, out3);
+    check_launch("rows4_to_vec3");
+}
+
+unsigned pcg_max_grid()
+{
+    return std::max({resident_grid(k_pcg_spmv<float>, kSpmvThreads), resident_grid(k_pcg_update<float>, 256),
+                     resident_grid(k_pcg_init<float>, 256), resident_grid(k_pcg_init_rhs<float>, 256),
+                     resident_grid(k_pcg_spmv<double>, kSpmvThreads), resident_grid(k_pcg_update<double>, 256),
+                     resident_grid(k_pcg_init<double>, 256), resident_grid(k_pcg_init_rhs<double>, 256)});
+}
+
+template <typename T>
 void launch_dot_rows4(const T* du, const double* g, int n_rows, double* partials, unsigned* ticket, double* out,
                       cudaStream_t s)
 {
@@ -870,6 +942,8 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
     template void launch_bcsr_spmv<T>(int, const int32_t*, const int32_t*, const T*, int64_t, const T*, T*, cudaStream_t); \
     template void launch_axpy_to<T>(int64_t, const double*, double, const T*, double*, cudaStream_t);                  \
     template void launch_dot_rows4<T>(const T*, const double*, int, double*, unsigned*, double*, cudaStream_t);        \
+    template void launch_pcg_init_rhs<T>(const PcgBuffers<T>&, const T*, cudaStream_t);                                \
+    template void launch_rows4_to_vec3<T>(int, const T*, T*, cudaStream_t);                                            \
     template void launch_max_abs_rows4<T>(const T*, int, double*, unsigned*, double*, cudaStream_t);                   \
     template void launch_axpy_rows4<T>(int, const double*, double, const T*, double*, cudaStream_t);                   \
     template void launch_convert_to_double<T>(int64_t, const T*, double*, cudaStream_t);

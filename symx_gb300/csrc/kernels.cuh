@@ -110,6 +110,15 @@ template <typename T>
 void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const T* vals, int64_t vstride,
                       const T* x, T* y, cudaStream_t s);
 
+// PCG on a right-hand side b with 3 values per block row (instead of a double gradient).
+template <typename T>
+void launch_pcg_init_rhs(const PcgBuffers<T>& B, const T* b3, cudaStream_t s);
+// out3[3i+d] = in4[4i+d]
+template <typename T>
+void launch_rows4_to_vec3(int n_rows, const T* in4, T* out3, cudaStream_t s);
+// Largest grid any PCG kernel launches with (the number of per-block partials it writes).
+unsigned pcg_max_grid();
+
 // On the PCG solution du (4 values per block row) and double vectors with 3 per row:
 // out = du . g;  out = max |du|;  x_out = x0 + step * du.
 template <typename T>

@@ -68,6 +68,27 @@ def test_oracle_problem_matches_reference(golden, case):
     assert np.linalg.norm(x - sol["x_full"]) / np.linalg.norm(sol["x_full"] - p["x0"]) < 1e-10
 
 
+def test_oracle_pcg_solves_assembled_system():
+    import scipy.sparse.linalg as spla
+
+    from symx_gb300 import problems
+
+    p = problems.step_problem("tet4_6p")
+    rp, cols, vals, _ = O.Problem(p, 1).assemble(True)
+    A = O.bcsr_to_scipy(rp, cols, vals)
+    b = problems.normal(3, A.shape[0])
+    x, it, conv = O.bcsr_pcg(rp, cols, vals, b, 1e-14, 1e-12, 5000)
+    xe = spla.spsolve(A.tocsc(), b)
+    assert conv and 0 < it < 5000
+    assert np.max(np.abs(x - xe)) <= 1e-8 * np.max(np.abs(xe))
+    x, it, conv = O.bcsr_pcg(rp, cols, vals, np.zeros_like(b), 1e-12, 1e-6, 100)
+    assert conv and it == 0 and not np.any(x)
+    x, it, conv = O.bcsr_pcg(rp, cols, -vals, b, 1e-12, 1e-6, 100)
+    assert not conv and it == 1
+    with pytest.raises(ValueError):
+        O.bcsr_pcg(np.array([0, 1, 2]), np.array([1, 0]), vals[:2], b[:6], 1e-12, 1e-6, 10)
+
+
 def test_oracle_failure_codes():
     p = problems.step_problem("tet4_3")
     P = O.Problem(p, 1)
