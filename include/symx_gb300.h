@@ -199,6 +199,23 @@ int symxg_bcsr_pcg_f64(int32_t n_blocks, const int32_t* row_ptr, const int32_t* 
                        int64_t vals_stride, const double* b, double* x, double abs_tol, double rel_tol,
                        int32_t max_iterations, symxg_pcg_info* info, void* stream);
 
+/* Allocation-free variant of symxg_bcsr_pcg_f32; it has no counterpart in the reference.  Same
+ * arguments and results, but the workspace is a static device array sized for
+ * SYMXG_PCG_NOALLOC_MAX_BLOCKS block rows (about 9.5 MB per device), so the call allocates no
+ * device memory.  It is meant for callers that cannot allocate while they run: all device
+ * memory reserved up front by a caching allocator or a fixed budget, or no room for the
+ * device-wide wait that cudaFree implies.  Larger systems fail with SYMXG_ERR_INVALID_ARGUMENT
+ * before any launch.  The array is shared by all calls on a device: overlapping calls (two
+ * threads or two streams at once) race on it, so issue them one after another.  The first
+ * call on a device (with that device current) looks up the array's address; if that call is
+ * part of a program's set-up, it must come before any stream capture.  Each call clears the
+ * reduction tickets and counters it needs zeroed, on its stream, before its first kernel,
+ * and returns with `stream` synchronized. */
+#define SYMXG_PCG_NOALLOC_MAX_BLOCKS 65536
+int symxg_bcsr_pcg_f32_noalloc(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
+                               int64_t vals_stride, const float* b, float* x, double abs_tol, double rel_tol,
+                               int32_t max_iterations, symxg_pcg_info* info, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

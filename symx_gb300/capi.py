@@ -27,7 +27,7 @@ EXPORTS = [
     "symxg_upload", "symxg_solve_device", "symxg_download", "symxg_evaluate", "symxg_evaluate_energy",
     "symxg_assembled_hessian", "symxg_element_outputs", "symxg_op_counts", "symxg_project_pd_f32",
     "symxg_project_pd_f64", "symxg_bcsr_spmv_f32", "symxg_bcsr_spmv_f64", "symxg_launch_count",
-    "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64",
+    "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64", "symxg_bcsr_pcg_f32_noalloc",
 ]
 
 
@@ -126,6 +126,7 @@ def load(path: str | None = None):
         "symxg_bcsr_spmv_f64": ([I32, P, P, P, I64, P, P, P], C.c_int),
         "symxg_bcsr_pcg_f32": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
         "symxg_bcsr_pcg_f64": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
+        "symxg_bcsr_pcg_f32_noalloc": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -53,4 +53,12 @@ BcsrPcgResult run_bcsr_pcg(int n_blocks, const int32_t* row_ptr, const int32_t* 
                            int64_t vals_stride, const T* b, T* x, double abs_tol, double rel_tol, int max_iterations,
                            void* workspace, size_t workspace_bytes, unsigned partials_per_part, cudaStream_t s);
 
+// run_bcsr_pcg<float> on a static device array instead of a caller's workspace, for callers
+// that cannot allocate device memory (see bcsr_pcg_noalloc.cu for the rules of use).  At most
+// bcsr_pcg_noalloc_max_blocks() block rows.
+int bcsr_pcg_noalloc_max_blocks();
+BcsrPcgResult run_bcsr_pcg_noalloc_f32(int n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
+                                       int64_t vals_stride, const float* b, float* x, double abs_tol, double rel_tol,
+                                       int max_iterations, cudaStream_t s);
+
 }  // namespace symxg

@@ -458,4 +458,26 @@ int symxg_bcsr_pcg_f64(int32_t nb, const int32_t* rp, const int32_t* cols, const
     return pcg_impl<double>(nb, rp, cols, vals, vs, b, x, abs_tol, rel_tol, max_it, info, stream);
 }
 
+int symxg_bcsr_pcg_f32_noalloc(int32_t nb, const int32_t* rp, const int32_t* cols, const float* vals, int64_t vs,
+                               const float* b, float* x, double abs_tol, double rel_tol, int32_t max_it,
+                               symxg_pcg_info* info, void* stream)
+{
+    return guarded([&] {
+        if (!info) throw std::invalid_argument("null info");
+        std::memset(info, 0, sizeof(*info));
+        if (nb < 0 || vs < 0 || max_it < 0) throw std::invalid_argument("negative size");
+        if (nb > 0 && (!rp || !cols || !vals || !b || !x)) throw std::invalid_argument("null device pointer");
+        if (symxg::bcsr_pcg_noalloc_max_blocks() != SYMXG_PCG_NOALLOC_MAX_BLOCKS) throw std::logic_error("limit mismatch");
+        const symxg::BcsrPcgResult r = symxg::run_bcsr_pcg_noalloc_f32(nb, rp, cols, vals, vs, b, x, abs_tol, rel_tol,
+                                                                       max_it, (cudaStream_t)stream);
+        info->converged = r.converged;
+        info->n_iterations = r.iterations;
+        info->error = r.error;
+        info->found_indefiniteness = r.indefinite;
+        info->missing_diagonal = r.missing_diagonal;
+        if (r.missing_diagonal) throw std::invalid_argument("block rows without a diagonal block");
+        return SYMXG_OK;
+    });
+}
+
 }  // extern "C"
