@@ -269,7 +269,7 @@ def run_ours(args):
         "spmv_standalone": {"kernel": "k_bcsr_spmv<float>", "algorithmic_bytes": rf["algorithmic_bytes"],
                             "launch_seconds": rf["seconds"], "achieved_gbs": round(achieved_standalone, 1),
                             "frac": round(achieved_standalone / peak, 4)},
-        "projection": {"kernel": "k_project_pd_unrolled<float,12>", "launch_seconds": t_proj, "launches": int(n_proj),
+        "projection": {"kernel": "k_project_pd_deflated<float,12> + k_project_pd_listed<float,12> (fallback list)", "launch_seconds": t_proj, "launches": int(n_proj),
                        "matrices_per_launch": int(p["conn"].shape[0]),
                        "ns_per_matrix": round(t_proj / p["conn"].shape[0] * 1e9, 3) if n_proj else None},
         "clocks": clocks.summary(),

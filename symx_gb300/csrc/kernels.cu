@@ -145,10 +145,53 @@ __global__ void __launch_bounds__(128) k_project_pd_unrolled(T* __restrict__ H, 
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= count) return;
     int nc = 0;
+    T* h = H + m * (N * N);
+    // Tet4-sized matrices of translation-invariant energies: 9 x 9 decomposition (the
+    // scratch-free form of k_project_pd_deflated + k_project_pd_listed).
+    if constexpr (N == 12) {
+        if (symxg_dev::project_pd_deflated<T, N / 3>(h, eps, mirroring != 0, &nc) >= 0) {
+            if (nc) *not_converged = 1;
+            return;
+        }
+    }
     if constexpr (std::is_same<T, float>::value && N % 2 == 0)
-        symxg_dev::project_pd_inplace_packed<N>(H + m * (N * N), eps, mirroring != 0, &nc);
+        symxg_dev::project_pd_inplace_packed<N>(h, eps, mirroring != 0, &nc);
     else
-        symxg_dev::project_pd_inplace<T, N>(H + m * (N * N), eps, mirroring != 0, &nc);
+        symxg_dev::project_pd_inplace<T, N>(h, eps, mirroring != 0, &nc);
+    if (nc) *not_converged = 1;
+}
+
+// Translation-deflated projection (project_pd_deflated) of every matrix whose translation
+// residual is rounding noise; the others are left unchanged and their indices appended to
+// `fallback` (count in *n_fallback, zeroed before the launch) for k_project_pd_listed.
+template <typename T, int N>
+__global__ void __launch_bounds__(128) k_project_pd_deflated(T* __restrict__ H, int64_t count, T eps, int mirroring,
+                                                             int* not_converged, int64_t* __restrict__ fallback,
+                                                             unsigned long long* n_fallback)
+{
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= count) return;
+    int nc = 0;
+    if (symxg_dev::project_pd_deflated<T, N / 3>(H + m * (N * N), eps, mirroring != 0, &nc) < 0)
+        fallback[atomicAdd(n_fallback, 1ull)] = m;
+    if (nc) *not_converged = 1;
+}
+
+// Full projection of the matrices listed by k_project_pd_deflated (grid-stride over the list).
+template <typename T, int N>
+__global__ void __launch_bounds__(128) k_project_pd_listed(T* __restrict__ H, const int64_t* __restrict__ list,
+                                                           const unsigned long long* n_list, T eps, int mirroring,
+                                                           int* not_converged)
+{
+    const int64_t n = (int64_t)*n_list;
+    int nc = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        T* h = H + list[k] * (N * N);
+        if constexpr (std::is_same<T, float>::value && N % 2 == 0)
+            symxg_dev::project_pd_inplace_packed<N>(h, eps, mirroring != 0, &nc);
+        else
+            symxg_dev::project_pd_inplace<T, N>(h, eps, mirroring != 0, &nc);
+    }
     if (nc) *not_converged = 1;
 }
 
@@ -742,6 +785,24 @@ void check_launch(const char* what)
     if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: launch of ") + what + " failed: " + cudaGetErrorString(e));
 }
 
+// Blocks of `kernel` resident at once on the whole device (cached per kernel).
+template <typename K>
+unsigned resident_grid(K kernel, int threads)
+{
+    static std::mutex m;
+    static std::unordered_map<const void*, unsigned> cache;
+    std::lock_guard<std::mutex> lock(m);
+    auto it = cache.find((const void*)kernel);
+    if (it != cache.end()) return it->second;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    const unsigned g = (unsigned)std::max(1, sms * std::max(1, per_sm));
+    cache[(const void*)kernel] = g;
+    return g;
+}
+
 }  // namespace
 
 int64_t launch_count() { return g_launches.load(); }
@@ -768,9 +829,22 @@ void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, 
 }
 
 template <typename T>
-void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s)
+void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s,
+                       ProjectionScratch scratch)
 {
     if (count <= 0) return;
+    if (N == 12 && scratch.fallback && scratch.n_fallback) {
+        const cudaError_t e = cudaMemsetAsync(scratch.n_fallback, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
+        k_project_pd_deflated<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged,
+                                                                              scratch.fallback, scratch.n_fallback);
+        check_launch("project_pd_deflated");
+        static const unsigned listed_grid = resident_grid(k_project_pd_listed<T, 12>, 128);
+        k_project_pd_listed<T, 12><<<listed_grid, 128, 0, s>>>(H, scratch.fallback, scratch.n_fallback, eps, mirroring,
+                                                               not_converged);
+        check_launch("project_pd_listed");
+        return;
+    }
     switch (N) {
         case 3: k_project_pd_unrolled<T, 3><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
         case 6: k_project_pd_unrolled<T, 6><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
@@ -807,23 +881,6 @@ void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* 
     check_launch("block_jacobi_setup");
 }
 
-// Blocks of `kernel` resident at once on the whole device (cached per kernel).
-template <typename K>
-unsigned resident_grid(K kernel, int threads)
-{
-    static std::mutex m;
-    static std::unordered_map<const void*, unsigned> cache;
-    std::lock_guard<std::mutex> lock(m);
-    auto it = cache.find((const void*)kernel);
-    if (it != cache.end()) return it->second;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
-    const unsigned g = (unsigned)std::max(1, sms * std::max(1, per_sm));
-    cache[(const void*)kernel] = g;
-    return g;
-}
 
 template <typename T>
 void launch_pcg_init(const PcgBuffers<T>& B, const double* grad, cudaStream_t s)
@@ -932,7 +989,7 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
 
 #define SYMXG_INSTANTIATE(T)                                                                                          \
     template void launch_dot_mixed<T>(const T*, const double*, int64_t, double*, unsigned*, double*, cudaStream_t);  \
-    template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t);                                 \
+    template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t, ProjectionScratch);              \
     template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, int64_t, cudaStream_t); \
     template void launch_block_jacobi_setup<T>(int, const int32_t*, const T*, int64_t, T*, cudaStream_t);              \
     template void launch_pcg_init<T>(const PcgBuffers<T>&, const double*, cudaStream_t);                               \

@@ -44,9 +44,18 @@ void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, 
                       cudaStream_t s);
 
 // Element-Hessian projection, in place, block-major storage, `count` matrices of N x N.
-// not_converged: one int, set to 1 if any matrix hit the sweep cap.
+// not_converged: one int, set to 1 if any matrix hit the sweep cap.  With scratch (12 x 12
+// only: `fallback` holds `count` indices, `n_fallback` one counter), translation-invariant
+// matrices are projected in the 9-dimensional complement of the rigid translations and the
+// others with the full decomposition in a second launch; without it, every matrix takes the
+// full decomposition.
+struct ProjectionScratch {
+    int64_t* fallback = nullptr;
+    unsigned long long* n_fallback = nullptr;
+};
 template <typename T>
-void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s);
+void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s,
+                       ProjectionScratch scratch = ProjectionScratch{});
 
 // BCSR values are stored component-major: component m (row-major inside the 3x3 block) of
 // block k is vals[m * vstride + k], vstride >= nnzb.

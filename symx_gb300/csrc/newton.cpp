@@ -398,6 +398,16 @@ struct SolverImpl {
     DevBuf<unsigned> tickets;
     DevBuf<PcgState> pcg_state;
     DevBuf<int> flags;
+    // projection: indices of the 12 x 12 element Hessians that need the full decomposition
+    DevBuf<int64_t> proj_fallback;
+    DevBuf<unsigned long long> proj_n_fallback;
+    symxg::ProjectionScratch proj_scratch()
+    {
+        symxg::ProjectionScratch ps;
+        ps.fallback = proj_fallback.p;
+        ps.n_fallback = proj_n_fallback.p;
+        return ps;
+    }
     double* h_scalars = nullptr;
     PcgState* h_state = nullptr;
     Precision allocated_precision = Precision::FP64;
@@ -655,6 +665,15 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     ck(cudaMemset(I.tickets.p, 0, sizeof(unsigned) * 8), "memset");
     I.pcg_state.alloc(1);
     I.flags.alloc(4);
+    {
+        int64_t n12 = 0;
+        for (auto& cp : I.pots)
+            if (cp.nb == 4) n12 = std::max<int64_t>(n12, cp.n_elements);
+        if (n12 > 0) {
+            I.proj_fallback.alloc(n12);
+            I.proj_n_fallback.alloc(1);
+        }
+    }
     ck(cudaMallocHost(&I.h_scalars, sizeof(double) * 16), "pinned");
     ck(cudaMallocHost(&I.h_state, sizeof(PcgState)), "pinned");
     for (auto& cp : I.pots) {
@@ -794,7 +813,7 @@ void assemble_t(SolverImpl& I, bool project, const NewtonSettings& s, int mode)
         ck(cudaMemsetAsync(I.flags.p, 0, sizeof(int), I.stream), "memset");
         for (auto& cp : I.pots)
             symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)s.projection_eps,
-                                        s.project_to_pd_use_mirroring, I.flags.p, I.stream);
+                                        s.project_to_pd_use_mirroring, I.flags.p, I.stream, I.proj_scratch());
     }
     symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.vstride, I.stream);
 }
@@ -928,7 +947,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
                     cudaEventRecord(a, s);
                 }
                 symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)S.projection_eps,
-                                            S.project_to_pd_use_mirroring, I.flags.p, s);
+                                            S.project_to_pd_use_mirroring, I.flags.p, s, I.proj_scratch());
                 if (timed) {
                     cudaEventRecord(b, s);
                     pending_kernel_events.push_back({std::string("project_pd_12_") + (sizeof(T) == 4 ? "f32" : "f64"), a, b});

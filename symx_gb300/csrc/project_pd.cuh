@@ -285,32 +285,20 @@ SYMXG_DEVICE int project_pd_inplace_packed(float* __restrict__ H, float eps, boo
 }
 #endif
 
-// Project the matrix H (block-major, N x N) in place.  Returns 1 if the matrix changed,
-// and sets *not_converged when the sweep cap was reached.
+// Cyclic Jacobi on the symmetric matrix a (upper triangle) with eigenvectors accumulated in
+// v (v = I on entry): on return the diagonal of a holds the eigenvalues and column k of v
+// the eigenvector of a[k][k].  Convergence is tested every kGroup relabel steps (float) or
+// every double sweep (double); the off-diagonal norm and V diag(lambda) V^T do not depend on
+// the labelling, so stopping between full double sweeps is exact.  Returns false when the
+// sweep cap was reached.
 template <typename T, int N>
-SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, int* not_converged)
+SYMXG_DEVICE bool jacobi_eigen(T (&a)[N * (N + 1) / 2], T (&v)[N * N])
 {
-    constexpr int NT = N * (N + 1) / 2;
-    T a[NT];
-    T v[N * N];
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = i; j < N; ++j) a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = 0; j < N; ++j) v[i * N + j] = (i == j) ? T(1) : T(0);
-
     T fro2 = T(0);
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
         for (int j = i; j < N; ++j) fro2 += (i == j ? T(1) : T(2)) * sq(a[tri<N>(i, j)]);
-
-    // Convergence is tested every kGroup relabel steps (float) or every double sweep (double).
-    // The off-diagonal norm and the final V diag(lambda) V^T do not depend on the labelling,
-    // so stopping between full double sweeps is exact.
     constexpr int kGroup = (sizeof(T) == 4) ? (N < 4 ? N : 4) : N;
     constexpr int kMaxGroups = JacobiTol<T>::max_double_sweeps * ((N + kGroup - 1) / kGroup);
     int grp = 0;
@@ -328,7 +316,26 @@ SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, in
             jacobi_double_sweep_cyclic<T, N>(a, v);
         }
     }
-    if (grp == kMaxGroups && not_converged) *not_converged = 1;
+    return grp < kMaxGroups;
+}
+
+// Project the matrix H (block-major, N x N) in place.  Returns 1 if the matrix changed,
+// and sets *not_converged when the sweep cap was reached.
+template <typename T, int N>
+SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, int* not_converged)
+{
+    constexpr int NT = N * (N + 1) / 2;
+    T a[NT];
+    T v[N * N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = 0; j < N; ++j) v[i * N + j] = (i == j) ? T(1) : T(0);
+    if (!jacobi_eigen<T, N>(a, v) && not_converged) *not_converged = 1;
 
     bool changed = false;
     T lam[N];
@@ -349,6 +356,144 @@ SYMXG_DEVICE int project_pd_inplace(T* __restrict__ H, T eps, bool mirroring, in
             T s = T(0);
 #pragma unroll
             for (int k = 0; k < N; ++k) s += v[i * N + k] * lam[k] * v[j * N + k];
+            H[bm_index<N>(i, j)] = s;
+            H[bm_index<N>(j, i)] = s;
+        }
+    return 1;
+}
+
+// ---- translation deflation
+//
+// An element energy that depends on its nodes only through their differences (every elastic
+// energy) has a Hessian that annihilates the three rigid translations t_d = (e_d, ..., e_d) /
+// sqrt(NB) of its NB nodes; in floating point H t_d is rounding noise.  For such a matrix
+// the projection is done in the complement of the translations: with Q = B (x) I3, B the
+// Helmert basis of the node space orthogonal to (1, ..., 1) (column m = 1..NB-1:
+// 1/sqrt(m(m+1)) for the nodes before m, -m/sqrt(m(m+1)) for node m, 0 after), H equals
+// Q (Q^T H Q) Q^T, the translation eigenvalues are 0, and the eigen-decomposition shrinks
+// from N x N to (N-3) x (N-3) (Jacobi work grows as n^3: 0.42x for a Tet4).  The result is
+// the reference's V diag(lambda') V^T with the translation eigenvalues 0 -> eps (0 when
+// mirroring).  A matrix whose translation residual max |H t| exceeds tol * max |H| is left
+// alone and reported (returns -1): the caller projects it with the full decomposition.
+template <typename T>
+struct DeflationTol;
+template <>
+struct DeflationTol<float> {
+    static SYMXG_DEVICE float value() { return 1e-5f; }   // ~80 ulp of the largest entry
+};
+template <>
+struct DeflationTol<double> {
+    static SYMXG_DEVICE double value() { return 1e-12; }
+};
+
+// Helmert basis entry B[i][m] (m = 1..NB-1), with c[m] = 1/sqrt(m(m+1)).
+template <typename T, int NB>
+SYMXG_DEVICE T helmert(const T (&c)[NB], int i, int m)
+{
+    return i < m ? c[m] : (i == m ? -T(m) * c[m] : T(0));
+}
+
+template <typename T, int NB>
+SYMXG_DEVICE int project_pd_deflated(T* __restrict__ H, T eps, bool mirroring, int* not_converged)
+{
+    constexpr int N = 3 * NB;
+    constexpr int M = N - 3;
+    T c[NB];
+    c[0] = T(0);
+#pragma unroll
+    for (int m = 1; m < NB; ++m) c[m] = T(1) / sqrt(T(m * (m + 1)));
+    T b[M * (M + 1) / 2];
+    {
+        T a[N * (N + 1) / 2];
+        T hmax = T(0);
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int j = i; j < N; ++j) {
+                a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
+                hmax = fmax(hmax, fabs(a[tri<N>(i, j)]));
+            }
+        // translation residual: (H t_e) at row (i, d), up to the factor 1/sqrt(NB)
+        T res = T(0);
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                T r = T(0);
+#pragma unroll
+                for (int jn = 0; jn < NB; ++jn) r += a[tri<N>(i, 3 * jn + e)];
+                res = fmax(res, fabs(r));
+            }
+        if (!(res <= DeflationTol<T>::value() * hmax)) return -1;
+        // b = Q^T H Q (upper triangle), row (m, d) of b = row 3 (m - 1) + d
+#pragma unroll
+        for (int p = 0; p < M; ++p)
+#pragma unroll
+            for (int q = p; q < M; ++q) {
+                const int m = p / 3 + 1, d = p % 3, l = q / 3 + 1, e = q % 3;
+                T s = T(0);
+#pragma unroll
+                for (int i = 0; i <= m; ++i) {
+                    T t = T(0);
+#pragma unroll
+                    for (int j = 0; j <= l; ++j) t += helmert<T, NB>(c, j, l) * a[tri<N>(3 * i + d, 3 * j + e)];
+                    s += helmert<T, NB>(c, i, m) * t;
+                }
+                b[tri<M>(p, q)] = s;
+            }
+    }
+    T v[M * M];
+#pragma unroll
+    for (int i = 0; i < M; ++i)
+#pragma unroll
+        for (int j = 0; j < M; ++j) v[i * M + j] = (i == j) ? T(1) : T(0);
+    if (!jacobi_eigen<T, M>(b, v) && not_converged) *not_converged = 1;
+
+    bool changed = false;
+    T lam[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        T l = b[tri<M>(k, k)];
+        if (l < eps) {
+            changed = true;
+            l = mirroring ? -l : eps;
+        }
+        lam[k] = l;
+    }
+    T lam_t = T(0);  // the three translation eigenvalues
+    if (T(0) < eps) {
+        changed = true;
+        lam_t = mirroring ? T(0) : eps;
+    }
+    if (!changed) return 0;
+    // W = V diag(lam) V^T (upper triangle, reusing b), then H = Q W Q^T + lam_t / NB (1 1^T (x) I3)
+#pragma unroll
+    for (int p = 0; p < M; ++p)
+#pragma unroll
+        for (int q = p; q < M; ++q) {
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < M; ++k) s += v[p * M + k] * lam[k] * v[q * M + k];
+            b[tri<M>(p, q)] = s;
+        }
+    const T diag_t = lam_t / T(NB);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) {
+            const int in = i / 3, d = i % 3, jn = j / 3, e = j % 3;
+            T s = (d == e) ? diag_t : T(0);
+#pragma unroll
+            for (int m = 1; m < NB; ++m) {
+                if (m < in) continue;  // B[in][m] = 0 for in > m
+                T t = T(0);
+#pragma unroll
+                for (int l = 1; l < NB; ++l) {
+                    if (l < jn) continue;
+                    t += helmert<T, NB>(c, jn, l) * b[tri<M>(3 * (m - 1) + d, 3 * (l - 1) + e)];
+                }
+                s += helmert<T, NB>(c, in, m) * t;
+            }
             H[bm_index<N>(i, j)] = s;
             H[bm_index<N>(j, i)] = s;
         }

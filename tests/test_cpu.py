@@ -201,3 +201,32 @@ def test_cpp_generated_kernels_compile_with_nvrtc(cpp_test, tmp_path):
     r = subprocess.run([cpp_test, "nvrtc", str(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout
     assert "nvrtc PASS" in r.stdout
+
+
+def test_host_build_of_projection_matches_reference(golden, tmp_path):
+    """The device projection code built for the host: full and translation-deflated
+    decompositions against the reference's project_to_PD_inplace on the 12x12 fixtures
+    (32 Neo-Hookean element Hessians, which deflate, and 16 random symmetric matrices,
+    which must be refused by the deflation test)."""
+    exe = tmp_path / "test_projection_host"
+    subprocess.run(["g++", "-std=c++17", "-O2", os.path.join(ROOT, "tests", "cpp", "test_projection_host.cpp"),
+                    "-o", str(exe)], check=True)
+    d = golden("project12")
+    inp, ref = d["inputs"], d["outputs"]
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        np.array([inp.shape[0], 12], dtype=np.int64).tofile(f)
+        inp.astype(np.float64).tofile(f)
+    r = subprocess.run([str(exe), str(fin), str(fout)], capture_output=True, text=True, check=True)
+    assert "not_converged 0" in r.stdout
+    raw = np.fromfile(fout, dtype=np.uint8)
+    n = inp.size
+    out = raw[:32 * n].view(np.float64).reshape(4, *inp.shape)
+    status = raw[32 * n:].view(np.int32).reshape(2, -1)
+    nh = np.arange(inp.shape[0]) < 32
+    assert np.all(status[:, nh] >= 0) and np.all(status[:, ~nh] == -1)
+    scale = np.max(np.abs(inp), axis=(1, 2))[:, None, None]
+    for mode, tol in ((0, 1e-9), (1, 1e-9), (2, 1e-4), (3, 1e-4)):
+        err = np.abs(out[mode] - ref) / scale
+        sel = nh if mode in (1, 3) else slice(None)
+        assert np.max(err[sel]) <= tol, mode

@@ -226,3 +226,14 @@ def test_inverted_initial_element_is_rejected_by_line_search(sg):
     assert np.isinf(E) and E > 0
     st = s.solve()
     assert st["solver_return"] != 0
+
+
+def test_fp32_tet4_hessians_take_the_deflated_projection(sg):
+    """The mixed path projects 12x12 element Hessians in the complement of the rigid
+    translations when their translation residual is below 1e-5 of max |H|; the FP32
+    Neo-Hookean Hessians from the generated kernels should (nearly) all qualify."""
+    p, s = make(sg, "tet4_10", precision="mixed")
+    _, _, H = s.element_outputs(0, project=False)
+    res = np.abs(H.reshape(-1, 12, 4, 3).sum(axis=2)).max(axis=(1, 2))
+    hmax = np.abs(H).max(axis=(1, 2))
+    assert np.mean(res <= 1e-5 * hmax) >= 0.99
