@@ -264,10 +264,27 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
         }
 }
 
+// ---------------------------------------------------------------- BCSR value layouts
+// Component m (row-major inside the 3x3 block) of block k is vals[base(k) + m * step()].
+// Strided (the C ABI's): base = k, step = vstride (component-major arrays).
+// Tiled (the solver's own): blocks in tiles of 32, each tile nine component rows of 32
+// values, base = (k / 32) * 288 + k % 32, step = 32.  A warp's loads stay coalesced as in the
+// strided form, but the blocks of consecutive rows lie in one contiguous span of memory
+// (one DRAM stream per warp instead of nine), and the component offsets are constants.
+struct StridedBcsr {
+    int64_t vs;
+    __host__ __device__ __forceinline__ int64_t base(int64_t k) const { return k; }
+    __host__ __device__ __forceinline__ int64_t step() const { return vs; }
+};
+struct TiledBcsr {
+    __host__ __device__ __forceinline__ int64_t base(int64_t k) const { return (k >> 5) * 288 + (k & 31); }
+    __host__ __device__ __forceinline__ static constexpr int64_t step() { return 32; }
+};
+
 // ---------------------------------------------------------------- assembly
-template <typename T>
+template <typename T, typename L>
 __global__ void k_assemble_blocks(int64_t nnzb, const int64_t* __restrict__ slot_ptr, const int32_t* __restrict__ contrib,
-                                  const T* __restrict__ blocks, T* __restrict__ vals, int64_t vstride)
+                                  const T* __restrict__ blocks, T* __restrict__ vals, L lay)
 {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nnzb) return;
@@ -280,7 +297,7 @@ __global__ void k_assemble_blocks(int64_t nnzb, const int64_t* __restrict__ slot
         for (int k = 0; k < 9; ++k) acc[k] += b[k];
     }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) vals[k * vstride + s] = acc[k];
+    for (int k = 0; k < 9; ++k) vals[lay.base(s) + k * lay.step()] = acc[k];
 }
 
 __global__ void k_gather_gradient(int n_blocks, const int64_t* __restrict__ ptr, const int32_t* __restrict__ contrib,
@@ -303,16 +320,17 @@ __global__ void k_gather_gradient(int n_blocks, const int64_t* __restrict__ ptr,
 // ---------------------------------------------------------------- block Jacobi
 // Dinv holds, per block row, the inverse diagonal block as three rows of four (the fourth
 // entry zero), so the preconditioner is applied with three 16-byte (float) loads.
-template <typename T>
+template <typename T, typename L>
 __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ diag_slot, const T* __restrict__ vals,
-                                     int64_t vstride, T* __restrict__ Dinv)
+                                     L lay, T* __restrict__ Dinv)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_blocks) return;
     const int64_t k = diag_slot[r];
     // symmetric 3x3 inverse from the upper triangle (cofactors / determinant)
-    const double a = vals[k], b = vals[vstride + k], c = vals[2 * vstride + k], d = vals[4 * vstride + k],
-                 e = vals[5 * vstride + k], f = vals[8 * vstride + k];
+    const T* __restrict__ v = vals + lay.base(k);
+    const int64_t st = lay.step();
+    const double a = v[0], b = v[st], c = v[2 * st], d = v[4 * st], e = v[5 * st], f = v[8 * st];
     const double c00 = d * f - e * e, c01 = c * e - b * f, c02 = b * e - c * d;
     const double det = a * c00 + b * c01 + c * c02;
     const double id = 1.0 / det;
@@ -326,6 +344,12 @@ __global__ void k_block_jacobi_setup(int n_blocks, const int32_t* __restrict__ d
 
 // ---------------------------------------------------------------- SpMV / PCG
 constexpr int kSpmvThreads = 256;  // 16 rows per block, 16 lanes per row
+// Resident blocks per SM the SpMV kernels are compiled for: the full 2048 threads in float
+// (the kernels are latency-bound, so occupancy beats the few registers it costs).
+template <typename T>
+struct SpmvMinBlocks {
+    static constexpr int value = sizeof(T) == 4 ? 8 : 4;
+};
 
 // PCG vectors hold one block row as four values (x, y, z, 0): a gathered block column is
 // one 16-byte load (float) instead of three 4-byte loads spread over 12 bytes.
@@ -353,20 +377,20 @@ __device__ __forceinline__ void st4(double* __restrict__ p, const Row4<double>& 
     reinterpret_cast<double2*>(p)[1] = make_double2(v.z, v.w);
 }
 
-// BCSR storage: the nine components of 3x3 block k (row-major inside the block) are
-// vals[m * vstride + k], m = 0..8 (component-major), so each load of a half-warp reads 16
+// BCSR values in either layout above: each component load of a half-warp reads 16
 // consecutive values.
 //
-// Products of two block rows at once, each over the 16 lanes of its half-warp, lane-strided
-// over the row's blocks; both rows' loads are in flight together.  xv(c) is the multiplied
-// vector's block row c.  The sums are reduced across the 16 lanes in a fixed butterfly order;
-// every lane of the warp must call this (rows past the end pass valid = false), so the
-// full-mask shuffles are converged.
-template <typename T, typename XV>
+// Per-lane partial products of two block rows at once, each over the 16 lanes of its
+// half-warp, lane-strided over the row's blocks; both rows' loads are in flight together.
+// xv(c) is the multiplied vector's block row c.  half_warp_transpose_sum reduces the
+// partials; every lane of the warp must call both (rows past the end pass valid = false), so
+// the full-mask shuffles are converged.
+template <typename T, typename L, typename XV>
 __device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bool vB, int lane16,
                                                  const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
-                                                 const T* __restrict__ vals, int64_t vs, XV xv, T (&a)[3], T (&b)[3])
+                                                 const T* __restrict__ vals, L lay, XV xv, T (&a)[3], T (&b)[3])
 {
+    const int64_t st = lay.step();
     a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = T(0);
     const int kbA = vA ? row_ptr[rowA] : 0, keA = vA ? row_ptr[rowA + 1] : 0;
     const int kbB = vB ? row_ptr[rowB] : 0, keB = vB ? row_ptr[rowB + 1] : 0;
@@ -376,33 +400,59 @@ __device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bo
         if (!hA && !hB) break;
         if (hA) {
             const Row4<T> v = xv(cols[kA]);
-            a[0] += vals[kA] * v.x + vals[vs + kA] * v.y + vals[2 * vs + kA] * v.z;
-            a[1] += vals[3 * vs + kA] * v.x + vals[4 * vs + kA] * v.y + vals[5 * vs + kA] * v.z;
-            a[2] += vals[6 * vs + kA] * v.x + vals[7 * vs + kA] * v.y + vals[8 * vs + kA] * v.z;
+            const T* __restrict__ m = vals + lay.base(kA);
+            a[0] += m[0] * v.x + m[st] * v.y + m[2 * st] * v.z;
+            a[1] += m[3 * st] * v.x + m[4 * st] * v.y + m[5 * st] * v.z;
+            a[2] += m[6 * st] * v.x + m[7 * st] * v.y + m[8 * st] * v.z;
         }
         if (hB) {
             const Row4<T> v = xv(cols[kB]);
-            b[0] += vals[kB] * v.x + vals[vs + kB] * v.y + vals[2 * vs + kB] * v.z;
-            b[1] += vals[3 * vs + kB] * v.x + vals[4 * vs + kB] * v.y + vals[5 * vs + kB] * v.z;
-            b[2] += vals[6 * vs + kB] * v.x + vals[7 * vs + kB] * v.y + vals[8 * vs + kB] * v.z;
-        }
-    }
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            a[d] += __shfl_xor_sync(0xffffffffu, a[d], o, 16);
-            b[d] += __shfl_xor_sync(0xffffffffu, b[d], o, 16);
+            const T* __restrict__ m = vals + lay.base(kB);
+            b[0] += m[0] * v.x + m[st] * v.y + m[2 * st] * v.z;
+            b[1] += m[3 * st] * v.x + m[4 * st] * v.y + m[5 * st] * v.z;
+            b[2] += m[6 * st] * v.x + m[7 * st] * v.y + m[8 * st] * v.z;
         }
     }
 }
 
+// Sum the six per-lane partials (a[0..2] of row A, b[0..2] of row B) over the 16 lanes of a
+// half-warp with a transposing butterfly: at each level a lane keeps half of its values and
+// sends the other half, so 8 shuffles do what 24 would do lane-by-lane.  On return lanes
+// 2i and 2i+1 of the half-warp hold the total of value i (0..2: row A, 3..5: row B, 6..7:
+// zero padding), summed in a fixed order.
+template <typename T>
+__device__ __forceinline__ T half_warp_transpose_sum(const T (&a)[3], const T (&b)[3], int lane16)
+{
+    T v[8] = {a[0], a[1], a[2], b[0], b[1], b[2], T(0), T(0)};
+    const bool up8 = (lane16 & 8) != 0;
+    T w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const T send = up8 ? v[i] : v[i + 4];
+        const T keep = up8 ? v[i + 4] : v[i];
+        w[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8, 16);
+    }
+    const bool up4 = (lane16 & 4) != 0;
+    T u[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const T send = up4 ? w[i] : w[i + 2];
+        const T keep = up4 ? w[i + 2] : w[i];
+        u[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4, 16);
+    }
+    const bool up2 = (lane16 & 2) != 0;
+    const T send = up2 ? u[0] : u[1];
+    const T keep = up2 ? u[1] : u[0];
+    const T t = keep + __shfl_xor_sync(0xffffffffu, send, 2, 16);
+    return t + __shfl_xor_sync(0xffffffffu, t, 1, 16);
+}
+
 // y = A x (x and y with 3 values per block row, the C ABI layout); each warp takes four
 // block rows per pass (two per half-warp).
-template <typename T>
-__global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const int32_t* __restrict__ row_ptr,
-                                                            const int32_t* __restrict__ cols, const T* __restrict__ vals,
-                                                            int64_t vs, const T* __restrict__ x, T* __restrict__ y)
+template <typename T, typename L>
+__global__ void __launch_bounds__(kSpmvThreads, SpmvMinBlocks<T>::value)
+    k_bcsr_spmv(int n_blocks, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                const T* __restrict__ vals, L lay, const T* __restrict__ x, T* __restrict__ y)
 {
     const int lane16 = threadIdx.x & 15;
     const int half = (threadIdx.x >> 4) & 1;
@@ -413,10 +463,12 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bcsr_spmv(int n_blocks, const 
         const int rowA = base + half, rowB = base + 2 + half;
         const bool vA = rowA < n_blocks, vB = rowB < n_blocks;
         T a[3], b[3];
-        two_row_products<T>(rowA, vA, rowB, vB, lane16, row_ptr, cols, vals, vs, xv, a, b);
-        if (lane16 == 0) {
-            if (vA) { y[3 * rowA] = a[0]; y[3 * rowA + 1] = a[1]; y[3 * rowA + 2] = a[2]; }
-            if (vB) { y[3 * rowB] = b[0]; y[3 * rowB + 1] = b[1]; y[3 * rowB + 2] = b[2]; }
+        two_row_products<T>(rowA, vA, rowB, vB, lane16, row_ptr, cols, vals, lay, xv, a, b);
+        const T sum = half_warp_transpose_sum<T>(a, b, lane16);
+        const int idx = lane16 >> 1;  // 0..2 row A, 3..5 row B
+        if (!(lane16 & 1) && idx < 6) {
+            const int row = idx < 3 ? rowA : rowB;
+            if (idx < 3 ? vA : vB) y[3 * row + idx % 3] = sum;
         }
     }
 }
@@ -521,9 +573,9 @@ __device__ __forceinline__ Row4<T> direction(const T* __restrict__ z, const T* _
 
 // PCG step 1: p = z + beta p_old (fused), q = A p, p.q.  Grid sized to the resident
 // blocks; each warp takes four block rows per pass.
-template <typename T>
-__global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, const T* __restrict__ p_old,
-                                                           T* __restrict__ p_new, int first)
+template <typename T, typename L>
+__global__ void __launch_bounds__(kSpmvThreads, SpmvMinBlocks<T>::value)
+    k_pcg_spmv(PcgBuffers<T> B, L lay, const T* __restrict__ p_old, T* __restrict__ p_new, int first)
 {
     if (B.state->done) return;
     __shared__ double sh[32];
@@ -540,19 +592,18 @@ __global__ void __launch_bounds__(kSpmvThreads) k_pcg_spmv(PcgBuffers<T> B, cons
         const int rowA = base + half, rowB = base + 2 + half;
         const bool vA = rowA < B.n_blocks, vB = rowB < B.n_blocks;
         T a[3], b[3];
-        two_row_products<T>(rowA, vA, rowB, vB, lane16, B.row_ptr, B.cols, B.vals, B.vals_stride, pv, a, b);
-        if (lane16 == 0) {
-#pragma unroll
-            for (int rr = 0; rr < 2; ++rr) {
-                const int row = rr ? rowB : rowA;
-                if (!(rr ? vB : vA)) continue;
-                const Row4<T> pd = pv(row);
-                const T* qd = rr ? b : a;
-                st4(p_new + 4 * row, pd);
-                st4(B.q + 4 * row, Row4<T>{qd[0], qd[1], qd[2], T(0)});
-                pq.add_prod(pd.x, qd[0]);
-                pq.add_prod(pd.y, qd[1]);
-                pq.add_prod(pd.z, qd[2]);
+        two_row_products<T>(rowA, vA, rowB, vB, lane16, B.row_ptr, B.cols, B.vals, lay, pv, a, b);
+        const T qd = half_warp_transpose_sum<T>(a, b, lane16);
+        // one lane per output component: p and q of that component, and its p.q term
+        const int idx = lane16 >> 1;  // 0..2 row A, 3..5 row B
+        if (!(lane16 & 1) && idx < 6) {
+            const int row = idx < 3 ? rowA : rowB, d = idx % 3;
+            if (idx < 3 ? vA : vB) {
+                const int64_t o = 4 * (int64_t)row + d;
+                const T pd = f ? z[o] : fma(beta, p_old[o], z[o]);  // the bits direction() gives
+                p_new[o] = pd;
+                B.q[o] = qd;
+                pq.add_prod(pd, qd);
             }
         }
     }
@@ -862,7 +913,11 @@ void launch_assemble_blocks(int64_t nnzb, const int64_t* slot_ptr, const int32_t
                             int64_t vstride, cudaStream_t s)
 {
     if (nnzb <= 0) return;
-    k_assemble_blocks<T><<<blocks_for(nnzb, 256), 256, 0, s>>>(nnzb, slot_ptr, contrib, blocks, vals, vstride);
+    if (vstride == kTiledBcsr)
+        k_assemble_blocks<T><<<blocks_for(nnzb, 256), 256, 0, s>>>(nnzb, slot_ptr, contrib, blocks, vals, TiledBcsr{});
+    else
+        k_assemble_blocks<T><<<blocks_for(nnzb, 256), 256, 0, s>>>(nnzb, slot_ptr, contrib, blocks, vals,
+                                                                    StridedBcsr{vstride});
     check_launch("assemble");
 }
 
@@ -877,7 +932,11 @@ template <typename T>
 void launch_block_jacobi_setup(int n_blocks, const int32_t* diag_slot, const T* vals, int64_t vstride, T* Dinv,
                                cudaStream_t s)
 {
-    k_block_jacobi_setup<T><<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, diag_slot, vals, vstride, Dinv);
+    if (vstride == kTiledBcsr)
+        k_block_jacobi_setup<T><<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, diag_slot, vals, TiledBcsr{}, Dinv);
+    else
+        k_block_jacobi_setup<T><<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, diag_slot, vals,
+                                                                           StridedBcsr{vstride}, Dinv);
     check_launch("block_jacobi_setup");
 }
 
@@ -890,15 +949,22 @@ void launch_pcg_init(const PcgBuffers<T>& B, const double* grad, cudaStream_t s)
     check_launch("pcg_init");
 }
 
+template <typename T, typename L>
+void launch_pcg_spmv_l(const PcgBuffers<T>& B, L lay, int iteration, cudaStream_t s)
+{
+    const unsigned gs = std::min<unsigned>(blocks_for((int64_t)B.n_blocks * 8, kSpmvThreads),
+                                           resident_grid(k_pcg_spmv<T, L>, kSpmvThreads));
+    T* p_old = (iteration & 1) ? B.p : B.p2;
+    T* p_new = (iteration & 1) ? B.p2 : B.p;
+    k_pcg_spmv<T, L><<<gs, kSpmvThreads, 0, s>>>(B, lay, p_old, p_new, iteration == 0 ? 1 : 0);
+    check_launch("pcg_spmv");
+}
+
 template <typename T>
 void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 {
-    const unsigned gs = std::min<unsigned>(blocks_for((int64_t)B.n_blocks * 8, kSpmvThreads),
-                                           resident_grid(k_pcg_spmv<T>, kSpmvThreads));
-    T* p_old = (iteration & 1) ? B.p : B.p2;
-    T* p_new = (iteration & 1) ? B.p2 : B.p;
-    k_pcg_spmv<T><<<gs, kSpmvThreads, 0, s>>>(B, p_old, p_new, iteration == 0 ? 1 : 0);
-    check_launch("pcg_spmv");
+    if (B.vals_stride == kTiledBcsr) launch_pcg_spmv_l<T>(B, TiledBcsr{}, iteration, s);
+    else launch_pcg_spmv_l<T>(B, StridedBcsr{B.vals_stride}, iteration, s);
 }
 
 template <typename T>
@@ -922,9 +988,14 @@ void launch_bcsr_spmv(int n_blocks, const int32_t* row_ptr, const int32_t* cols,
                       const T* x, T* y, cudaStream_t s)
 {
     if (n_blocks <= 0) return;
-    const unsigned g = std::min<unsigned>(blocks_for((int64_t)n_blocks * 8, kSpmvThreads),
-                                          resident_grid(k_bcsr_spmv<T>, kSpmvThreads));
-    k_bcsr_spmv<T><<<g, kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols, vals, vstride, x, y);
+    const unsigned blocks = blocks_for((int64_t)n_blocks * 8, kSpmvThreads);
+    if (vstride == kTiledBcsr) {
+        const unsigned g = std::min<unsigned>(blocks, resident_grid(k_bcsr_spmv<T, TiledBcsr>, kSpmvThreads));
+        k_bcsr_spmv<T><<<g, kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols, vals, TiledBcsr{}, x, y);
+    } else {
+        const unsigned g = std::min<unsigned>(blocks, resident_grid(k_bcsr_spmv<T, StridedBcsr>, kSpmvThreads));
+        k_bcsr_spmv<T><<<g, kSpmvThreads, 0, s>>>(n_blocks, row_ptr, cols, vals, StridedBcsr{vstride}, x, y);
+    }
     check_launch("bcsr_spmv");
 }
 
@@ -945,9 +1016,12 @@ void launch_rows4_to_vec3(int n_rows, const T* in4, T* out3, cudaStream_t s)
 
 unsigned pcg_max_grid()
 {
-    return std::max({resident_grid(k_pcg_spmv<float>, kSpmvThreads), resident_grid(k_pcg_update<float>, 256),
+    return std::max({resident_grid(k_pcg_spmv<float, TiledBcsr>, kSpmvThreads),
+                     resident_grid(k_pcg_spmv<float, StridedBcsr>, kSpmvThreads),
+                     resident_grid(k_pcg_spmv<double, TiledBcsr>, kSpmvThreads),
+                     resident_grid(k_pcg_spmv<double, StridedBcsr>, kSpmvThreads), resident_grid(k_pcg_update<float>, 256),
                      resident_grid(k_pcg_init<float>, 256), resident_grid(k_pcg_init_rhs<float>, 256),
-                     resident_grid(k_pcg_spmv<double>, kSpmvThreads), resident_grid(k_pcg_update<double>, 256),
+                     resident_grid(k_pcg_update<double>, 256),
                      resident_grid(k_pcg_init<double>, 256), resident_grid(k_pcg_init_rhs<double>, 256)});
 }
 

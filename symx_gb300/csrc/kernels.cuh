@@ -58,7 +58,11 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
                        ProjectionScratch scratch = ProjectionScratch{});
 
 // BCSR values are stored component-major: component m (row-major inside the 3x3 block) of
-// block k is vals[m * vstride + k], vstride >= nnzb.
+// block k is vals[m * vstride + k], vstride >= nnzb.  vstride == kTiledBcsr selects the
+// solver's tiled layout instead: tiles of 32 blocks, each nine component rows of 32 values,
+// component m of block k at vals[(k / 32) * 288 + m * 32 + k % 32] (9 * nnzb rounded up to a
+// whole tile).
+constexpr int64_t kTiledBcsr = -1;
 //
 // Assembly: block s = sum over c in [slot_ptr[s], slot_ptr[s+1]) of blocks[contrib[c]]
 // (element blocks: 9 consecutive values, row-major), summed in that fixed order.
@@ -84,7 +88,7 @@ struct PcgBuffers {
     int n_blocks;
     const int32_t* row_ptr;
     const int32_t* cols;
-    const T* vals;      // component-major, stride vals_stride
+    const T* vals;      // component-major with stride vals_stride, or tiled (vals_stride == kTiledBcsr)
     int64_t vals_stride;
     const T* Dinv;
     T* x;
