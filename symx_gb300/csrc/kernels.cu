@@ -385,15 +385,15 @@ __device__ __forceinline__ void st4(double* __restrict__ p, const Row4<double>& 
 // xv(c) is the multiplied vector's block row c.  half_warp_transpose_sum reduces the
 // partials; every lane of the warp must call both (rows past the end pass valid = false), so
 // the full-mask shuffles are converged.
+// The product loop of two_row_products on explicit block ranges [kbA, keA) and [kbB, keB)
+// of `cols` / `vals` (global arrays, or a shared-memory stage indexed from its first block).
 template <typename T, typename L, typename XV>
-__device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bool vB, int lane16,
-                                                 const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
-                                                 const T* __restrict__ vals, L lay, XV xv, T (&a)[3], T (&b)[3])
+__device__ __forceinline__ void two_range_products(int kbA, int keA, int kbB, int keB, int lane16,
+                                                   const int32_t* __restrict__ cols, const T* __restrict__ vals, L lay,
+                                                   XV xv, T (&a)[3], T (&b)[3])
 {
     const int64_t st = lay.step();
     a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = T(0);
-    const int kbA = vA ? row_ptr[rowA] : 0, keA = vA ? row_ptr[rowA + 1] : 0;
-    const int kbB = vB ? row_ptr[rowB] : 0, keB = vB ? row_ptr[rowB + 1] : 0;
     for (int i = lane16;; i += 16) {
         const int kA = kbA + i, kB = kbB + i;
         const bool hA = kA < keA, hB = kB < keB;
@@ -413,6 +413,16 @@ __device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bo
             b[2] += m[6 * st] * v.x + m[7 * st] * v.y + m[8 * st] * v.z;
         }
     }
+}
+
+template <typename T, typename L, typename XV>
+__device__ __forceinline__ void two_row_products(int rowA, bool vA, int rowB, bool vB, int lane16,
+                                                 const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                                                 const T* __restrict__ vals, L lay, XV xv, T (&a)[3], T (&b)[3])
+{
+    const int kbA = vA ? row_ptr[rowA] : 0, keA = vA ? row_ptr[rowA + 1] : 0;
+    const int kbB = vB ? row_ptr[rowB] : 0, keB = vB ? row_ptr[rowB + 1] : 0;
+    two_range_products<T>(kbA, keA, kbB, keB, lane16, cols, vals, lay, xv, a, b);
 }
 
 // Sum the six per-lane partials (a[0..2] of row A, b[0..2] of row B) over the 16 lanes of a
@@ -620,6 +630,185 @@ __global__ void __launch_bounds__(kSpmvThreads, SpmvMinBlocks<T>::value)
         } else {
             st->alpha = st->rz / res[0];
         }
+    }
+}
+
+// ---------------------------------------------------------------- staged SpMV (bulk copies)
+// The same product as k_pcg_spmv (float, strided values), with the matrix streamed through
+// shared memory.  Each block owns a contiguous range of rows, cut into stages of
+// stage_rows rows; a producer thread copies a stage's block range (nine value components,
+// the column indices, the stage's row_ptr entries) with cp.async.bulk into a ring of
+// shared-memory stages, completion counted by an mbarrier per stage ("full"), while the
+// consumer warps (4 rows each per stage, two per half-warp) work on earlier stages and
+// release them through a second mbarrier ("empty").  The consumers' only global loads left
+// on the critical path are the gathers of the direction rows, which hit L2.  Every wait is
+// bounded: a wait that gives up marks the block aborted, the block stops issuing and
+// consuming, waits (bounded) for the copies it issued, and the solve is flagged in
+// PcgState::error.
+constexpr int kStagedConsumerWarps = 15;
+constexpr int kStagedThreads = 32 * (kStagedConsumerWarps + 1);  // warp 0: producer
+constexpr int kStagedRows = 4 * kStagedConsumerWarps;
+constexpr int kStagedMaxStages = 8;
+constexpr long long kMaxBarrierPolls = 1ll << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Wait for the phase of parity `parity` to complete; false after kMaxBarrierPolls polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (long long i = 0; i < kMaxBarrierPolls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// Bytes of one shared-memory stage: nine value slots and one column slot of `cap` entries,
+// then stage_rows + 4 row_ptr entries, rounded to 128.
+__host__ __device__ __forceinline__ size_t staged_stage_bytes(int cap, int stage_rows)
+{
+    return ((size_t)10 * cap * 4 + (size_t)(stage_rows + 4) * 4 + 127) / 128 * 128;
+}
+
+__global__ void __launch_bounds__(kStagedThreads, 1)
+    k_pcg_spmv_staged(PcgBuffers<float> B, const float* __restrict__ p_old, float* __restrict__ p_new, int first)
+{
+    if (B.state->done) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ double sh[32];
+    __shared__ int aborted;
+    const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
+    const size_t stage_bytes = staged_stage_bytes(CAP, S);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* empty = full + kStagedMaxStages;
+    unsigned char* stage0 = smem + 16 * kStagedMaxStages;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row_begin = blockIdx.x * B.staged.rows_per_block;
+    const int row_end = min(row_begin + B.staged.rows_per_block, B.n_blocks);
+    const int n_stages = B.staged.rows_per_block / S;
+    if (threadIdx.x == 0) {
+        aborted = 0;
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(smem_addr(&full[s]), 1);
+            mbar_init(smem_addr(&empty[s]), kStagedConsumerWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    volatile int* abort_flag = &aborted;
+    DotAcc<float> pq;
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int j = 0; j < n_stages && !*abort_flag; ++j) {
+                const int s = j % NS;
+                if (j >= NS && !mbar_wait(smem_addr(&empty[s]), ((j / NS) - 1) & 1)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                const int r0 = row_begin + j * S;
+                const int kb4 = B.staged.row_ptr_ext[r0] & ~3, ke4 = (B.staged.row_ptr_ext[r0 + S] + 3) & ~3;
+                const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
+                unsigned char* st = stage0 + s * stage_bytes;
+                const uint32_t fb = smem_addr(&full[s]);
+                mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
+                if (span) {
+                    for (int m = 0; m < 9; ++m)
+                        bulk_copy_g2s(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4, span, fb);
+                    bulk_copy_g2s(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb);
+                }
+                bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0, (uint32_t)(S + 4) * 4u, fb);
+                issued = j + 1;
+            }
+            if (*abort_flag) {  // let the copies already issued land before the block can exit
+                for (int j = max(0, issued - NS); j < issued; ++j) mbar_wait(smem_addr(&full[j % NS]), (j / NS) & 1);
+            }
+        }
+    } else {
+        const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
+        const float beta = first ? 0.f : (float)B.state->beta;
+        const bool f = first != 0;
+        const float* __restrict__ z = B.z;
+        auto pv = [z, p_old, beta, f](int c) { return direction(z, p_old, beta, f, c); };
+        for (int j = 0; j < n_stages; ++j) {
+            const int s = j % NS;
+            if (*abort_flag || !mbar_wait(smem_addr(&full[s]), (j / NS) & 1)) {
+                *abort_flag = 1;
+                break;
+            }
+            const unsigned char* st = stage0 + s * stage_bytes;
+            const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
+            const int kb4 = rp[0] & ~3;
+            const int r0 = row_begin + j * S;
+            const int la = 4 * cw + half, lb = la + 2;
+            const int rowA = r0 + la, rowB = r0 + lb;
+            const bool vA = rowA < row_end, vB = rowB < row_end;
+            float a[3], b[3];
+            two_range_products<float>(vA ? rp[la] - kb4 : 0, vA ? rp[la + 1] - kb4 : 0, vB ? rp[lb] - kb4 : 0,
+                                      vB ? rp[lb + 1] - kb4 : 0, lane16,
+                                      reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4),
+                                      reinterpret_cast<const float*>(st), StridedBcsr{CAP}, pv, a, b);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&empty[s]));
+            const float qd = half_warp_transpose_sum<float>(a, b, lane16);
+            const int idx = lane16 >> 1;  // 0..2 row A, 3..5 row B
+            if (!(lane16 & 1) && idx < 6) {
+                const int row = idx < 3 ? rowA : rowB, d = idx % 3;
+                if (idx < 3 ? vA : vB) {
+                    const int64_t o = 4 * (int64_t)row + d;
+                    const float pd = f ? z[o] : fmaf(beta, p_old[o], z[o]);  // the bits direction() gives
+                    p_new[o] = pd;
+                    B.q[o] = qd;
+                    pq.add_prod(pd, qd);
+                }
+            }
+        }
+    }
+    const double bpq[1] = {pq.block_sum(sh)};
+    __syncthreads();
+    const int block_aborted = *abort_flag;
+    double res[1];
+    if (publish_and_combine<1>(bpq, B.partials, B.tickets, res) && threadIdx.x == 0) {
+        PcgState* st = B.state;
+        st->pAp = res[0];
+        if (!(res[0] > 0.0)) {  // indefinite (or NaN): stop as the reference does
+            st->indefinite = 1;
+            st->converged = 0;
+            st->done = 1;
+            st->iteration += 1;
+        } else {
+            st->alpha = st->rz / res[0];
+        }
+    }
+    if (block_aborted && threadIdx.x == 0) {
+        B.state->wait_failed = 1;
+        B.state->converged = 0;
+        B.state->done = 1;
     }
 }
 
@@ -963,8 +1152,69 @@ void launch_pcg_spmv_l(const PcgBuffers<T>& B, L lay, int iteration, cudaStream_
 template <typename T>
 void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 {
+    if constexpr (std::is_same<T, float>::value) {
+        if (B.staged.stages > 0 && B.vals_stride != kTiledBcsr) {
+            float* p_old = (iteration & 1) ? B.p : B.p2;
+            float* p_new = (iteration & 1) ? B.p2 : B.p;
+            k_pcg_spmv_staged<<<B.staged.grid, kStagedThreads, B.staged.smem_bytes, s>>>(B, p_old, p_new,
+                                                                                        iteration == 0 ? 1 : 0);
+            check_launch("pcg_spmv_staged");
+            return;
+        }
+    }
     if (B.vals_stride == kTiledBcsr) launch_pcg_spmv_l<T>(B, TiledBcsr{}, iteration, s);
     else launch_pcg_spmv_l<T>(B, StridedBcsr{B.vals_stride}, iteration, s);
+}
+
+StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged& st)
+{
+    st = PcgBuffers<float>::Staged{};
+    StagedSizes none;
+    if (n <= 0) return none;
+    int dev = 0, sms = 0, optin = 0, per_sm_bytes = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return none;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const int S = kStagedRows;
+    const int64_t nnzb = rp[n];
+    for (int per_sm : {2, 1}) {
+        const int64_t grid = (int64_t)sms * per_sm;
+        const int64_t rows = ((n + grid - 1) / grid + S - 1) / S * S;
+        int64_t cap = 4;
+        for (int64_t r0 = 0; r0 < grid * rows; r0 += S) {
+            const int64_t kb = rp[std::min<int64_t>(r0, n)], ke = rp[std::min<int64_t>(r0 + S, n)];
+            cap = std::max<int64_t>(cap, ((ke + 3) & ~int64_t(3)) - (kb & ~int64_t(3)));
+        }
+        const size_t stage_bytes = staged_stage_bytes((int)cap, S);
+        const int64_t budget =
+            std::min<int64_t>(optin, per_sm_bytes / per_sm - 1024) - 16 * kStagedMaxStages - 1024;  // static smem
+        const int stages = (int)std::min<int64_t>(kStagedMaxStages, budget / (int64_t)stage_bytes);
+        if (stages < 2 || cap > (1 << 24)) continue;
+        const size_t smem = 16 * kStagedMaxStages + (size_t)stages * stage_bytes;
+        if (cudaFuncSetAttribute(k_pcg_spmv_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        int resident = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_pcg_spmv_staged, kStagedThreads, smem) !=
+                cudaSuccess ||
+            resident < per_sm) {
+            cudaGetLastError();
+            continue;
+        }
+        st.stages = stages;
+        st.stage_rows = S;
+        st.stage_cap = (int)cap;
+        st.rows_per_block = (int)rows;
+        st.grid = (int)grid;
+        st.smem_bytes = smem;
+        StagedSizes z;
+        z.row_ptr_ext = grid * rows + S + 8;
+        z.cols_ext = ((nnzb + 3) & ~int64_t(3)) + 4;
+        return z;
+    }
+    return none;
 }
 
 template <typename T>

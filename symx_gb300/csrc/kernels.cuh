@@ -25,7 +25,7 @@ struct PcgState {
     int done;         // 1 once converged, failed or out of iterations
     int converged;
     int indefinite;
-    int pad;
+    int wait_failed;  // 1 if a bounded wait inside a kernel gave up (the solve is invalid)
 };
 
 // Deterministic reductions: each launch uses a fixed grid, every block sums a fixed
@@ -100,6 +100,18 @@ struct PcgBuffers {
     double* partials;   // kPcgPartials doubles x 2
     unsigned* tickets;  // 4 counters
     PcgState* state;
+    // Staged SpMV (float, strided layout only; stages == 0: not used).  The producer copies
+    // each stage's rows with bulk copies, which read these padded copies of row_ptr and cols.
+    struct Staged {
+        int stages = 0;          // shared-memory stages per block
+        int stage_rows = 0;      // rows per stage (4 per consumer warp)
+        int stage_cap = 0;       // values per component slot in a stage (multiple of 4)
+        int rows_per_block = 0;  // multiple of stage_rows
+        int grid = 0;
+        size_t smem_bytes = 0;
+        const int32_t* row_ptr_ext = nullptr;  // row_ptr, then nnzb repeated to grid * rows_per_block + stage_rows + 8
+        const int32_t* cols_ext = nullptr;     // cols, padded with zeros to a multiple of 4 plus 4
+    } staged;
 };
 constexpr int kPcgMaxPartials = 1 << 16;
 
@@ -131,6 +143,15 @@ template <typename T>
 void launch_rows4_to_vec3(int n_rows, const T* in4, T* out3, cudaStream_t s);
 // Largest grid any PCG kernel launches with (the number of per-block partials it writes).
 unsigned pcg_max_grid();
+
+// Plan of the staged (bulk-copy) PCG SpMV for a float matrix with n_blocks rows whose
+// row_ptr (host copy) is given: fills everything in `st` but the two device pointers, and
+// returns the lengths the padded row_ptr and cols copies need (0, 0 when the staged kernel
+// cannot run on this device or matrix, which then keeps the plain kernel).
+struct StagedSizes {
+    int64_t row_ptr_ext = 0, cols_ext = 0;
+};
+StagedSizes plan_staged_spmv(int n_blocks, const int32_t* row_ptr_host, PcgBuffers<float>::Staged& st);
 
 // On the PCG solution du (4 values per block row) and double vectors with 3 per row:
 // out = du . g;  out = max |du|;  x_out = x0 + step * du.

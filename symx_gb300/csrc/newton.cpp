@@ -388,6 +388,9 @@ struct SolverImpl {
     int64_t n_elements_total = 0, n_gblocks = 0, n_hblocks = 0;
 
     DevBuf<int32_t> row_ptr, cols, diag_slot, contrib, gcontrib;
+    // staged (bulk-copy) float SpMV: its plan and the padded row_ptr / cols it copies from
+    symxg::PcgBuffers<float>::Staged staged;
+    DevBuf<int32_t> row_ptr_ext, cols_ext;
     DevBuf<int64_t> slot_ptr, gptr;
     int64_t nnzb = 0;
     DevBuf<float> vals32, Dinv32;
@@ -649,6 +652,18 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     };
     up(I.row_ptr, row_ptr);
     up(I.cols, cols);
+    {
+        const symxg::StagedSizes ss = symxg::plan_staged_spmv(nbk, row_ptr.data(), I.staged);
+        if (ss.row_ptr_ext > 0) {
+            std::vector<int32_t> rpx(ss.row_ptr_ext, (int32_t)I.nnzb), cx(ss.cols_ext, 0);
+            std::copy(row_ptr.begin(), row_ptr.end(), rpx.begin());
+            std::copy(cols.begin(), cols.end(), cx.begin());
+            up(I.row_ptr_ext, rpx);
+            up(I.cols_ext, cx);
+            I.staged.row_ptr_ext = I.row_ptr_ext.p;
+            I.staged.cols_ext = I.cols_ext.p;
+        }
+    }
     up(I.diag_slot, diag);
     up(I.slot_ptr, sptr);
     up(I.contrib, contrib);
@@ -899,6 +914,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     B.partials = I.partials.p;
     B.tickets = I.tickets.p;
     B.state = I.pcg_state.p;
+    if constexpr (std::is_same<T, float>::value) B.staged = I.staged;
     T* du = V[0].p;
 
     if (S.projection_mode != ProjectionToPD::ProjectedNewton && S.projection_mode != ProjectionToPD::Newton)
@@ -995,6 +1011,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         }
         timer.stop();
         const PcgState ps = *I.h_state;
+        if (ps.wait_failed) throw std::runtime_error("symx_gb300: a bounded wait in the PCG SpMV gave up");
         if (S.time_kernels) {
             auto& kt = st.kernels[std::string("pcg_spmv_") + (sizeof(T) == 4 ? "f32" : "f64")];
             for (size_t k = 0; k < spmv_ev.size(); ++k) {
