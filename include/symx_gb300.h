@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SYMXG_ABI_VERSION 1
+#define SYMXG_ABI_VERSION 2
 
 /* status codes */
 #define SYMXG_OK 0
@@ -111,6 +111,8 @@ typedef struct symxg_solve_stats {
     double spmv_seconds;             /* ... and their summed device time */
     int64_t project_launches;        /* with time_kernels: 12x12 projection launches ... */
     double project_seconds;          /* ... and their summed device time */
+    int64_t pcg_solve_iterations;    /* with time_kernels: PCG iterations run by the one-launch PCG ... */
+    double pcg_solve_seconds;        /* ... and the device time of those launches */
 } symxg_solve_stats;
 
 /* message of the last failing call on this thread ("" if none) */

@@ -65,6 +65,7 @@ class SolveStats(C.Structure):
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
         ("spmv_launches", C.c_int64), ("spmv_seconds", C.c_double),
         ("project_launches", C.c_int64), ("project_seconds", C.c_double),
+        ("pcg_solve_iterations", C.c_int64), ("pcg_solve_seconds", C.c_double),
     ]
 
     def as_dict(self):

@@ -147,6 +147,9 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
         } else if (kv.first.rfind("project_pd", 0) == 0) {
             o->project_launches += kv.second.first;
             o->project_seconds += kv.second.second;
+        } else if (kv.first.rfind("pcg_solve", 0) == 0) {
+            o->pcg_solve_iterations += kv.second.first;
+            o->pcg_solve_seconds += kv.second.second;
         }
     }
 }

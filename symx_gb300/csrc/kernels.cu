@@ -580,6 +580,19 @@ __device__ __forceinline__ Row4<T> direction(const T* __restrict__ z, const T* _
     const Row4<T> pp = ld4(p_old + 4 * i);
     return Row4<T>{fma(beta, pp.x, zz.x), fma(beta, pp.y, zz.y), fma(beta, pp.z, zz.z), T(0)};
 }
+// The same with loads that bypass L1 (for vectors other blocks of the same launch wrote).
+__device__ __forceinline__ Row4<float> ld4cg(const float* p)
+{
+    const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+    return Row4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Row4<float> direction_cg(const float* z, const float* p_old, float beta, bool first, int i)
+{
+    const Row4<float> zz = ld4cg(z + 4 * i);
+    if (first) return zz;
+    const Row4<float> pp = ld4cg(p_old + 4 * i);
+    return Row4<float>{fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y), fmaf(beta, pp.z, zz.z), 0.f};
+}
 
 // PCG step 1: p = z + beta p_old (fused), q = A p, p.q.  Grid sized to the resident
 // blocks; each warp takes four block rows per pass.
@@ -695,47 +708,68 @@ __host__ __device__ __forceinline__ size_t staged_stage_bytes(int cap, int stage
     return ((size_t)10 * cap * 4 + (size_t)(stage_rows + 4) * 4 + 127) / 128 * 128;
 }
 
-__global__ void __launch_bounds__(kStagedThreads, 1)
-    k_pcg_spmv_staged(PcgBuffers<float> B, const float* __restrict__ p_old, float* __restrict__ p_new, int first)
+// Shared-memory layout of a staged block: full barriers, empty barriers (kStagedMaxStages
+// each), then the ring of stages.
+struct StagedShared {
+    uint64_t* full;
+    uint64_t* empty;
+    unsigned char* stage0;
+};
+__device__ __forceinline__ StagedShared staged_shared(unsigned char* smem)
 {
-    if (B.state->done) return;
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ double sh[32];
-    __shared__ int aborted;
+    StagedShared ss;
+    ss.full = reinterpret_cast<uint64_t*>(smem);
+    ss.empty = ss.full + kStagedMaxStages;
+    ss.stage0 = smem + 16 * kStagedMaxStages;
+    return ss;
+}
+__device__ __forceinline__ void staged_init_barriers(const StagedShared& ss, int stages)
+{
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(smem_addr(&ss.full[s]), 1);
+            mbar_init(smem_addr(&ss.empty[s]), kStagedConsumerWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+}
+
+// One pass of the staged product over this block's rows: p = z + beta p_old (fused into
+// the gathers; the owning lane stores p_new), q = A p, and this thread's share of p.q.
+// Stages are numbered over the whole launch (pass after pass; the matrix does not change):
+// `seq` is the first stage of this pass and advances by the pass's stage count in every
+// thread; `issued` (producer thread) counts the stages copied so far.  With run_ahead the
+// producer goes on into the next pass's stages until the ring is full, so the next pass
+// starts on stages already in shared memory; the caller then waits for them before the
+// block exits (staged_drain).  kCg: read the direction vectors through L2 only (they were
+// written by other blocks of the same launch).  Sets *abort_flag when a wait gives up.
+template <bool kCg>
+__device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, const StagedShared& ss,
+                                                 const float* __restrict__ p_old, float* __restrict__ p_new, bool first,
+                                                 float beta, unsigned& seq, unsigned& issued, bool run_ahead,
+                                                 volatile int* abort_flag, DotAcc<float>& pq)
+{
     const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
     const size_t stage_bytes = staged_stage_bytes(CAP, S);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-    uint64_t* empty = full + kStagedMaxStages;
-    unsigned char* stage0 = smem + 16 * kStagedMaxStages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row_begin = blockIdx.x * B.staged.rows_per_block;
     const int row_end = min(row_begin + B.staged.rows_per_block, B.n_blocks);
     const int n_stages = B.staged.rows_per_block / S;
-    if (threadIdx.x == 0) {
-        aborted = 0;
-        for (int s = 0; s < NS; ++s) {
-            mbar_init(smem_addr(&full[s]), 1);
-            mbar_init(smem_addr(&empty[s]), kStagedConsumerWarps);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    volatile int* abort_flag = &aborted;
-    DotAcc<float> pq;
     if (warp == 0) {
         if (lane == 0) {
-            int issued = 0;
-            for (int j = 0; j < n_stages && !*abort_flag; ++j) {
-                const int s = j % NS;
-                if (j >= NS && !mbar_wait(smem_addr(&empty[s]), ((j / NS) - 1) & 1)) {
+            const unsigned last = seq + n_stages + (run_ahead ? NS : 0);  // one past the last stage to copy now
+            for (unsigned g = issued; g < last && !*abort_flag; ++g) {
+                const unsigned s = g % NS, use = g / NS;
+                const int j = (int)(g % (unsigned)n_stages);
+                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1)) {
                     *abort_flag = 1;
                     break;
                 }
                 const int r0 = row_begin + j * S;
                 const int kb4 = B.staged.row_ptr_ext[r0] & ~3, ke4 = (B.staged.row_ptr_ext[r0 + S] + 3) & ~3;
                 const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
-                unsigned char* st = stage0 + s * stage_bytes;
-                const uint32_t fb = smem_addr(&full[s]);
+                unsigned char* st = ss.stage0 + s * stage_bytes;
+                const uint32_t fb = smem_addr(&ss.full[s]);
                 mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
                 if (span) {
                     for (int m = 0; m < 9; ++m)
@@ -743,25 +777,22 @@ __global__ void __launch_bounds__(kStagedThreads, 1)
                     bulk_copy_g2s(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb);
                 }
                 bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0, (uint32_t)(S + 4) * 4u, fb);
-                issued = j + 1;
-            }
-            if (*abort_flag) {  // let the copies already issued land before the block can exit
-                for (int j = max(0, issued - NS); j < issued; ++j) mbar_wait(smem_addr(&full[j % NS]), (j / NS) & 1);
+                issued = g + 1;
             }
         }
     } else {
         const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
-        const float beta = first ? 0.f : (float)B.state->beta;
-        const bool f = first != 0;
         const float* __restrict__ z = B.z;
-        auto pv = [z, p_old, beta, f](int c) { return direction(z, p_old, beta, f, c); };
+        auto pv = [z, p_old, beta, first](int c) {
+            return kCg ? direction_cg(z, p_old, beta, first, c) : direction(z, p_old, beta, first, c);
+        };
         for (int j = 0; j < n_stages; ++j) {
-            const int s = j % NS;
-            if (*abort_flag || !mbar_wait(smem_addr(&full[s]), (j / NS) & 1)) {
+            const unsigned g = seq + j, s = g % NS;
+            if (*abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1)) {
                 *abort_flag = 1;
                 break;
             }
-            const unsigned char* st = stage0 + s * stage_bytes;
+            const unsigned char* st = ss.stage0 + s * stage_bytes;
             const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
             const int kb4 = rp[0] & ~3;
             const int r0 = row_begin + j * S;
@@ -774,14 +805,15 @@ __global__ void __launch_bounds__(kStagedThreads, 1)
                                       reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4),
                                       reinterpret_cast<const float*>(st), StridedBcsr{CAP}, pv, a, b);
             __syncwarp();
-            if (lane == 0) mbar_arrive(smem_addr(&empty[s]));
+            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
             const float qd = half_warp_transpose_sum<float>(a, b, lane16);
             const int idx = lane16 >> 1;  // 0..2 row A, 3..5 row B
             if (!(lane16 & 1) && idx < 6) {
                 const int row = idx < 3 ? rowA : rowB, d = idx % 3;
                 if (idx < 3 ? vA : vB) {
                     const int64_t o = 4 * (int64_t)row + d;
-                    const float pd = f ? z[o] : fmaf(beta, p_old[o], z[o]);  // the bits direction() gives
+                    const float zo = kCg ? __ldcg(z + o) : z[o];
+                    const float pd = first ? zo : fmaf(beta, kCg ? __ldcg(p_old + o) : p_old[o], zo);  // direction()'s bits
                     p_new[o] = pd;
                     B.q[o] = qd;
                     pq.add_prod(pd, qd);
@@ -789,6 +821,38 @@ __global__ void __launch_bounds__(kStagedThreads, 1)
             }
         }
     }
+    seq += n_stages;
+}
+
+// Producer thread: wait (bounded) until the last stages it copied have landed, so no bulk
+// copy is still writing this block's shared memory when it exits.  Only the last `stages`
+// copies can be in flight (a slot is reused only after its previous stage was consumed), and
+// each is the latest use of its slot, so waiting on its own phase parity is exact.
+__device__ __forceinline__ void staged_drain(const PcgBuffers<float>& B, const StagedShared& ss, unsigned issued)
+{
+    if (threadIdx.x != 0) return;
+    const unsigned NS = (unsigned)B.staged.stages;
+    for (unsigned g = issued > NS ? issued - NS : 0; g < issued; ++g)
+        mbar_wait(smem_addr(&ss.full[g % NS]), (g / NS) & 1);
+}
+
+__global__ void __launch_bounds__(kStagedThreads, 1)
+    k_pcg_spmv_staged(PcgBuffers<float> B, const float* __restrict__ p_old, float* __restrict__ p_new, int first)
+{
+    if (B.state->done) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ double sh[32];
+    __shared__ int aborted;
+    const StagedShared ss = staged_shared(smem);
+    if (threadIdx.x == 0) aborted = 0;
+    staged_init_barriers(ss, B.staged.stages);
+    __syncthreads();
+    volatile int* abort_flag = &aborted;
+    DotAcc<float> pq;
+    unsigned seq = 0, issued = 0;
+    staged_spmv_pass<false>(B, ss, p_old, p_new, first != 0, first ? 0.f : (float)B.state->beta, seq, issued, false,
+                            abort_flag, pq);
+    if (*abort_flag) staged_drain(B, ss, issued);
     const double bpq[1] = {pq.block_sum(sh)};
     __syncthreads();
     const int block_aborted = *abort_flag;
@@ -867,6 +931,204 @@ __global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __
             st->beta = res[1] / st->rz;
             st->rz = res[1];
         }
+    }
+}
+
+// ---------------------------------------------------------------- persistent PCG
+// The whole PCG loop in one cooperative launch (all blocks resident): per iteration the
+// staged product pass, a grid barrier, p.Ap from every block's partial (each block sums the
+// partials itself in index order, so all blocks hold the same alpha), the update of the
+// block's own rows (x, r, z, r.r, r.z), a second grid barrier, and the convergence test and
+// beta, computed identically in every block.  The iteration and its stopping rules are
+// those of k_pcg_spmv + k_pcg_update.  Plain (L1-cached) loads are safe across iterations:
+// the barrier's acquire at GPU scope, ordered before every thread of the block by
+// __syncthreads, makes the other blocks' writes visible to them (the guarantee a grid
+// synchronization gives).  Grid barrier words: bar[0] counts arrivals over the
+// whole launch, bar[1] is the released generation; both are zero at launch.  Every wait is
+// bounded; a block that gives up flags PcgState::wait_failed and leaves the loop.
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* ok_flag)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned target = generation + 1;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&bar[0], 1u) + 1u;
+        if (arrived == gridDim.x * target) {
+            __threadfence();
+            atomicExch(&bar[1], target);
+        }
+        bool ok = true;
+        for (long long polls = 0; ld_acquire(&bar[1]) < target; ++polls) {
+            if (polls > kMaxBarrierPolls) {
+                ok = false;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        *ok_flag = ok ? 1 : 0;
+    }
+    __syncthreads();
+    generation += 1;
+    return *ok_flag != 0;
+}
+
+// Sum over the gridDim.x partials, in index order and the same tree in every block.
+__device__ double sum_grid_partials(const double* partials, double* sh)
+{
+    double v = 0.0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) v += __ldcg(partials + i);
+    v = block_reduce<false>(v, sh);
+    __shared__ double result;
+    if (threadIdx.x == 0) result = v;
+    __syncthreads();
+    return result;
+}
+
+// The same for two partial arrays at once (one pass over both, two block reductions).
+__device__ void sum_grid_partials2(const double* pa, const double* pb, double* sh, double& a, double& b)
+{
+    double va = 0.0, vb = 0.0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+        va += __ldcg(pa + i);
+        vb += __ldcg(pb + i);
+    }
+    va = block_reduce<false>(va, sh);
+    __shared__ double result[2];
+    if (threadIdx.x == 0) result[0] = va;
+    vb = block_reduce<false>(vb, sh);
+    if (threadIdx.x == 0) result[1] = vb;
+    __syncthreads();
+    a = result[0];
+    b = result[1];
+}
+
+__global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffers<float> B)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ double sh[32];
+    __shared__ int aborted, barrier_ok;
+    __shared__ PcgState st0;  // as k_pcg_init left it (an earlier launch)
+    if (threadIdx.x == 0) st0 = *B.state;
+    __syncthreads();
+    if (st0.done) return;
+    const StagedShared ss = staged_shared(smem);
+    if (threadIdx.x == 0) aborted = 0;
+    staged_init_barriers(ss, B.staged.stages);
+    __syncthreads();
+    volatile int* abort_flag = &aborted;
+    unsigned* bar = B.tickets + 6;
+    unsigned generation = 0, seq = 0, issued = 0;
+    const unsigned G = gridDim.x;
+    double* part_pq = B.partials;
+    double* part_rr = B.partials + G;
+    double* part_rz = B.partials + 2 * G;
+    const int row_begin = blockIdx.x * B.staged.rows_per_block;
+    const int row_end = min(row_begin + B.staged.rows_per_block, B.n_blocks);
+    double rz = st0.rz, alpha = 0.0, beta = 0.0, pAp = 0.0, rr = 0.0, error = st0.error;
+    int iteration = st0.iteration, converged = 0, indefinite = 0;
+    bool failed = false;
+    while (true) {
+        float* p_old = (iteration & 1) ? B.p : B.p2;
+        float* p_new = (iteration & 1) ? B.p2 : B.p;
+        const bool first = iteration == 0;
+        DotAcc<float> pq;
+        staged_spmv_pass<false>(B, ss, p_old, p_new, first, first ? 0.f : (float)beta, seq, issued, true, abort_flag,
+                                pq);
+        const double bpq = pq.block_sum(sh);
+        if (threadIdx.x == 0) part_pq[blockIdx.x] = bpq;
+        if (!grid_barrier(bar, generation, &barrier_ok) || *abort_flag) {
+            failed = true;
+            break;
+        }
+        pAp = sum_grid_partials(part_pq, sh);
+        if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
+            indefinite = 1;
+            iteration += 1;
+            break;
+        }
+        alpha = rz / pAp;
+        const float a = (float)alpha;
+        DotAcc<float> rra, rza;
+        // two rows per thread and pass, all loads of both issued before either row's math
+        for (int i = row_begin + (int)threadIdx.x; i < row_end; i += 2 * blockDim.x) {
+            const int j = i + blockDim.x;
+            const bool has_j = j < row_end;
+            Row4<float> xs[2], rs[2], ps[2], qs[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (k == 1 && !has_j) break;
+                const int row = k ? j : i;
+                xs[k] = ld4(B.x + 4 * row);
+                rs[k] = ld4(B.r + 4 * row);
+                ps[k] = ld4(p_new + 4 * row);
+                qs[k] = ld4(B.q + 4 * row);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (k == 1 && !has_j) break;
+                const int row = k ? j : i;
+                Row4<float> x = xs[k], r = rs[k];
+                x.x = fmaf(a, ps[k].x, x.x);
+                x.y = fmaf(a, ps[k].y, x.y);
+                x.z = fmaf(a, ps[k].z, x.z);
+                r.x = fmaf(-a, qs[k].x, r.x);
+                r.y = fmaf(-a, qs[k].y, r.y);
+                r.z = fmaf(-a, qs[k].z, r.z);
+                const Row4<float> z = apply_block_jacobi(B.Dinv, row, r);
+                st4(B.x + 4 * row, x);
+                st4(B.r + 4 * row, r);
+                st4(B.z + 4 * row, z);
+                rra.add_prod(r.x, r.x);
+                rra.add_prod(r.y, r.y);
+                rra.add_prod(r.z, r.z);
+                rza.add_prod(r.x, z.x);
+                rza.add_prod(r.y, z.y);
+                rza.add_prod(r.z, z.z);
+            }
+        }
+        const double brr = rra.block_sum(sh);
+        const double brz = rza.block_sum(sh);
+        if (threadIdx.x == 0) {
+            part_rr[blockIdx.x] = brr;
+            part_rz[blockIdx.x] = brz;
+        }
+        if (!grid_barrier(bar, generation, &barrier_ok)) {
+            failed = true;
+            break;
+        }
+        double rz_new;
+        sum_grid_partials2(part_rr, part_rz, sh, rr, rz_new);
+        iteration += 1;
+        error = sqrt(rr / st0.bb);
+        if (error < st0.abs_tol || error / st0.error0 < st0.rel_tol) {
+            converged = 1;
+            break;
+        }
+        if (iteration >= st0.max_iterations) break;
+        beta = rz_new / rz;
+        rz = rz_new;
+    }
+    staged_drain(B, ss, issued);  // stages copied ahead for a pass that will not run
+    if (failed && threadIdx.x == 0) atomicExch(&B.state->wait_failed, 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !failed) {
+        PcgState* st = B.state;
+        st->iteration = iteration;
+        st->converged = converged;
+        st->indefinite = indefinite;
+        st->done = 1;
+        st->pAp = pAp;
+        st->alpha = alpha;
+        st->beta = beta;
+        st->rz = rz;
+        st->rr = rr;
+        st->error = error;
     }
 }
 
@@ -1166,6 +1428,20 @@ void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
     else launch_pcg_spmv_l<T>(B, StridedBcsr{B.vals_stride}, iteration, s);
 }
 
+void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s)
+{
+    if (!B.staged.persistent) throw std::runtime_error("symx_gb300: persistent PCG not planned for this matrix");
+    const cudaError_t e = cudaMemsetAsync(B.tickets + 6, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
+    PcgBuffers<float> arg = B;
+    void* args[] = {&arg};
+    const cudaError_t l = cudaLaunchCooperativeKernel((const void*)k_pcg_solve_staged, dim3(B.staged.grid),
+                                                      dim3(kStagedThreads), args, B.staged.smem_bytes, s);
+    if (l != cudaSuccess)
+        throw std::runtime_error(std::string("symx_gb300: cooperative launch of the PCG failed: ") + cudaGetErrorString(l));
+    check_launch("pcg_solve_staged");
+}
+
 StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged& st)
 {
     st = PcgBuffers<float>::Staged{};
@@ -1203,6 +1479,17 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
             cudaGetLastError();
             continue;
         }
+        // the persistent form needs every block resident at once (cooperative launch)
+        int coop = 0, resident_solve = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        if (coop &&
+            cudaFuncSetAttribute(k_pcg_solve_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+                cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_solve, k_pcg_solve_staged, kStagedThreads, smem) ==
+                cudaSuccess &&
+            resident_solve >= per_sm && 3 * grid <= 2 * kPcgMaxPartials)
+            st.persistent = 1;
+        cudaGetLastError();
         st.stages = stages;
         st.stage_rows = S;
         st.stage_cap = (int)cap;

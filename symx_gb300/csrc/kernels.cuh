@@ -109,6 +109,7 @@ struct PcgBuffers {
         int rows_per_block = 0;  // multiple of stage_rows
         int grid = 0;
         size_t smem_bytes = 0;
+        int persistent = 0;      // 1: the whole PCG loop can run as one cooperative launch
         const int32_t* row_ptr_ext = nullptr;  // row_ptr, then nnzb repeated to grid * rows_per_block + stage_rows + 8
         const int32_t* cols_ext = nullptr;     // cols, padded with zeros to a multiple of 4 plus 4
     } staged;
@@ -152,6 +153,11 @@ struct StagedSizes {
     int64_t row_ptr_ext = 0, cols_ext = 0;
 };
 StagedSizes plan_staged_spmv(int n_blocks, const int32_t* row_ptr_host, PcgBuffers<float>::Staged& st);
+
+// All PCG iterations (after launch_pcg_init) in one cooperative launch of the staged kernel:
+// runs until convergence, p.Ap <= 0 or state->max_iterations, then sets state->done.  Only
+// when B.staged.persistent; uses tickets[6..7] (cleared here) as its grid barrier.
+void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s);
 
 // On the PCG solution du (4 values per block row) and double vectors with 3 per row:
 // out = du . g;  out = max |du|;  x_out = x0 + step * du.

@@ -988,7 +988,30 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         symxg::launch_pcg_init<T>(B, I.grad.p, s);
         int launched = 0, chunk = 8;
         std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spmv_ev;
-        while (true) {
+        bool persistent = false;
+        if constexpr (std::is_same<T, float>::value) persistent = B.staged.persistent != 0;
+        if (persistent) {  // every iteration in one cooperative launch
+            cudaEvent_t a = nullptr, b = nullptr;
+            if (S.time_kernels) {
+                cudaEventCreate(&a);
+                cudaEventCreate(&b);
+                cudaEventRecord(a, s);
+            }
+            if constexpr (std::is_same<T, float>::value) symxg::launch_pcg_solve_persistent(B, s);
+            if (S.time_kernels) cudaEventRecord(b, s);
+            ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
+            ck(cudaStreamSynchronize(s), "synchronize");
+            if (S.time_kernels) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                auto& kt = st.kernels["pcg_solve_f32"];
+                kt.first += I.h_state->iteration;
+                kt.second += ms * 1e-3;
+                cudaEventDestroy(a);
+                cudaEventDestroy(b);
+            }
+        }
+        while (!persistent) {
             for (int k = 0; k < chunk; ++k) {
                 if (S.time_kernels) {
                     cudaEvent_t a, b;
@@ -1011,7 +1034,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
         }
         timer.stop();
         const PcgState ps = *I.h_state;
-        if (ps.wait_failed) throw std::runtime_error("symx_gb300: a bounded wait in the PCG SpMV gave up");
+        if (ps.wait_failed) throw std::runtime_error("symx_gb300: a bounded wait in the PCG kernels gave up");
         if (S.time_kernels) {
             auto& kt = st.kernels[std::string("pcg_spmv_") + (sizeof(T) == 4 ? "f32" : "f64")];
             for (size_t k = 0; k < spmv_ev.size(); ++k) {

@@ -131,7 +131,7 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(capi.EXPORTS) == declared
     for name in declared:
         assert hasattr(lib, name), name
-    assert lib.symxg_abi_version() == 1
+    assert lib.symxg_abi_version() == 2
 
 
 def test_invalid_arguments_are_reported(lib):
