@@ -50,7 +50,8 @@ typedef struct symxg_solver symxg_solver;
  * (symx/src/solver/fem_integrators.cpp:52-133), backward-Euler inertia
  * 1/2 m |x - (x0 + dt v0 + dt^2 g)|^2 / dt^2 (examples/dynamic_elasticity_with_contact.cpp:86-103)
  * and penalty Dirichlet 1/2 k |x - target|^2 (examples/rubber_extrusion.cpp:94-107).
- * All arrays are copied at creation. */
+ * With mass given and dt <= 0 the solve is quasistatic: gravity enters as the potential
+ * -m g.x instead of the inertia term.  All arrays are copied at creation. */
 typedef struct symxg_elastic_problem {
     int32_t n_vertices;
     int32_t n_elements;
@@ -113,6 +114,7 @@ typedef struct symxg_solve_stats {
     double project_seconds;          /* ... and their summed device time */
     int64_t pcg_solve_iterations;    /* with time_kernels: PCG iterations run by the one-launch PCG ... */
     double pcg_solve_seconds;        /* ... and the device time of those launches */
+    int32_t cg_iterations_per_newton[16]; /* PCG iterations of the first 16 linear solves (0 after) */
 } symxg_solve_stats;
 
 /* message of the last failing call on this thread ("" if none) */
@@ -217,6 +219,52 @@ int symxg_bcsr_pcg_f64(int32_t n_blocks, const int32_t* row_ptr, const int32_t* 
 int symxg_bcsr_pcg_f32_noalloc(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
                                int64_t vals_stride, const float* b, float* x, double abs_tol, double rel_tol,
                                int32_t max_iterations, symxg_pcg_info* info, void* stream);
+
+/* ---- adjoint (no counterpart in the reference; an addition of this library) ----
+ *
+ * The state x of a step solves g(x; mu, lambda, x0, v0) = 0 (g the gradient of the step's
+ * energy).  For a loss L(x), with H lambda_adj = dL/dx (H the true Hessian at x), the
+ * gradient of L with respect to any input q of the energy is -lambda_adj . dg/dq; the
+ * mixed derivatives dg/dq are differentiated symbolically from the same potentials. */
+typedef struct symxg_adjoint_info {
+    int32_t converged;
+    int32_t iterations;   /* PCG iterations of the adjoint solve */
+    double error;         /* sqrt(r.r / b.b) at exit */
+} symxg_adjoint_info;
+
+/* At the current device state (after symxg_solve / symxg_solve_device): solve
+ * H lambda = dLdx (n_vertices*3) in the handle's precision (PCG to rel_tol), then
+ * dLdmu[e] = -lambda . dg/dmu_e, dLdlambda[e] = -lambda . dg/dlambda_e (n_elements each),
+ * dLdx0 = -lambda . dg/dx0 and dLdv0 = -lambda . dg/dv0 (n_vertices*3; zero without inertia).
+ * Every output may be NULL.  For E-scaled parameters p_e = ln E_e (mu, lambda proportional
+ * to E_e): dL/dp_e = mu_e dLdmu[e] + lambda_e dLdlambda[e]. */
+int symxg_adjoint(symxg_solver* solver, const double* dLdx, double rel_tol, int32_t max_iterations, double* lambda,
+                  double* dLdmu, double* dLdlambda, double* dLdx0, double* dLdv0, symxg_adjoint_info* info);
+
+typedef struct symxg_rollout_info {
+    int32_t steps;
+    int32_t checkpoints;
+    int32_t newton_iterations;   /* forward solves, including the recomputed ones */
+    int32_t cg_iterations;
+    int32_t recomputed_steps;
+    int32_t adjoint_iterations;  /* PCG iterations of all adjoint solves */
+    double seconds_forward;
+    double seconds_backward;
+} symxg_rollout_info;
+
+/* n_steps implicit-Euler steps from the handle's state (x0, v0 as set by symxg_set_state):
+ * each step runs Newton from x = x0, then x0 <- x, v0 <- (x - x0_old) / dt.  The state before
+ * every checkpoint_every-th step is kept (host memory) for symxg_rollout_backward.  On
+ * return symxg_get_positions gives the final positions. */
+int symxg_rollout_forward(symxg_solver* solver, int32_t n_steps, int32_t checkpoint_every, symxg_rollout_info* info);
+/* Reverse-time adjoint of the last forward rollout for a loss of the final state
+ * (dLdx_final, dLdv_final (may be NULL) with respect to x_N and v_N): recomputes each segment
+ * from its checkpoint, then per step solves H lambda = dL/dx_{n+1} + dL/dv_{n+1} / dt and
+ * propagates through the mixed derivatives to (x_n, v_n) and the material.  Outputs (each
+ * may be NULL): dL/dx_0, dL/dv_0 (n_vertices*3), dL/dmu, dL/dlambda (n_elements). */
+int symxg_rollout_backward(symxg_solver* solver, const double* dLdx_final, const double* dLdv_final, double rel_tol,
+                           int32_t max_iterations, double* dLdx_init, double* dLdv_init, double* dLdmu,
+                           double* dLdlambda, symxg_rollout_info* info);
 
 #ifdef __cplusplus
 }

@@ -26,6 +26,9 @@
 //       (BlockedSparseMatrix.h:1146-1278) and its application (:1280-1361).
 //   * bsm::solve_pcg (solve_pcg.h:82-232): x0 = 0, stop when sqrt(r.r/b.b) < abs_tol or
 //       error/error_0 < rel_tol, stop on p.Ap <= 0.
+//   * Quasistatic form (dt <= 0): gravity as the potential -m g.x instead of the inertia term
+//       (the GPU library's convention; the reference expresses it the same way as a user
+//       potential).
 //   * NewtonsMethod::solve with ProjectedNewton (NewtonsMethod.cpp:28-252), forcing term
 //       (:423-424), descent check (:159-171), step tolerance (:208-215), Armijo line search
 //       (:459-641), residual = max |grad| (solver_utils.h:127).
@@ -413,9 +416,15 @@ double evaluate(Problem& P, double* grad, bool want_hess, double* t_eval)
     }
     double E = 0.0;
     for (int e = 0; e < P.ne; ++e) E += P.Eel[e];
-    const double idt2 = 1.0 / (P.dt * P.dt);
+    // dt > 0: backward-Euler inertia; dt <= 0: quasistatic, gravity as the potential -m g.x
+    const bool quasistatic = !(P.dt > 0.0);
+    const double idt2 = quasistatic ? 0.0 : 1.0 / (P.dt * P.dt);
     double Ein = 0.0;
     for (int v = 0; v < P.nv; ++v) {
+        if (quasistatic) {
+            Ein -= P.mass[v] * (P.g[0] * P.x[3 * v] + P.g[1] * P.x[3 * v + 1] + P.g[2] * P.x[3 * v + 2]);
+            continue;
+        }
         double s = 0;
         for (int d = 0; d < 3; ++d) {
             const double xh = P.x0[3 * v + d] + P.dt * P.v0[3 * v + d] + P.dt * P.dt * P.g[d];
@@ -441,6 +450,10 @@ double evaluate(Problem& P, double* grad, bool want_hess, double* t_eval)
                 for (int d = 0; d < 3; ++d) grad[3 * P.conn[e * nn + a] + d] += P.gel[(size_t)e * n + 3 * a + d];
         for (int v = 0; v < P.nv; ++v)
             for (int d = 0; d < 3; ++d) {
+                if (quasistatic) {
+                    grad[3 * v + d] -= P.mass[v] * P.g[d];
+                    continue;
+                }
                 const double xh = P.x0[3 * v + d] + P.dt * P.v0[3 * v + d] + P.dt * P.dt * P.g[d];
                 grad[3 * v + d] += P.mass[v] * (P.x[3 * v + d] - xh) * idt2;
             }
@@ -492,7 +505,7 @@ void assemble(Problem& P, double* t)
                 for (int i = 0; i < 3; ++i)
                     for (int j = 0; j < 3; ++j) blk[3 * i + j] += h[(3 * a + i) * n + 3 * b + j];
             }
-    const double idt2 = 1.0 / (P.dt * P.dt);
+    const double idt2 = P.dt > 0.0 ? 1.0 / (P.dt * P.dt) : 0.0;  // quasistatic: gravity has no Hessian
     for (int v = 0; v < P.nv; ++v) {
         double* blk = &P.vals[(size_t)P.diag_slot[v] * 9];
         for (int d = 0; d < 3; ++d) blk[4 * d] += P.mass[v] * idt2;
@@ -684,6 +697,15 @@ void* oracle_create(int nv, int ne, int nodes, const int32_t* conn, const double
 }
 
 void oracle_destroy(void* h) { delete static_cast<Problem*>(h); }
+
+// Step inputs x0 (previous positions) and v0 (velocities), 3 per vertex.
+int oracle_set_state(void* h, const double* x0, const double* v0)
+{
+    Problem& P = *static_cast<Problem*>(h);
+    if (x0) P.x0.assign(x0, x0 + 3 * (size_t)P.nv);
+    if (v0) P.v0.assign(v0, v0 + 3 * (size_t)P.nv);
+    return 0;
+}
 
 int oracle_set_x(void* h, const double* x)
 {

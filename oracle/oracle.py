@@ -52,6 +52,7 @@ def lib():
         L.oracle_nh_element_batch.argtypes = [C.c_int, C.c_int, P, P, P, P, P, P, P]
         L.oracle_project_pd_batch.argtypes = [C.c_int, C.c_int, P, C.c_double, C.c_int, P]
         L.oracle_num_threads.restype = C.c_int
+        L.oracle_set_state.argtypes = [P, P, P]
         L.oracle_bcsr_pcg.argtypes = [C.c_int32, P, P, P, P, P, C.c_double, C.c_double, C.c_int32, P, P]
         _lib = L
     return _lib
@@ -136,6 +137,10 @@ class Problem:
         lib().oracle_assemble(self.h, int(project), eps, _p(nnzb), _p(rowptr), _p(cols), _p(vals), _p(eh))
         return rowptr, cols, vals, eh
 
+    def set_state(self, x0=None, v0=None):
+        a = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (x0, v0)]
+        lib().oracle_set_state(self.h, _p(a[0]), _p(a[1]))
+
     def solve(self, settings: Settings | None = None) -> dict:
         s = settings or default_settings()
         st = Stats()
@@ -158,6 +163,76 @@ def bcsr_pcg(rowptr, cols, vals, b, abs_tol, rel_tol, max_iter):
     if rc != 0:
         raise ValueError("a block row has no diagonal block")
     return x, int(it[0]), bool(conv[0])
+
+
+def adjoint(P: "Problem", p: dict, dLdx):
+    """FP64 adjoint at the oracle's current positions: lambda = H^-1 dL/dx with H the true
+    (unprojected) Hessian, solved with a sparse direct factorisation, and the parameter
+    gradients -lambda . dg/dq in closed form: the Neo-Hookean element gradient is linear in
+    (mu, lambda), so dg_e/dmu_e = g_e(mu=1, lambda=0) and dg_e/dlambda_e = g_e(0, 1); the
+    inertia gradient m (x - x0 - dt v0 - dt^2 g) / dt^2 gives -dg/dx0 = m / dt^2 and
+    -dg/dv0 = m / dt.  Returns a dict of lambda, dLdmu, dLdlam, dLdx0, dLdv0 (flat)."""
+    import scipy.sparse.linalg as spla
+
+    rp, cols, vals, _ = P.assemble(project=False)
+    A = bcsr_to_scipy(rp, cols, vals)
+    lam = spla.spsolve(A.tocsc(), np.asarray(dLdx, dtype=np.float64).ravel())
+    x = P.get_x()
+    X, conn = p["X"], p["conn"]
+    ne = conn.shape[0]
+    one, zero = np.ones(ne), np.zeros(ne)
+    _, g_mu, _ = nh_element_batch(x[conn], X[conn], one, zero, want_hess=False)
+    _, g_lam, _ = nh_element_batch(x[conn], X[conn], zero, one, want_hess=False)
+    lam_e = lam.reshape(-1, 3)[conn].reshape(ne, -1)
+    out = {"lambda": lam, "dLdmu": -(lam_e * g_mu).sum(1), "dLdlam": -(lam_e * g_lam).sum(1)}
+    if float(p["dt"]) > 0.0:
+        ml = p["mass"][:, None] * lam.reshape(-1, 3)
+        out["dLdx0"] = (ml / p["dt"] ** 2).ravel()
+        out["dLdv0"] = (ml / p["dt"]).ravel()
+    else:
+        out["dLdx0"] = np.zeros_like(lam)
+        out["dLdv0"] = np.zeros_like(lam)
+    return out
+
+
+def rollout(p: dict, n_steps: int, settings: "Settings"):
+    """Forward implicit-Euler rollout: each step solves from x = x0, then x0 <- x,
+    v0 <- (x - x0_old) / dt.  Returns the states [(x_n, v_n)] for n = 0..n_steps."""
+    P = Problem(p, 1)
+    x0, v0 = np.array(p["x0"], dtype=np.float64), np.array(p["v0"], dtype=np.float64)
+    states = [(x0.copy(), v0.copy())]
+    for _ in range(n_steps):
+        P.set_state(x0, v0)
+        P.set_x(x0)
+        st = P.solve(settings)
+        if not (st["solver_return"] == 0 or (st["solver_return"] == 6 and st["final_residual"] < 1e-7)):
+            raise RuntimeError(f"oracle rollout step did not converge: {st}")
+        x = P.get_x()
+        v0 = (x - x0) / p["dt"]
+        x0 = x
+        states.append((x0.copy(), v0.copy()))
+    return states
+
+
+def rollout_adjoint(p: dict, states, dLdx_final, dLdv_final=None):
+    """Reverse-time adjoint of `rollout` in FP64 (per step the oracle adjoint at the step's
+    solution): returns dL/dx_0, dL/dv_0 (flat) and dL/dmu, dL/dlam (per element)."""
+    dt = float(p["dt"])
+    ax = np.asarray(dLdx_final, dtype=np.float64).ravel().copy()
+    av = np.zeros_like(ax) if dLdv_final is None else np.asarray(dLdv_final, dtype=np.float64).ravel().copy()
+    dmu = np.zeros(p["conn"].shape[0])
+    dlam = np.zeros_like(dmu)
+    P = Problem(p, 1)
+    for n in range(len(states) - 2, -1, -1):
+        (xn, vn), (xn1, _) = states[n], states[n + 1]
+        P.set_state(xn, vn)
+        P.set_x(xn1)
+        q = dict(p, x0=xn, v0=vn)
+        adj = adjoint(P, q, ax + av / dt)
+        dmu += adj["dLdmu"]
+        dlam += adj["dLdlam"]
+        ax, av = adj["dLdx0"] - av / dt, adj["dLdv0"]
+    return {"dLdx0": ax, "dLdv0": av, "dLdmu": dmu, "dLdlam": dlam}
 
 
 def bcsr_to_dense(rowptr, cols, vals):

@@ -151,6 +151,41 @@ class ElasticSolver:
         check(load().symxg_element_outputs(self.h, potential, int(project), _ptr(E), _ptr(g), _ptr(H)))
         return E, g, H
 
+    def adjoint(self, dLdx, rel_tol=1e-10, max_iterations=20000):
+        """symxg_adjoint at the current device state: returns lambda, dLdmu, dLdlam (per
+        element), dLdx0, dLdv0 (per vertex, zero without inertia) and the PCG info."""
+        nd = 3 * self.nv
+        ne = self._keep["conn"].shape[0]
+        b = _f64(dLdx).ravel()
+        out = {"lambda": np.empty(nd), "dLdmu": np.empty(ne), "dLdlam": np.empty(ne), "dLdx0": np.empty(nd),
+               "dLdv0": np.empty(nd)}
+        info = capi.AdjointInfo()
+        check(load().symxg_adjoint(self.h, _ptr(b), float(rel_tol), int(max_iterations), _ptr(out["lambda"]),
+                                   _ptr(out["dLdmu"]), _ptr(out["dLdlam"]), _ptr(out["dLdx0"]), _ptr(out["dLdv0"]),
+                                   C.byref(info)))
+        out["info"] = info.as_dict()
+        return out
+
+    def rollout_forward(self, n_steps, checkpoint_every):
+        info = capi.RolloutInfo()
+        check(load().symxg_rollout_forward(self.h, int(n_steps), int(checkpoint_every), C.byref(info)))
+        return info.as_dict()
+
+    def rollout_backward(self, dLdx_final, dLdv_final=None, rel_tol=1e-10, max_iterations=20000):
+        """Reverse-time adjoint of the last rollout: dL/dx_0, dL/dv_0 (per vertex), dL/dmu,
+        dL/dlam (per element) and the rollout info."""
+        nd = 3 * self.nv
+        ne = self._keep["conn"].shape[0]
+        bx = _f64(dLdx_final).ravel()
+        bv = None if dLdv_final is None else _f64(dLdv_final).ravel()
+        out = {"dLdx0": np.empty(nd), "dLdv0": np.empty(nd), "dLdmu": np.empty(ne), "dLdlam": np.empty(ne)}
+        info = capi.RolloutInfo()
+        check(load().symxg_rollout_backward(self.h, _ptr(bx), _ptr(bv), float(rel_tol), int(max_iterations),
+                                            _ptr(out["dLdx0"]), _ptr(out["dLdv0"]), _ptr(out["dLdmu"]),
+                                            _ptr(out["dLdlam"]), C.byref(info)))
+        out["info"] = info.as_dict()
+        return out
+
     def op_counts(self, potential=0):
         c = np.zeros(3, dtype=np.int64)
         check(load().symxg_op_counts(self.h, potential, _ptr(c)))

@@ -27,7 +27,8 @@ EXPORTS = [
     "symxg_upload", "symxg_solve_device", "symxg_download", "symxg_evaluate", "symxg_evaluate_energy",
     "symxg_assembled_hessian", "symxg_element_outputs", "symxg_op_counts", "symxg_project_pd_f32",
     "symxg_project_pd_f64", "symxg_bcsr_spmv_f32", "symxg_bcsr_spmv_f64", "symxg_launch_count",
-    "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64", "symxg_bcsr_pcg_f32_noalloc",
+    "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64", "symxg_bcsr_pcg_f32_noalloc", "symxg_adjoint",
+    "symxg_rollout_forward", "symxg_rollout_backward",
 ]
 
 
@@ -66,10 +67,12 @@ class SolveStats(C.Structure):
         ("spmv_launches", C.c_int64), ("spmv_seconds", C.c_double),
         ("project_launches", C.c_int64), ("project_seconds", C.c_double),
         ("pcg_solve_iterations", C.c_int64), ("pcg_solve_seconds", C.c_double),
+        ("cg_iterations_per_newton", C.c_int32 * 16),
     ]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["cg_iterations_per_newton"] = [int(v) for v in self.cg_iterations_per_newton if v]
         d["solver_return_name"] = SOLVER_RETURN.get(self.solver_return, str(self.solver_return))
         return d
 
@@ -78,6 +81,24 @@ class PcgInfo(C.Structure):
     _fields_ = [
         ("converged", C.c_int32), ("n_iterations", C.c_int32), ("error", C.c_double),
         ("found_indefiniteness", C.c_int32), ("missing_diagonal", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AdjointInfo(C.Structure):
+    _fields_ = [("converged", C.c_int32), ("iterations", C.c_int32), ("error", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RolloutInfo(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int32), ("checkpoints", C.c_int32), ("newton_iterations", C.c_int32),
+        ("cg_iterations", C.c_int32), ("recomputed_steps", C.c_int32), ("adjoint_iterations", C.c_int32),
+        ("seconds_forward", C.c_double), ("seconds_backward", C.c_double),
     ]
 
     def as_dict(self):
@@ -128,6 +149,9 @@ def load(path: str | None = None):
         "symxg_bcsr_pcg_f32": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
         "symxg_bcsr_pcg_f64": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
         "symxg_bcsr_pcg_f32_noalloc": ([I32, P, P, P, I64, P, P, D, D, I32, C.POINTER(PcgInfo), P], C.c_int),
+        "symxg_adjoint": ([P, P, D, I32, P, P, P, P, P, C.POINTER(AdjointInfo)], C.c_int),
+        "symxg_rollout_forward": ([P, I32, I32, C.POINTER(RolloutInfo)], C.c_int),
+        "symxg_rollout_backward": ([P, P, P, D, I32, P, P, P, P, C.POINTER(RolloutInfo)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -6,6 +6,7 @@
 #include "../../include/symx_gb300.h"
 
 #include <array>
+#include <chrono>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -59,6 +60,9 @@ struct symxg_solver {
     bool has_inertia = false;
     symx::spGlobalPotential G;
     std::unique_ptr<symx::NewtonsMethod> newton;
+    // rollout: (x0, v0) before every checkpoint_every-th step of the last forward rollout
+    std::vector<std::vector<Vec3>> ckpt_x0, ckpt_v0;
+    int rollout_steps = 0, checkpoint_every = 0;
 };
 
 template <typename T>
@@ -139,6 +143,8 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
     o->t_linear_system_solve = get("linear_system_solve");
     o->t_evaluate_P = get("evaluate_P");
     o->h2d_bytes = st.h2d_bytes;
+    for (size_t i = 0; i < st.cg_iterations_per_newton.size() && i < 16; ++i)
+        o->cg_iterations_per_newton[i] = st.cg_iterations_per_newton[i];
     o->d2h_bytes = st.d2h_bytes;
     for (const auto& kv : st.kernels) {
         if (kv.first.rfind("pcg_spmv", 0) == 0) {
@@ -153,6 +159,35 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
         }
     }
 }
+
+namespace {
+
+std::vector<double> flat(const std::vector<Vec3>& v)
+{
+    std::vector<double> out(3 * v.size());
+    std::memcpy(out.data(), v.data(), sizeof(double) * out.size());
+    return out;
+}
+
+// One implicit-Euler step of the handle's problem from (x0, v0): Newton from x = x0, then
+// x0 <- x, v0 <- (x - x0_old) / dt.
+void rollout_step(symxg_solver* s, int n, symxg_rollout_info* info)
+{
+    s->x = s->x0;
+    const symx::SolverReturn r = s->newton->solve();
+    const auto& st = s->newton->get_last_solve_stats();
+    if (info) {
+        info->newton_iterations += st.newton_iterations;
+        info->cg_iterations += st.cg_iterations;
+    }
+    if (r != symx::SolverReturn::Successful)
+        throw std::runtime_error("rollout step " + std::to_string(n) + " did not converge: " + symx::to_string(r));
+    for (size_t i = 0; i < s->x.size(); ++i)
+        for (int d = 0; d < 3; ++d) s->v0[i][d] = (s->x[i][d] - s->x0[i][d]) / s->dt;
+    s->x0 = s->x;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -247,7 +282,14 @@ int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, 
                     return psi * JX.det() * w;
                 });
             });
-        if (S->has_inertia) {
+        if (S->has_inertia && S->dt <= 0.0) {  // quasistatic: gravity as the potential -m g.x
+            S->G->add_potential("gravity", S->vertices, [s](MappedWorkspace<double>& mws, Element& elem) {
+                Vector x = mws.make_vector(s->x, elem[0]);
+                Scalar m = mws.make_scalar(s->mass, elem[0]);
+                Vector g = mws.make_vector(s->gravity);
+                return -m * g.dot(x);
+            });
+        } else if (S->has_inertia) {
             S->G->add_potential("backward_euler_inertia", S->vertices, [s](MappedWorkspace<double>& mws, Element& elem) {
                 Vector x1 = mws.make_vector(s->x, elem[0]);
                 Vector x0 = mws.make_vector(s->x0, elem[0]);
@@ -479,6 +521,134 @@ int symxg_bcsr_pcg_f32_noalloc(int32_t nb, const int32_t* rp, const int32_t* col
         info->found_indefiniteness = r.indefinite;
         info->missing_diagonal = r.missing_diagonal;
         if (r.missing_diagonal) throw std::invalid_argument("block rows without a diagonal block");
+        return SYMXG_OK;
+    });
+}
+
+int symxg_adjoint(symxg_solver* s, const double* dLdx, double rel_tol, int32_t max_iterations, double* lambda,
+                  double* dLdmu, double* dLdlambda, double* dLdx0, double* dLdv0, symxg_adjoint_info* info)
+{
+    return guarded([&] {
+        if (!s || !dLdx) throw std::invalid_argument("null argument");
+        if (!(rel_tol > 0.0) || max_iterations <= 0) throw std::invalid_argument("rel_tol and max_iterations must be positive");
+        const size_t nd = 3 * s->x.size();
+        std::vector<double> lam(nd);
+        const symx::AdjointInfo ai = s->newton->adjoint_solve(dLdx, lam.data(), rel_tol, max_iterations);
+        if (info) {
+            info->converged = ai.converged ? 1 : 0;
+            info->iterations = ai.iterations;
+            info->error = ai.error;
+        }
+        if (lambda) std::memcpy(lambda, lam.data(), sizeof(double) * nd);
+        if (dLdmu) s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->mu), lam.data(), dLdmu, (int64_t)s->mu.size());
+        if (dLdlambda)
+            s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->lam), lam.data(), dLdlambda, (int64_t)s->lam.size());
+        const bool inertia = s->has_inertia && s->dt > 0.0;
+        if (dLdx0) {
+            if (inertia) s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->x0), lam.data(), dLdx0, (int64_t)nd);
+            else std::fill(dLdx0, dLdx0 + nd, 0.0);
+        }
+        if (dLdv0) {
+            if (inertia) s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->v0), lam.data(), dLdv0, (int64_t)nd);
+            else std::fill(dLdv0, dLdv0 + nd, 0.0);
+        }
+        if (!ai.converged) throw std::runtime_error("adjoint PCG did not converge (" + std::to_string(ai.iterations) + " iterations)");
+        return SYMXG_OK;
+    });
+}
+
+int symxg_rollout_forward(symxg_solver* s, int32_t n_steps, int32_t checkpoint_every, symxg_rollout_info* info)
+{
+    return guarded([&] {
+        if (!s) throw std::invalid_argument("null argument");
+        if (n_steps <= 0 || checkpoint_every <= 0) throw std::invalid_argument("n_steps and checkpoint_every must be positive");
+        if (!(s->has_inertia && s->dt > 0.0)) throw std::invalid_argument("a rollout needs masses and dt > 0");
+        if (info) std::memset(info, 0, sizeof(*info));
+        const auto t0 = std::chrono::steady_clock::now();
+        s->ckpt_x0.clear();
+        s->ckpt_v0.clear();
+        for (int n = 0; n < n_steps; ++n) {
+            if (n % checkpoint_every == 0) {
+                s->ckpt_x0.push_back(s->x0);
+                s->ckpt_v0.push_back(s->v0);
+            }
+            rollout_step(s, n, info);
+        }
+        s->rollout_steps = n_steps;
+        s->checkpoint_every = checkpoint_every;
+        if (info) {
+            info->steps = n_steps;
+            info->checkpoints = (int32_t)s->ckpt_x0.size();
+            info->seconds_forward = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
+        return SYMXG_OK;
+    });
+}
+
+int symxg_rollout_backward(symxg_solver* s, const double* dLdx_final, const double* dLdv_final, double rel_tol,
+                           int32_t max_iterations, double* dLdx_init, double* dLdv_init, double* dLdmu,
+                           double* dLdlambda, symxg_rollout_info* info)
+{
+    return guarded([&] {
+        if (!s || !dLdx_final) throw std::invalid_argument("null argument");
+        if (s->rollout_steps <= 0) throw std::invalid_argument("no forward rollout to differentiate");
+        if (!(rel_tol > 0.0) || max_iterations <= 0) throw std::invalid_argument("rel_tol and max_iterations must be positive");
+        const auto t0 = std::chrono::steady_clock::now();
+        const size_t nv = s->x.size(), nd = 3 * nv, ne = s->mu.size();
+        const double dt = s->dt;
+        std::vector<double> ax(dLdx_final, dLdx_final + nd), av(nd, 0.0), a(nd), lam(nd), gx(nd), gv(nd);
+        if (dLdv_final) av.assign(dLdv_final, dLdv_final + nd);
+        std::vector<double> dmu(ne, 0.0), dlam(ne, 0.0), tmu(ne), tlam(ne);
+        const int N = s->rollout_steps, K = s->checkpoint_every;
+        const std::vector<Vec3> x_final = s->x, x0_final = s->x0, v0_final = s->v0;
+        for (int seg = (int)s->ckpt_x0.size() - 1; seg >= 0; --seg) {
+            const int start = seg * K, end = std::min(start + K, N);
+            // recompute the segment's states from its checkpoint
+            std::vector<std::vector<Vec3>> xs{s->ckpt_x0[seg]}, vs{s->ckpt_v0[seg]};
+            s->x0 = s->ckpt_x0[seg];
+            s->v0 = s->ckpt_v0[seg];
+            for (int n = start; n < end; ++n) {
+                rollout_step(s, n, info);
+                xs.push_back(s->x0);
+                vs.push_back(s->v0);
+                if (info) info->recomputed_steps += 1;
+            }
+            for (int n = end - 1; n >= start; --n) {
+                const int k = n - start;
+                s->x = xs[k + 1];
+                s->x0 = xs[k];
+                s->v0 = vs[k];
+                s->newton->upload();
+                for (size_t i = 0; i < nd; ++i) a[i] = ax[i] + av[i] / dt;
+                const symx::AdjointInfo ai = s->newton->adjoint_solve(a.data(), lam.data(), rel_tol, max_iterations);
+                if (info) info->adjoint_iterations += ai.iterations;
+                if (!ai.converged)
+                    throw std::runtime_error("adjoint PCG of rollout step " + std::to_string(n) + " did not converge");
+                s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->x0), lam.data(), gx.data(), (int64_t)nd);
+                s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->v0), lam.data(), gv.data(), (int64_t)nd);
+                if (dLdmu) {
+                    s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->mu), lam.data(), tmu.data(), (int64_t)ne);
+                    for (size_t e = 0; e < ne; ++e) dmu[e] += tmu[e];
+                }
+                if (dLdlambda) {
+                    s->newton->parameter_gradient(reinterpret_cast<std::uintptr_t>(&s->lam), lam.data(), tlam.data(), (int64_t)ne);
+                    for (size_t e = 0; e < ne; ++e) dlam[e] += tlam[e];
+                }
+                for (size_t i = 0; i < nd; ++i) {
+                    ax[i] = gx[i] - av[i] / dt;
+                    av[i] = gv[i];
+                }
+            }
+        }
+        // leave the handle at the end of the rollout
+        s->x = x_final;
+        s->x0 = x0_final;
+        s->v0 = v0_final;
+        if (dLdx_init) std::memcpy(dLdx_init, ax.data(), sizeof(double) * nd);
+        if (dLdv_init) std::memcpy(dLdv_init, av.data(), sizeof(double) * nd);
+        if (dLdmu) std::memcpy(dLdmu, dmu.data(), sizeof(double) * ne);
+        if (dLdlambda) std::memcpy(dLdlambda, dlam.data(), sizeof(double) * ne);
+        if (info) info->seconds_backward = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return SYMXG_OK;
     });
 }

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <sstream>
 #include <stdexcept>
+#include <map>
 #include <unordered_map>
 
 #include <cuda_runtime.h>
@@ -411,6 +412,11 @@ struct SolverImpl {
         ps.n_fallback = proj_n_fallback.p;
         return ps;
     }
+    // adjoint: mixed-derivative modules per (potential, data map), lambda on the device
+    std::string cache_dir;
+    std::map<std::pair<int, int>, std::shared_ptr<CudaModule>> mixed_modules;
+    DevBuf<double> lambda, mixed_out;
+    DevBuf<const double*> lmap_ptrs;
     double* h_scalars = nullptr;
     PcgState* h_state = nullptr;
     Precision allocated_precision = Precision::FP64;
@@ -493,6 +499,102 @@ template <> double* SolverImpl::Dinv<double>() { return Dinv64.p; }
 template <> DevBuf<float>* SolverImpl::vecs<float>() { return v32; }
 template <> DevBuf<double>* SolverImpl::vecs<double>() { return v64; }
 
+// Source of the mixed-derivative kernel of one potential for the data map `mk` (the
+// parameter): per element, out[j] = sum_i lambda_i * d g_i / d p_j for the map's symbols p_j,
+// g the element gradient with respect to its DoF symbols (summed over the quadrature points
+// of an FEM rule).  lambda_i are new symbols gathered from a DoF-shaped vector through the
+// same maps as the DoFs.  Everything is evaluated in FP64 from the gathered data (no
+// hoisting: the kernel runs once per adjoint).
+std::string build_mixed_source(const CompiledPotential& cp, const GlobalPotential& GP, int mk)
+{
+    const Potential& pot = *cp.pot;
+    MappedWorkspace<double>& mws = *pot.mws;
+    Expressions& g = mws.ws.get_expression_graph();
+    std::vector<Scalar> wrt;
+    std::vector<int> dof_maps;
+    for (size_t k = 0; k < mws.maps.size(); ++k) {
+        bool is_dof = false;
+        for (const auto& d : GP.dofs)
+            if (d.id == mws.maps[k].id) is_dof = true;
+        if (!is_dof) continue;
+        dof_maps.push_back((int)k);
+        for (int j = 0; j < 3; ++j) wrt.push_back(Scalar(g.symbol_node(mws.maps[k].first_symbol + j), &g));
+    }
+    const DataMap& pm = mws.maps[mk];
+    DiffCache cache;
+    Vector grad = gradient(pot.expression, wrt, cache);
+    std::vector<Scalar> lam;
+    for (size_t i = 0; i < wrt.size(); ++i) lam.push_back(Scalar(g.new_symbol(), &g));  // new_symbol: node id
+    std::vector<int32_t> outs;
+    for (int j = 0; j < pm.stride; ++j) {
+        const Scalar pj(g.symbol_node(pm.first_symbol + j), &g);
+        Scalar acc = pj.get_zero();
+        for (size_t i = 0; i < wrt.size(); ++i) acc += lam[i] * diff(grad[(int32_t)i], pj, cache);
+        outs.push_back(acc.expr_id);
+    }
+    const Summation& sum = mws.summation;
+    const int NS = g.n_symbols();
+    const int NQ = std::max(1, sum.n_iterations);
+    const bool acc = sum.n_iterations > 1;
+    std::ostringstream s;
+    s << "// generated mixed-derivative kernel of potential '" << cp.name << "' for data map " << mk << "\n";
+    s << codegen_prelude();
+    s << emit_device_function(g, outs, "symxg_mixed_f", "double", acc, nullptr, nullptr);
+    if (pot.has_condition) s << emit_device_function(g, {pot.condition.expr_id}, "symxg_mixed_cond", "double", false, nullptr, nullptr);
+    if (sum.n_iterations > 0) {
+        s << "static __device__ const double symxg_sum_data[" << sum.data.size() << "] = {";
+        for (size_t i = 0; i < sum.data.size(); ++i) s << (i ? ", " : "") << double_literal(sum.data[i]);
+        s << "};\n";
+    }
+    s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_mixed(long long n, const int* __restrict__ conn, "
+         "const double* const* __restrict__ maps, const double* const* __restrict__ lmaps, double* __restrict__ out)\n{\n";
+    s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
+    s << "    const int* __restrict__ ce = conn + e * " << cp.conn_stride << "LL;\n    (void)ce;\n";
+    s << "    double in[" << NS << "];\n";
+    for (size_t k = 0; k < mws.maps.size(); ++k) {
+        const DataMap& m = mws.maps[k];
+        s << "    { const double* __restrict__ m = maps[" << k << "]";
+        if (m.conn_column >= 0) s << " + (long long)ce[" << m.conn_column << "] * " << m.stride << "LL";
+        s << ";";
+        for (int j = 0; j < m.stride; ++j) s << " in[" << (m.first_symbol + j) << "] = m[" << j << "];";
+        s << " }\n";
+    }
+    int li = 0;
+    for (int k : dof_maps) {
+        const DataMap& m = mws.maps[k];
+        s << "    { const double* __restrict__ m = lmaps[" << k << "] + (long long)ce[" << m.conn_column << "] * 3LL;";
+        for (int j = 0; j < 3; ++j) s << " in[" << lam[li++].get_symbol_idx() << "] = m[" << j << "];";
+        s << " }\n";
+    }
+    auto set_sum = [&](const std::string& q) {
+        std::ostringstream t;
+        for (int j = 0; j < sum.stride && sum.n_iterations > 0; ++j)
+            t << "        in[" << (sum.first_symbol + j) << "] = symxg_sum_data[" << q << " * " << sum.stride << " + " << j
+              << "];\n";
+        return t.str();
+    };
+    s << "    double r[" << pm.stride << "];\n    for (int j = 0; j < " << pm.stride << "; ++j) r[j] = 0.0;\n";
+    if (pot.has_condition) {
+        s << "    {\n" << set_sum("0") << "        double cv[1]; symxg_mixed_cond(in, nullptr, cv);\n"
+          << "        if (!(cv[0] > 0.0)) { for (int j = 0; j < " << pm.stride << "; ++j) out[e * " << pm.stride
+          << "LL + j] = 0.0; return; }\n    }\n";
+    }
+    s << "    for (int q = 0; q < " << NQ << "; ++q) {\n" << set_sum("q") << "        symxg_mixed_f(in, nullptr, r);\n    }\n";
+    s << "    for (int j = 0; j < " << pm.stride << "; ++j) out[e * " << pm.stride << "LL + j] = r[j];\n}\n";
+    return s.str();
+}
+
+std::vector<std::string> generate_mixed_kernel_sources(const GlobalPotential& GP, std::uintptr_t param)
+{
+    std::vector<std::string> out;
+    for (const Potential& pot : GP.potentials) {
+        CompiledPotential cp = prepare_potential(pot, GP);
+        for (size_t k = 0; k < pot.mws->maps.size(); ++k)
+            if (pot.mws->maps[k].id == param) out.push_back(build_mixed_source(cp, GP, (int)k));
+    }
+    return out;
+}
+
 std::vector<std::string> generate_element_kernel_sources(const GlobalPotential& GP)
 {
     std::vector<std::string> out;
@@ -529,6 +631,7 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     I.n_blocks = I.n_dofs / 3;
     const std::string cache_dir =
         context->compilation_directory.empty() ? symxg::default_cache_dir() : context->compilation_directory;
+    I.cache_dir = cache_dir;
 
     // ---- per potential: DoF symbols, differentiation, code generation, compilation
     for (const Potential& pot : GP.potentials) {
@@ -1049,6 +1152,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             }
         }
         st.cg_iterations += ps.iteration;
+        st.cg_iterations_per_newton.push_back(ps.iteration);
         if (verbosity > 0) std::printf("#CG: %4d | ", ps.iteration);
         if (!ps.converged) {
             result = SolverReturn::LinearSystemSolveFailure;
@@ -1127,6 +1231,142 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------- adjoint
+namespace {
+template <typename T>
+AdjointInfo adjoint_solve_t(SolverImpl& I, const NewtonSettings& S, const double* rhs, double* lambda, double rel_tol,
+                            int max_iterations, bool project)
+{
+    cudaStream_t s = I.stream;
+    assemble_t<T>(I, project, S, std::is_same<T, float>::value ? 1 : 0);
+    symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.vstride, I.Dinv<T>(), s);
+    // the PCG initialisation takes -b
+    std::vector<double> neg(rhs, rhs + I.n_dofs);
+    for (double& v : neg) v = -v;
+    ck(cudaMemcpyAsync(I.grad.p, neg.data(), sizeof(double) * I.n_dofs, cudaMemcpyHostToDevice, s), "upload rhs");
+    DevBuf<T>* V = I.vecs<T>();
+    PcgBuffers<T> B;
+    B.n_blocks = I.n_blocks;
+    B.row_ptr = I.row_ptr.p;
+    B.cols = I.cols.p;
+    B.vals = I.vals<T>();
+    B.vals_stride = I.vstride;
+    B.Dinv = I.Dinv<T>();
+    B.x = V[0].p;
+    B.r = V[1].p;
+    B.z = V[2].p;
+    B.p = V[3].p;
+    B.q = V[4].p;
+    B.p2 = V[5].p;
+    B.partials = I.partials.p;
+    B.tickets = I.tickets.p;
+    B.state = I.pcg_state.p;
+    if constexpr (std::is_same<T, float>::value) B.staged = I.staged;
+    PcgState init{};
+    init.abs_tol = 0.0;
+    init.rel_tol = rel_tol;
+    init.max_iterations = max_iterations;
+    ck(cudaMemcpyAsync(I.pcg_state.p, &init, sizeof(PcgState), cudaMemcpyHostToDevice, s), "pcg state");
+    symxg::launch_pcg_init<T>(B, I.grad.p, s);
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value) {
+        if (B.staged.persistent) {
+            symxg::launch_pcg_solve_persistent(B, s);
+            done = true;
+        }
+    }
+    for (int launched = 0, chunk = 8; !done;) {
+        for (int k = 0; k < chunk; ++k) symxg::launch_pcg_iteration<T>(B, launched + k, s);
+        launched += chunk;
+        ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
+        ck(cudaStreamSynchronize(s), "synchronize");
+        if (I.h_state->done || launched > max_iterations + 1) break;
+        chunk = std::min(chunk * 2, 64);
+    }
+    ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
+    std::vector<T> x4(4 * (size_t)I.n_blocks);
+    ck(cudaMemcpyAsync(x4.data(), V[0].p, sizeof(T) * x4.size(), cudaMemcpyDeviceToHost, s), "download solution");
+    ck(cudaStreamSynchronize(s), "synchronize");
+    const PcgState ps = *I.h_state;
+    if (ps.wait_failed) throw std::runtime_error("symx_gb300: a bounded wait in the PCG kernels gave up");
+    for (int64_t r = 0; r < I.n_blocks; ++r)
+        for (int d = 0; d < 3; ++d) lambda[3 * r + d] = (double)x4[4 * r + d];
+    AdjointInfo info;
+    info.iterations = ps.iteration;
+    info.converged = ps.converged != 0;
+    info.error = ps.error;
+    return info;
+}
+}  // namespace
+
+AdjointInfo NewtonsMethod::adjoint_solve(const double* rhs, double* lambda, double rel_tol, int max_iterations,
+                                         bool project)
+{
+    if (settings.precision == Precision::Mixed)
+        return adjoint_solve_t<float>(*impl, settings, rhs, lambda, rel_tol, max_iterations, project);
+    return adjoint_solve_t<double>(*impl, settings, rhs, lambda, rel_tol, max_iterations, project);
+}
+
+void NewtonsMethod::parameter_gradient(std::uintptr_t param, const double* lambda, double* out, int64_t n_out)
+{
+    SolverImpl& I = *impl;
+    GlobalPotential& GP = *global_potential;
+    cudaStream_t s = I.stream;
+    std::fill(out, out + n_out, 0.0);
+    I.lambda.alloc((size_t)I.n_dofs);
+    ck(cudaMemcpyAsync(I.lambda.p, lambda, sizeof(double) * I.n_dofs, cudaMemcpyHostToDevice, s), "upload lambda");
+    bool bound = false;
+    for (size_t p = 0; p < I.pots.size(); ++p) {
+        CompiledPotential& cp = I.pots[p];
+        const auto& maps = cp.pot->mws->maps;
+        for (size_t k = 0; k < maps.size(); ++k) {
+            const DataMap& m = maps[k];
+            if (m.id != param) continue;
+            bound = true;
+            for (const auto& d : GP.dofs)
+                if (d.id == param) throw std::invalid_argument("symx: parameter_gradient of a DoF container");
+            if (cp.n_elements == 0) continue;
+            auto key = std::make_pair((int)p, (int)k);
+            auto it = I.mixed_modules.find(key);
+            if (it == I.mixed_modules.end())
+                it = I.mixed_modules.emplace(key, CudaModule::build(build_mixed_source(cp, GP, (int)k), I.cache_dir, {}, nullptr))
+                         .first;
+            // lambda through the DoF maps, nothing through the others
+            std::vector<const double*> lp(maps.size(), nullptr);
+            for (size_t j = 0; j < maps.size(); ++j)
+                for (size_t set = 0; set < GP.dofs.size(); ++set)
+                    if (GP.dofs[set].id == maps[j].id) lp[j] = I.lambda.p + I.dof_offsets[set];
+            I.lmap_ptrs.alloc(std::max<size_t>(maps.size(), I.lmap_ptrs.n));
+            ck(cudaMemcpyAsync(I.lmap_ptrs.p, lp.data(), sizeof(double*) * lp.size(), cudaMemcpyHostToDevice, s),
+               "upload lambda maps");
+            const size_t n_vals = (size_t)cp.n_elements * m.stride;
+            if (I.mixed_out.n < n_vals) I.mixed_out.alloc(n_vals);
+            long long n = cp.n_elements;
+            const int32_t* conn = cp.conn.p;
+            const double* const* mp = cp.map_ptrs.p;
+            const double* const* lmp = I.lmap_ptrs.p;
+            double* o = I.mixed_out.p;
+            void* args[] = {&n, &conn, &mp, &lmp, &o};
+            it->second->launch("symxg_mixed", dim3((unsigned)((n + 127) / 128)), dim3(128), 0, s, args);
+            std::vector<double> vals(n_vals);
+            ck(cudaMemcpyAsync(vals.data(), I.mixed_out.p, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, s),
+               "download mixed derivatives");
+            ck(cudaStreamSynchronize(s), "synchronize");
+            // element order, one fixed summation order per entry
+            const int32_t* hconn = cp.pot->mws->conn.data();
+            for (int64_t e = 0; e < cp.n_elements; ++e) {
+                const int64_t item = m.conn_column >= 0 ? hconn[e * cp.conn_stride + m.conn_column] : 0;
+                for (int j = 0; j < m.stride; ++j) {
+                    const int64_t idx = item * m.stride + j;
+                    if (idx < 0 || idx >= n_out) throw std::invalid_argument("symx: parameter_gradient output too small");
+                    out[idx] -= vals[(size_t)e * m.stride + j];
+                }
+            }
+        }
+    }
+    if (!bound) throw std::invalid_argument("symx: the parameter container is not bound in any potential");
+}
 
 SolverReturn NewtonsMethod::solve_device()
 {

@@ -94,9 +94,17 @@ struct SolveStats {
     std::map<std::string, double> timers;
     // With time_kernels: per kernel name, {launches that did work, total seconds}.
     std::map<std::string, std::pair<int64_t, double>> kernels;
+    // PCG iterations of each Newton iteration's linear solve, in order.
+    std::vector<int> cg_iterations_per_newton;
 };
 
 struct SolverImpl;
+
+struct AdjointInfo {
+    int iterations = 0;
+    bool converged = false;
+    double error = 0.0;  // sqrt(r.r / b.b) at exit
+};
 
 class NewtonsMethod {
 public:
@@ -138,6 +146,29 @@ public:
     std::array<int64_t, 3> op_counts(int p) const;
     std::string generated_source(int p) const;
 
+    // ---- adjoint (an addition of this library; the reference has no adjoint)
+    // Solve H lambda = rhs with block-Jacobi PCG, H the Hessian of the total energy at the
+    // device DoFs (true Hessian, or projected with `project`), assembled in the current
+    // precision.  rhs and lambda are host arrays of n_dofs doubles.  Stops at
+    // sqrt(r.r / b.b) < rel_tol (or after max_iterations).
+    AdjointInfo adjoint_solve(const double* rhs, double* lambda, double rel_tol, int max_iterations,
+                              bool project = false);
+    // out = -sum over elements of lambda_e . d g_e / d p for the data container `param`
+    // (identified by its address, bound in the potentials with make_scalar / make_vector(s)):
+    // the contribution of an implicit state x(p) with g(x(p), p) = 0 to dL/dp when
+    // H lambda = dL/dx.  The mixed derivatives d g / d p are differentiated symbolically from
+    // the potentials and compiled on first use.  Evaluated in FP64 at the device DoFs and
+    // uploaded data; `out` (host) holds n_out doubles, the container's size.
+    void parameter_gradient(std::uintptr_t param, const double* lambda, double* out, int64_t n_out);
+    template <typename C>
+    std::vector<double> parameter_gradient(const C& param, const std::vector<double>& lambda)
+    {
+        const int64_t n = (int64_t)(param.size() * (sizeof(typename C::value_type) / sizeof(double)));
+        std::vector<double> out((size_t)n);
+        parameter_gradient(reinterpret_cast<std::uintptr_t>(&param), lambda.data(), out.data(), n);
+        return out;
+    }
+
 private:
     spGlobalPotential global_potential;
     spContext context;
@@ -151,5 +182,8 @@ std::string to_string(SolverReturn r);
 // CUDA source of the element kernels NewtonsMethod would generate for each potential
 // (differentiation + code generation only; no GPU or compiler involved).
 std::vector<std::string> generate_element_kernel_sources(const GlobalPotential& gp);
+// CUDA source of the mixed-derivative kernels parameter_gradient would generate for the data
+// container with address `param`, one per (potential, binding).
+std::vector<std::string> generate_mixed_kernel_sources(const GlobalPotential& gp, std::uintptr_t param);
 
 }  // namespace symx

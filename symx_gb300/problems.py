@@ -190,3 +190,41 @@ def step_problem(name_or_cfg, *, youngs=1e5, poisson=0.3, density=1000.0, dt=1.0
         bc_idx=bc_idx, bc_target=X[bc_idx].copy(), dt=float(dt),
         gravity=np.asarray(gravity, dtype=np.float64), k_bc=float(k_bc),
     )
+
+
+def adjoint_problem(name_or_cfg="tet4_32", *, youngs=1e5, poisson=0.3, log_std=0.3, seed=3, target_seed=4,
+                    **kw):
+    """Quasistatic adjoint case: a clamped Neo-Hookean box at equilibrium under gravity
+    (dt = 0 selects the quasistatic form: gravity as the potential -m g.x, no inertia), with one
+    parameter per element p_e = ln E_e ~ N(ln youngs, log_std^2) drawn from `seed`.  The target
+    positions x* are the equilibrium of a second field drawn from `target_seed` (the caller
+    solves for them).  Adds logE, mu_target, lam_target to the step_problem dict."""
+    p = step_problem(name_or_cfg, youngs=youngs, poisson=poisson, **kw)
+    ne = p["conn"].shape[0]
+    logE = normal(seed * 1000 + 5, ne, mean=np.log(youngs), std=log_std)
+    logE_t = normal(target_seed * 1000 + 5, ne, mean=np.log(youngs), std=log_std)
+    p["mu"], p["lam"] = lame(np.exp(logE), poisson)
+    p["mu_target"], p["lam_target"] = lame(np.exp(logE_t), poisson)
+    p["logE"] = logE
+    p["dt"] = 0.0
+    p["x0"] = p["X"].copy()
+    p["x_init"] = p["X"].copy()
+    p["v0"] = np.zeros_like(p["X"])
+    return p
+
+
+def rollout_problem(name_or_cfg="tet4_40", *, youngs=1e5, poisson=0.3, log_std=0.3, seed=4, **kw):
+    """Differentiable rollout case: implicit-Euler steps of a clamped Neo-Hookean box with
+    v0 ~ N(0, 0.5^2) per component and per-element ln E_e ~ N(ln youngs, log_std^2) (both from
+    `seed`), and a seeded target point for the final centroid (the box centroid displaced by
+    N(0, (0.1 L)^2) per axis, L the largest box side)."""
+    p = step_problem(name_or_cfg, youngs=youngs, poisson=poisson, **kw)
+    ne = p["conn"].shape[0]
+    logE = normal(seed * 1000 + 5, ne, mean=np.log(youngs), std=log_std)
+    p["mu"], p["lam"] = lame(np.exp(logE), poisson)
+    p["logE"] = logE
+    p["x0"] = p["X"].copy()
+    p["x_init"] = p["X"].copy()
+    L = float(np.max(p["X"].max(axis=0) - p["X"].min(axis=0)))
+    p["target"] = p["X"].mean(axis=0) + normal(seed * 1000 + 7, 3, std=0.1 * L)
+    return p

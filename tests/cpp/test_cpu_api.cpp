@@ -142,6 +142,17 @@ static int nvrtc(const char* cache_dir)
         std::printf("potential %zu: %zu source bytes -> %zu cubin bytes\n", i, src[i].size(), cubin.size());
         if (cubin.size() < 1000) { std::printf("FAIL cubin too small\n"); return 1; }
     }
+    // mixed-derivative (adjoint) kernels for every bound non-DoF input
+    const std::vector<std::uintptr_t> params = {reinterpret_cast<std::uintptr_t>(&mu), reinterpret_cast<std::uintptr_t>(&lam),
+                                                reinterpret_cast<std::uintptr_t>(&x0), reinterpret_cast<std::uintptr_t>(&v0),
+                                                reinterpret_cast<std::uintptr_t>(&mass)};
+    for (std::uintptr_t prm : params) {
+        const std::vector<std::string> ms = generate_mixed_kernel_sources(*G, prm);
+        if (ms.size() != 1) { std::printf("FAIL expected one mixed kernel per parameter, got %zu\n", ms.size()); return 1; }
+        const std::string cubin = symxg::compile_cubin(ms[0], {});
+        std::printf("mixed kernel: %zu source bytes -> %zu cubin bytes\n", ms[0].size(), cubin.size());
+        if (cubin.size() < 1000) { std::printf("FAIL cubin too small\n"); return 1; }
+    }
     std::printf("nvrtc PASS\n");
     return 0;
 }
