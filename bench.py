@@ -104,6 +104,14 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def workload_name(name, p):
+    cfg = __import__("symx_gb300.problems", fromlist=["CONFIGS"]).CONFIGS.get(name, {})
+    kind = "Tet4" if p["conn"].shape[1] == 4 else "Hex8 (2x2x2 Gauss points)"
+    cells = "x".join(str(c) for c in cfg.get("cells", ())) or "custom"
+    return (f"Neo-Hookean {kind} implicit-Euler step, {cells} cells ({p['X'].shape[0]:,} vertices, "
+            f"{p['conn'].shape[0]:,} elements)")
+
+
 def spmv_roofline(solver, torch, sg, n_rep=30):
     """Time the BCSR SpMV kernel (the PCG's dominant HBM-bound kernel) on the assembled
     mixed-precision Hessian of the workload, with CUDA events on its stream."""
@@ -254,8 +262,8 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 Hessian/PCG, f64 energy/gradient/line search",
-        "data": "synthetic (seeded 64^3 Tet4 cube)",
-        "config": {"workload": "Neo-Hookean Tet4 implicit-Euler step, 64^3 cells (274,625 vertices, 1,572,864 tets)",
+        "data": f"synthetic (seeded {args.config})",
+        "config": {"workload": workload_name(args.config, p),
                    "name": args.config, "precision": "mixed", "newton_iterations": newton_its,
                    "cg_iterations": st["cg_iterations"], "final_residual": st["final_residual"],
                    "l2": "working set > L2 (element Hessians 0.9 GB, BCSR 0.16 GB)",
@@ -367,14 +375,164 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT + " per Newton step",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(per_solve), 3),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded 64^3 Tet4 cube)",
-        "config": {"workload": "Neo-Hookean Tet4 implicit-Euler step, 64^3 cells (274,625 vertices, 1,572,864 tets)",
+        "data": f"synthetic (seeded {args.config})",
+        "config": {"workload": workload_name(args.config, p),
                    "name": args.config},
         "cpu_baseline": {"value": round(v, 3), "unit": UNIT + " per Newton step", "cores": threads, "kind": "port",
                          "sample": ("each step: the complete solve" if n <= 0 else f"each step: the first {n} Newton "
                                     f"iterations of the solve") + f" from the same state ({its} Newton iterations)"},
         "e2e": {"value": round(v, 3), "unit": UNIT + " per Newton step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def measure_adjoint(args):
+    """Quasistatic adjoint (config 3 sizes by default: tet4_32): forward solve and adjoint in
+    FP64 and mixed precision, dL/d(ln E) against the oracle's FP64 adjoint at the FP64 state and
+    against central differences (h = 1e-6) of GPU FP64 solves on 16 seeded elements."""
+    import torch
+
+    import symx_gb300 as sg
+    from oracle import oracle as O
+    from symx_gb300 import problems
+
+    cfg = args.config if args.config != "tet4_64" else "tet4_32"
+    p = problems.adjoint_problem(cfg)
+    # The configuration's stopping rule is |grad E|_inf < 1e-6; near that point the Armijo test
+    # stalls on the rounding of the energy, so states used for differences are polished with
+    # full Newton steps (no line search) to 1e-8 (the floor is ~3e-9: the 1e8 boundary penalty
+    # times the rounding of x).
+    settings = dict(residual_tolerance_abs=1e-6, cg_rel_tolerance=1e-3, max_iterations=100)
+    polish = dict(residual_tolerance_abs=1e-8, cg_rel_tolerance=1e-10, max_iterations=30,
+                  enable_armijo_backtracking=0)
+
+    def solve(q, precision="fp64", x_init=None, polished=True):
+        s = sg.ElasticSolver(q)
+        s.set_settings(precision=precision, **settings)
+        s.set_state(q["x_init"] if x_init is None else x_init, q["x0"], q["v0"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = s.solve() if x_init is None else {"solver_return": 0, "newton_iterations": 0}
+        t = time.perf_counter() - t0
+        if st["solver_return"] != 0:
+            raise RuntimeError(f"solve failed: {st}")
+        if polished:
+            s.set_settings(precision=precision, **polish)
+            s.set_state(s.get_positions() if x_init is None else x_init, q["x0"], q["v0"])
+            st2 = s.solve()
+            if st2["solver_return"] != 0:
+                raise RuntimeError(f"polish failed: {st2}")
+        return s, st, t
+
+    x_star = solve(dict(p, mu=p["mu_target"], lam=p["lam_target"]))[0].get_positions()
+    out = {"measure": "adjoint", "config": cfg, "n_vertices": int(p["X"].shape[0]),
+           "n_elements": int(p["conn"].shape[0]), "loss": "0.5 |x(p) - x*|^2, p_e = ln E_e"}
+    grads = {}
+    for precision in ("fp64", "mixed"):
+        solve(p, precision, polished=False)  # warm: compiled kernels
+        s, st, t_fwd = solve(p, precision, polished=False)  # timed: the configuration's own tolerance
+        if precision == "fp64":
+            s, _, _ = solve(p, precision)  # polished state for the gradient checks
+        x = s.get_positions()
+        rel_tol = 1e-12 if precision == "fp64" else 1e-10  # mixed: FP32 PCG inside FP64 defect correction
+        s.adjoint((x - x_star).ravel(), rel_tol=rel_tol)  # warm-up (compiles the mixed-derivative kernels)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a = s.adjoint((x - x_star).ravel(), rel_tol=rel_tol)
+        t_adj = time.perf_counter() - t0
+        grads[precision] = p["mu"] * a["dLdmu"] + p["lam"] * a["dLdlam"]
+        out[precision] = {"forward_s": round(t_fwd, 4), "newton_iterations": st["newton_iterations"],
+                          "adjoint_s": round(t_adj, 4), "adjoint_pcg_iterations": a["info"]["iterations"],
+                          "adjoint_error": a["info"]["error"]}
+        if precision == "fp64":
+            x64 = x
+    P = O.Problem(p, 0)
+    P.set_x(x64)
+    ref = O.adjoint(P, p, (x64 - x_star).ravel(), solver="pcg")
+    g_ref = p["mu"] * ref["dLdmu"] + p["lam"] * ref["dLdlam"]
+    scale = np.max(np.abs(g_ref))
+    for precision in ("fp64", "mixed"):
+        out[precision]["rel_err_vs_oracle_fp64"] = float(np.max(np.abs(grads[precision] - g_ref)) / scale)
+    # central differences of FP64 GPU solves on 16 seeded elements
+    h = 1e-6
+    elems = problems.splitmix64(31, 16) % p["conn"].shape[0]
+    fd = []
+    for e in elems:
+        vals = []
+        for sgn in (1.0, -1.0):
+            logE = p["logE"].copy()
+            logE[e] += sgn * h
+            mu, lam = problems.lame(np.exp(logE), 0.3)
+            xx = solve(dict(p, mu=mu, lam=lam), x_init=x64)[0].get_positions()
+            vals.append(0.5 * float(np.sum((xx - x_star) ** 2)))
+        fd.append((vals[0] - vals[1]) / (2 * h))
+    fd = np.array(fd)
+    fd_scale = np.max(np.abs(fd))
+    for precision in ("fp64", "mixed"):
+        out[precision]["max_rel_err_vs_central_differences_16"] = float(
+            np.max(np.abs(grads[precision][elems] - fd)) / fd_scale)
+    out["central_differences"] = {"h": h, "elements": [int(e) for e in elems], "max_abs_fd": float(fd_scale)}
+    return out
+
+
+def measure_rollout(args):
+    """Differentiable rollout (config 4 sizes by default: tet4_40, 50 steps, checkpoint every
+    10): forward and reverse-time adjoint in FP64 and mixed precision, device memory held by
+    the solver, and the gradients along seeded directions of v0 and ln E against central
+    differences of FP64 GPU rollouts."""
+    import torch
+
+    import symx_gb300 as sg
+    from symx_gb300 import problems
+
+    cfg = args.config if args.config != "tet4_64" else "tet4_40"
+    n_steps, every = args.rollout_steps, 10
+    p = problems.rollout_problem(cfg)
+    settings = dict(residual_tolerance_abs=1e-8, cg_rel_tolerance=1e-3, max_iterations=100)
+
+    def forward(q, precision="fp64"):
+        s = sg.ElasticSolver(q)
+        s.set_settings(precision=precision, **settings)
+        s.set_state(q["x_init"], q["x0"], q["v0"])
+        info = s.rollout_forward(n_steps, every)
+        xN = s.get_positions()
+        d = xN.mean(axis=0) - q["target"]
+        return s, info, xN, 0.5 * float(d @ d)
+
+    out = {"measure": "rollout", "config": cfg, "n_vertices": int(p["X"].shape[0]),
+           "n_elements": int(p["conn"].shape[0]), "steps": n_steps, "checkpoint_every": every,
+           "loss": "0.5 |centroid(x_N) - target|^2; gradients wrt v0 and ln E"}
+    grads = {}
+    for precision in ("fp64", "mixed"):
+        free0, total = torch.cuda.mem_get_info()
+        s, info_f, xN, L = forward(p, precision)
+        d = xN.mean(axis=0) - p["target"]
+        dLdx = np.tile(d / xN.shape[0], (xN.shape[0], 1))
+        g = s.rollout_backward(dLdx, rel_tol=1e-10)  # mixed: FP32 PCG inside FP64 defect correction
+        free1, _ = torch.cuda.mem_get_info()
+        grads[precision] = (g["dLdv0"], p["mu"] * g["dLdmu"] + p["lam"] * g["dLdlam"])
+        out[precision] = {"forward_s": round(info_f["seconds_forward"], 3),
+                          "backward_s": round(g["info"]["seconds_backward"], 3),
+                          "newton_iterations_forward": info_f["newton_iterations"],
+                          "recomputed_steps": g["info"]["recomputed_steps"],
+                          "armijo_polished_steps": info_f["armijo_polished_steps"] + g["info"]["armijo_polished_steps"],
+                          "adjoint_pcg_iterations": g["info"]["adjoint_iterations"],
+                          "device_memory_held_mb": round((free0 - free1) / 2**20, 1), "loss": L}
+        del s
+    h = 1e-4
+    dv = np.tile([1.0, 0.5, -0.3], (p["v0"].shape[0], 1)) + 0.1 * problems.normal(41, p["v0"].size).reshape(-1, 3)
+    dp = 1.0 + 0.3 * problems.normal(42, p["logE"].size)
+    fd_v = (forward(dict(p, v0=p["v0"] + h * dv))[3] - forward(dict(p, v0=p["v0"] - h * dv))[3]) / (2 * h)
+    fd_p = []
+    for sgn in (1.0, -1.0):
+        mu, lam = problems.lame(np.exp(p["logE"] + sgn * h * dp), 0.3)
+        fd_p.append(forward(dict(p, mu=mu, lam=lam))[3])
+    fd_p = (fd_p[0] - fd_p[1]) / (2 * h)
+    for precision in ("fp64", "mixed"):
+        gv, gp = grads[precision]
+        out[precision]["rel_err_dv0_direction"] = float(abs(gv @ dv.ravel() - fd_v) / abs(fd_v))
+        out[precision]["rel_err_dlnE_direction"] = float(abs(gp @ dp - fd_p) / abs(fd_p))
+    out["central_differences"] = {"h": h, "d_v0": fd_v, "d_lnE": fd_p}
+    return out
 
 
 def main():
@@ -388,7 +546,14 @@ def main():
     ap.add_argument("--cpu-newton-iterations", type=int, default=0, help="0: the complete solve")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--profile-solve", choices=["mixed", "fp64"], default=None)
+    ap.add_argument("--measure", choices=["adjoint", "rollout"], default=None,
+                    help="instead of the bench line: the adjoint (quasistatic) or rollout measurement")
+    ap.add_argument("--rollout-steps", type=int, default=50)
     args = ap.parse_args()
+    if args.measure:
+        out = measure_adjoint(args) if args.measure == "adjoint" else measure_rollout(args)
+        print(json.dumps(out))
+        return
     rank, world, _ = dist_env()
     if world > 1 and args.impl == "ours":
         import torch

@@ -248,6 +248,8 @@ typedef struct symxg_rollout_info {
     int32_t cg_iterations;
     int32_t recomputed_steps;
     int32_t adjoint_iterations;  /* PCG iterations of all adjoint solves */
+    int32_t armijo_polished_steps; /* steps finished with full Newton steps after an Armijo stall */
+    int32_t pad;
     double seconds_forward;
     double seconds_backward;
 } symxg_rollout_info;

@@ -98,6 +98,7 @@ class RolloutInfo(C.Structure):
     _fields_ = [
         ("steps", C.c_int32), ("checkpoints", C.c_int32), ("newton_iterations", C.c_int32),
         ("cg_iterations", C.c_int32), ("recomputed_steps", C.c_int32), ("adjoint_iterations", C.c_int32),
+        ("armijo_polished_steps", C.c_int32), ("pad", C.c_int32),
         ("seconds_forward", C.c_double), ("seconds_backward", C.c_double),
     ]
 

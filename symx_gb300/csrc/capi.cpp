@@ -170,15 +170,35 @@ std::vector<double> flat(const std::vector<Vec3>& v)
 }
 
 // One implicit-Euler step of the handle's problem from (x0, v0): Newton from x = x0, then
-// x0 <- x, v0 <- (x - x0_old) / dt.
+// x0 <- x, v0 <- (x - x0_old) / dt.  When the Armijo line search stalls (near the solution the
+// energy decrease falls below the rounding of the energy), the step continues from its last
+// iterate with full Newton steps, which still converge quadratically there.
 void rollout_step(symxg_solver* s, int n, symxg_rollout_info* info)
 {
     s->x = s->x0;
-    const symx::SolverReturn r = s->newton->solve();
-    const auto& st = s->newton->get_last_solve_stats();
-    if (info) {
-        info->newton_iterations += st.newton_iterations;
-        info->cg_iterations += st.cg_iterations;
+    symx::SolverReturn r = s->newton->solve();
+    auto count = [&] {
+        const auto& st = s->newton->get_last_solve_stats();
+        if (info) {
+            info->newton_iterations += st.newton_iterations;
+            info->cg_iterations += st.cg_iterations;
+        }
+    };
+    count();
+    if (r == symx::SolverReturn::TooManyArmijoIterations) {
+        symx::NewtonSettings& S = s->newton->settings;
+        const symx::NewtonSettings saved = S;
+        S.enable_armijo_backtracking = false;
+        S.max_iterations = 20;
+        try {
+            r = s->newton->solve();
+        } catch (...) {
+            S = saved;
+            throw;
+        }
+        S = saved;
+        count();
+        if (info) info->armijo_polished_steps += 1;
     }
     if (r != symx::SolverReturn::Successful)
         throw std::runtime_error("rollout step " + std::to_string(n) + " did not converge: " + symx::to_string(r));

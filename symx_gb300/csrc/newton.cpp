@@ -1234,13 +1234,11 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
 
 // ---------------------------------------------------------------- adjoint
 namespace {
+// PCG on the Hessian already assembled in precision T (with its block-Jacobi set up).
 template <typename T>
-AdjointInfo adjoint_solve_t(SolverImpl& I, const NewtonSettings& S, const double* rhs, double* lambda, double rel_tol,
-                            int max_iterations, bool project)
+AdjointInfo adjoint_pcg_t(SolverImpl& I, const double* rhs, double* lambda, double rel_tol, int max_iterations)
 {
     cudaStream_t s = I.stream;
-    assemble_t<T>(I, project, S, std::is_same<T, float>::value ? 1 : 0);
-    symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.vstride, I.Dinv<T>(), s);
     // the PCG initialisation takes -b
     std::vector<double> neg(rhs, rhs + I.n_dofs);
     for (double& v : neg) v = -v;
@@ -1303,9 +1301,56 @@ AdjointInfo adjoint_solve_t(SolverImpl& I, const NewtonSettings& S, const double
 AdjointInfo NewtonsMethod::adjoint_solve(const double* rhs, double* lambda, double rel_tol, int max_iterations,
                                          bool project)
 {
-    if (settings.precision == Precision::Mixed)
-        return adjoint_solve_t<float>(*impl, settings, rhs, lambda, rel_tol, max_iterations, project);
-    return adjoint_solve_t<double>(*impl, settings, rhs, lambda, rel_tol, max_iterations, project);
+    SolverImpl& I = *impl;
+    cudaStream_t s = I.stream;
+    if (settings.precision != Precision::Mixed) {
+        assemble_t<double>(I, project, settings, 0);
+        symxg::launch_block_jacobi_setup<double>(I.n_blocks, I.diag_slot.p, I.vals<double>(), I.vstride,
+                                                 I.Dinv<double>(), s);
+        return adjoint_pcg_t<double>(I, rhs, lambda, rel_tol, max_iterations);
+    }
+    // Mixed: FP32 Hessian and PCG inside defect correction.  Each pass solves
+    // H32 d = b - H64 lambda (FP32 PCG to 1e-6, or rel_tol if looser), with the residual formed
+    // from the FP64 Hessian, until |b - H64 lambda| / |b| < rel_tol.
+    assemble_t<float>(I, project, settings, 1);
+    symxg::launch_block_jacobi_setup<float>(I.n_blocks, I.diag_slot.p, I.vals<float>(), I.vstride, I.Dinv<float>(), s);
+    assemble_t<double>(I, project, settings, 0);
+    const size_t n = (size_t)I.n_dofs;
+    double bb = 0.0;
+    for (size_t i = 0; i < n; ++i) bb += rhs[i] * rhs[i];
+    std::fill(lambda, lambda + n, 0.0);
+    AdjointInfo total;
+    if (bb == 0.0) {
+        total.converged = true;
+        return total;
+    }
+    std::vector<double> r(rhs, rhs + n), d(n), Hl(n);
+    DevBuf<double> lam_dev, Hl_dev;
+    lam_dev.alloc(n);
+    Hl_dev.alloc(n);
+    const double inner_tol = std::max(rel_tol, 1e-6);
+    for (int pass = 0; pass < 12; ++pass) {
+        const AdjointInfo inner = adjoint_pcg_t<float>(I, r.data(), d.data(), inner_tol, max_iterations);
+        total.iterations += inner.iterations;
+        if (!inner.converged && inner.iterations == 0) break;
+        for (size_t i = 0; i < n; ++i) lambda[i] += d[i];
+        ck(cudaMemcpyAsync(lam_dev.p, lambda, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload lambda");
+        symxg::launch_bcsr_spmv<double>(I.n_blocks, I.row_ptr.p, I.cols.p, I.vals<double>(), I.vstride, lam_dev.p,
+                                        Hl_dev.p, s);
+        ck(cudaMemcpyAsync(Hl.data(), Hl_dev.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "download product");
+        ck(cudaStreamSynchronize(s), "synchronize");
+        double rr = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            r[i] = rhs[i] - Hl[i];
+            rr += r[i] * r[i];
+        }
+        total.error = std::sqrt(rr / bb);
+        if (total.error < rel_tol) {
+            total.converged = true;
+            break;
+        }
+    }
+    return total;
 }
 
 void NewtonsMethod::parameter_gradient(std::uintptr_t param, const double* lambda, double* out, int64_t n_out)
