@@ -264,6 +264,119 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
         }
 }
 
+// Large element matrices (24 x 24 for Hex8): one warp per matrix, A and V in shared memory
+// (rows padded to N + 1 so that row and column accesses are both free of bank conflicts),
+// parallel cyclic Jacobi in the round-robin ("circle method") order: a sweep is N - 1 rounds
+// of N / 2 disjoint pairs; in each round every pair's rotation is formed from the current
+// A (same formula and convergence test as the register kernels), then all rows, all columns
+// and all eigenvector columns of the round's pairs are rotated by the lanes together.
+template <typename T>
+struct ProjWarpCfg {
+    static constexpr int warps = sizeof(T) == 4 ? 8 : 4;  // 38.4 KB of shared memory per block
+};
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ProjWarpCfg<T>::warps * 32)
+    k_project_pd_warp(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged)
+{
+    static_assert(N % 2 == 0 && N <= 32, "even N up to 32");
+    constexpr int W = ProjWarpCfg<T>::warps;
+    constexpr int LD = N + 1, NP = N / 2, nb = N / 3;
+    __shared__ T sA[W][N * LD];
+    __shared__ T sV[W][N * LD];
+    __shared__ T sc[W][NP], ss[W][NP], sl[W][N];
+    __shared__ int sp[W][NP], sq[W][NP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T* A = sA[w];
+    T* V = sV[w];
+    int nc = 0;
+    constexpr int max_sweeps = 2 * symxg_dev::JacobiTol<T>::max_double_sweeps;
+    for (int64_t m = (int64_t)blockIdx.x * W + w; m < count; m += (int64_t)gridDim.x * W) {
+        T* h = H + m * (int64_t)(N * N);
+        T f = T(0);
+        for (int idx = lane; idx < N * N; idx += 32) {  // block-major storage, read in order
+            const int blk = idx / 9, r = idx % 9;
+            const int i = (blk / nb) * 3 + r / 3, j = (blk % nb) * 3 + r % 3;
+            const T v = h[idx];
+            A[i * LD + j] = v;
+            f += v * v;
+            V[(idx / N) * LD + idx % N] = (idx / N == idx % N) ? T(1) : T(0);
+        }
+        // every lane must take the same decisions below (the loops hold full-warp __syncwarp):
+        // the sums are reduced, then lane 0's value is broadcast
+        f = (T)__shfl_sync(0xffffffffu, warp_sum(f), 0);
+        __syncwarp();
+        int sweep = 0;
+        for (; sweep < max_sweeps; ++sweep) {
+            T off = T(0);
+            for (int idx = lane; idx < N * N; idx += 32) {
+                const int i = idx / N, j = idx % N;
+                if (i != j) off += A[i * LD + j] * A[i * LD + j];
+            }
+            off = (T)__shfl_sync(0xffffffffu, warp_sum(off), 0);
+            if (!(off > symxg_dev::JacobiTol<T>::rel2() * f)) break;
+            for (int r = 0; r < N - 1; ++r) {
+                if (lane < NP) {
+                    const int a = lane == 0 ? r : (r + lane) % (N - 1);
+                    const int b = lane == 0 ? N - 1 : (r - lane + N - 1) % (N - 1);
+                    const int p = min(a, b), q = max(a, b);
+                    const T t = symxg_dev::jacobi_t(A[p * LD + p], A[q * LD + q], A[p * LD + q]);
+                    const T c = symxg_dev::inv_hypot1(t);
+                    sc[w][lane] = c;
+                    ss[w][lane] = t * c;
+                    sp[w][lane] = p;
+                    sq[w][lane] = q;
+                }
+                __syncwarp();
+                for (int idx = lane; idx < NP * N; idx += 32) {  // rows p, q
+                    const int k = idx / N, j = idx % N, p = sp[w][k], q = sq[w][k];
+                    const T c = sc[w][k], sn = ss[w][k], apj = A[p * LD + j], aqj = A[q * LD + j];
+                    A[p * LD + j] = c * apj - sn * aqj;
+                    A[q * LD + j] = sn * apj + c * aqj;
+                }
+                __syncwarp();
+                for (int idx = lane; idx < NP * N; idx += 32) {  // columns p, q
+                    const int k = idx / N, i = idx % N, p = sp[w][k], q = sq[w][k];
+                    const T c = sc[w][k], sn = ss[w][k], aip = A[i * LD + p], aiq = A[i * LD + q];
+                    A[i * LD + p] = c * aip - sn * aiq;
+                    A[i * LD + q] = sn * aip + c * aiq;
+                }
+                for (int idx = lane; idx < NP * N; idx += 32) {  // eigenvector columns p, q
+                    const int k = idx / N, i = idx % N, p = sp[w][k], q = sq[w][k];
+                    const T c = sc[w][k], sn = ss[w][k], vip = V[i * LD + p], viq = V[i * LD + q];
+                    V[i * LD + p] = c * vip - sn * viq;
+                    V[i * LD + q] = sn * vip + c * viq;
+                }
+                __syncwarp();
+            }
+        }
+        if (sweep == max_sweeps) nc = 1;
+        bool mine = false;
+        if (lane < N) {
+            T l = A[lane * LD + lane];
+            if (l < eps) {
+                mine = true;
+                l = mirroring ? -l : eps;
+            }
+            sl[w][lane] = l;
+        }
+        const bool changed = __any_sync(0xffffffffu, mine);
+        __syncwarp();
+        if (changed) {
+            for (int idx = lane; idx < N * N; idx += 32) {
+                const int blk = idx / 9, r = idx % 9;
+                const int i = (blk / nb) * 3 + r / 3, j = (blk % nb) * 3 + r % 3;
+                T acc = T(0);
+#pragma unroll 4
+                for (int k = 0; k < N; ++k) acc += V[i * LD + k] * sl[w][k] * V[j * LD + k];
+                h[idx] = acc;
+            }
+        }
+        __syncwarp();  // the next matrix reuses this warp's shared memory
+    }
+    if (nc) *not_converged = 1;
+}
+
 // ---------------------------------------------------------------- BCSR value layouts
 // Component m (row-major inside the 3x3 block) of block k is vals[base(k) + m * step()].
 // Strided (the C ABI's): base = k, step = vstride (component-major arrays).
@@ -788,7 +901,9 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
         };
         for (int j = 0; j < n_stages; ++j) {
             const unsigned g = seq + j, s = g % NS;
-            if (*abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1)) {
+            // one decision per warp: the product below shuffles over the full warp
+            const bool stop = __any_sync(0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1));
+            if (stop) {
                 *abort_flag = 1;
                 break;
             }
@@ -1352,6 +1467,11 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
         case 6: k_project_pd_unrolled<T, 6><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
         case 9: k_project_pd_unrolled<T, 9><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
         case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
+        case 24: {
+            constexpr int W = ProjWarpCfg<T>::warps;
+            k_project_pd_warp<T, 24><<<blocks_for(count, W), W * 32, 0, s>>>(H, count, eps, mirroring, not_converged);
+            break;
+        }
         default:
             if (N > 24 || N % 3 != 0) throw std::runtime_error("symx_gb300: projection supports N = 3k <= 24");
             k_project_pd_generic<T><<<blocks_for(count, 64), 64, 0, s>>>(H, N, count, eps, mirroring, not_converged);
