@@ -165,18 +165,24 @@ def bcsr_pcg(rowptr, cols, vals, b, abs_tol, rel_tol, max_iter):
     return x, int(it[0]), bool(conv[0])
 
 
-def adjoint(P: "Problem", p: dict, dLdx):
+def adjoint(P: "Problem", p: dict, dLdx, solver: str = "direct"):
     """FP64 adjoint at the oracle's current positions: lambda = H^-1 dL/dx with H the true
     (unprojected) Hessian, solved with a sparse direct factorisation, and the parameter
     gradients -lambda . dg/dq in closed form: the Neo-Hookean element gradient is linear in
     (mu, lambda), so dg_e/dmu_e = g_e(mu=1, lambda=0) and dg_e/dlambda_e = g_e(0, 1); the
     inertia gradient m (x - x0 - dt v0 - dt^2 g) / dt^2 gives -dg/dx0 = m / dt^2 and
-    -dg/dv0 = m / dt.  Returns a dict of lambda, dLdmu, dLdlam, dLdx0, dLdv0 (flat)."""
+    -dg/dv0 = m / dt.  solver: "direct" (sparse LU) or "pcg" (the oracle's PCG to 1e-12, for
+    systems too large to factor).  Returns a dict of lambda, dLdmu, dLdlam, dLdx0, dLdv0 (flat)."""
     import scipy.sparse.linalg as spla
 
     rp, cols, vals, _ = P.assemble(project=False)
-    A = bcsr_to_scipy(rp, cols, vals)
-    lam = spla.spsolve(A.tocsc(), np.asarray(dLdx, dtype=np.float64).ravel())
+    b = np.asarray(dLdx, dtype=np.float64).ravel()
+    if solver == "direct":
+        lam = spla.spsolve(bcsr_to_scipy(rp, cols, vals).tocsc(), b)
+    else:  # large systems: the oracle's block-Jacobi PCG to 1e-12
+        lam, _, conv = bcsr_pcg(rp, cols, vals, b, 0.0, 1e-12, 100000)
+        if not conv:
+            raise RuntimeError("oracle adjoint PCG did not converge")
     x = P.get_x()
     X, conn = p["X"], p["conn"]
     ne = conn.shape[0]
