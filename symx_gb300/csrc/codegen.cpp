@@ -48,11 +48,83 @@ __device__ __forceinline__ double symxg_acos(double x) { return acos(x); }
 __device__ __forceinline__ float symxg_acos(float x) { return acosf(x); }
 __device__ __forceinline__ double symxg_atan(double x) { return atan(x); }
 __device__ __forceinline__ float symxg_atan(float x) { return atanf(x); }
+// ---- double-float: an unevaluated sum hi + lo of two floats (about 48 significant bits).
+// Arithmetic runs on the FP32 pipe with error-free transformations (TwoSum; TwoProd through
+// fmaf), Dekker / Knuth style; the __f*_rn intrinsics keep the compiler from contracting or
+// reassociating them.  Transcendentals go through double.
+struct symxg_df {
+    float hi, lo;
+    __device__ __forceinline__ symxg_df() : hi(0.0f), lo(0.0f) {}
+    __device__ __forceinline__ symxg_df(float h, float l) : hi(h), lo(l) {}
+    // nearest split of a double (folded at compile time for literals)
+    __device__ __forceinline__ symxg_df(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    __device__ __forceinline__ void operator+=(const symxg_df& b);
+    __device__ __forceinline__ void operator*=(const symxg_df& b);
+};
+__device__ __forceinline__ double symxg_to_double(const symxg_df& a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ symxg_df symxg_df_fast(float a, float b)  // |a| >= |b|
+{
+    const float s = __fadd_rn(a, b);
+    return symxg_df(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ symxg_df operator+(const symxg_df& a, const symxg_df& b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return symxg_df_fast(s, e);
+}
+__device__ __forceinline__ symxg_df operator-(const symxg_df& a) { return symxg_df(-a.hi, -a.lo); }
+__device__ __forceinline__ symxg_df operator-(const symxg_df& a, const symxg_df& b) { return a + (-b); }
+__device__ __forceinline__ symxg_df operator*(const symxg_df& a, const symxg_df& b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return symxg_df_fast(p, e);
+}
+__device__ __forceinline__ symxg_df operator/(const symxg_df& a, const symxg_df& b)
+{
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const symxg_df r = a - b * symxg_df(q1, 0.0f);
+    const float q2 = __fdiv_rn(r.hi, b.hi);
+    const symxg_df r2 = r - b * symxg_df(q2, 0.0f);
+    const float q3 = __fdiv_rn(r2.hi, b.hi);
+    return symxg_df_fast(q1, q2) + symxg_df(q3, 0.0f);
+}
+__device__ __forceinline__ bool operator>(const symxg_df& a, const symxg_df& b)
+{
+    return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo);
+}
+__device__ __forceinline__ void symxg_df::operator+=(const symxg_df& b) { *this = *this + b; }
+__device__ __forceinline__ void symxg_df::operator*=(const symxg_df& b) { *this = *this * b; }
+__device__ __forceinline__ symxg_df symxg_sqrt(const symxg_df& a)
+{
+    if (!(a.hi > 0.0f)) return symxg_df(sqrtf(a.hi), 0.0f);
+    const float s = sqrtf(a.hi);
+    const symxg_df e = a - symxg_df(s, 0.0f) * symxg_df(s, 0.0f);  // one Newton step in double-float
+    return symxg_df_fast(s, __fdiv_rn(e.hi, __fmul_rn(2.0f, s)));
+}
+__device__ __forceinline__ symxg_df symxg_ln(const symxg_df& a) { return symxg_df(symxg_ln(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_log10(const symxg_df& a) { return symxg_df(symxg_log10(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_exp(const symxg_df& a) { return symxg_df(exp(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_powf(const symxg_df& x, const symxg_df& p)
+{
+    return symxg_df(pow(symxg_to_double(x), symxg_to_double(p)));
+}
+__device__ __forceinline__ symxg_df symxg_sin(const symxg_df& a) { return symxg_df(sin(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_cos(const symxg_df& a) { return symxg_df(cos(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_tan(const symxg_df& a) { return symxg_df(tan(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_asin(const symxg_df& a) { return symxg_df(asin(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_acos(const symxg_df& a) { return symxg_df(acos(symxg_to_double(a))); }
+__device__ __forceinline__ symxg_df symxg_atan(const symxg_df& a) { return symxg_df(atan(symxg_to_double(a))); }
 // x^n for n >= 2 by binary powering.
 template <typename T>
 __device__ __forceinline__ T symxg_powi(T x, int n)
 {
-    T r = T(1), b = x;
+    T r = T(1.0), b = x;
     while (n > 0) { if (n & 1) r *= b; b *= b; n >>= 1; }
     return r;
 }

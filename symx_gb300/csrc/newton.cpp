@@ -115,6 +115,7 @@ struct CompiledPotential {
     DevBuf<int32_t> conn;
     DevBuf<const double*> map_ptrs;
     int n_cache = 0, n_qp = 1;      // hoisted values per element and quadrature point
+    bool cache_df = false;          // the cache holds (hi, lo) float pairs (mixed-precision kernels)
     DevBuf<double> cache;
     int64_t e_off = 0, g_off = 0, h_off = 0;  // offsets: elements, gradient blocks, Hessian blocks
 };
@@ -214,6 +215,10 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
     s << emit_device_function(g, h_bm, "symxg_eval_h_f32", "float", acc, nullptr, &ext);
     s << emit_device_function(g, e_only, "symxg_eval_e", "double", acc, oe, &ext);
     if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond", "double", false, nullptr, &ext);
+    // mixed precision: energy and gradient in double-float (FP32 pipe), see the prelude
+    s << emit_device_function(g, eg, "symxg_eval_eg_df", "symxg_df", acc, nullptr, &ext);
+    s << emit_device_function(g, e_only, "symxg_eval_e_df", "symxg_df", acc, nullptr, &ext);
+    if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond_df", "symxg_df", false, nullptr, &ext);
     if (K > 0) s << emit_device_function(g, frontier, "symxg_eval_pre", "double", false, nullptr, nullptr);
     if (sum.n_iterations > 0) {
         s << "static __device__ const double symxg_sum_data[" << sum.data.size() << "] = {";
@@ -312,9 +317,111 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
             s << "        symxg_eval_h_f32(in32, c32, h);\n";
         }
         s << "    }\n";
-        s << "    E[e] = eg[0];\n    for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = eg[1 + i];\n";
+        s << "    E[e] = eg[0];\n";
+        // 16-byte stores where the rows allow it (one element's outputs are contiguous)
+        if (NG % 2 == 0)
+            s << "    if ((reinterpret_cast<unsigned long long>(G) & 15ull) == 0ull) {\n"
+              << "        double2* G2 = reinterpret_cast<double2*>(G + e * " << NG << "LL);\n"
+              << "        for (int i = 0; i < " << NG / 2 << "; ++i) G2[i] = make_double2(eg[1 + 2 * i], eg[2 + 2 * i]);\n"
+              << "    } else\n";
+        s << "    for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = eg[1 + i];\n";
+        if (prec == 0 && NH % 2 == 0)
+            s << "    if ((reinterpret_cast<unsigned long long>(H) & 15ull) == 0ull) {\n"
+              << "        double2* H2 = reinterpret_cast<double2*>(H + e * " << NH << "LL);\n"
+              << "        for (int i = 0; i < " << NH / 2 << "; ++i) H2[i] = make_double2(h[2 * i], h[2 * i + 1]);\n"
+              << "    } else\n";
+        if (prec == 1 && NH % 4 == 0)
+            s << "    if ((reinterpret_cast<unsigned long long>(H) & 15ull) == 0ull) {\n"
+              << "        float4* H4 = reinterpret_cast<float4*>(H + e * " << NH << "LL);\n"
+              << "        for (int i = 0; i < " << NH / 4 << "; ++i) H4[i] = make_float4(h[4 * i], h[4 * i + 1], h[4 * i + 2], "
+              << "h[4 * i + 3]);\n    } else\n";
         s << "    for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = h[i];\n}\n";
     }
+    // ---- mixed precision: the cache holds (hi, lo) float pairs in place of the doubles
+    s << "extern \"C\" __global__ void __launch_bounds__(256) symxg_cache_to_df(long long count, double* cache)\n{\n"
+         "    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (i >= count) return;\n"
+         "    const symxg_df v(cache[i]);\n    reinterpret_cast<float2*>(cache)[i] = make_float2(v.hi, v.lo);\n}\n";
+    auto set_sum_df = [&](const std::string& q) {
+        std::ostringstream t;
+        if (sum.n_iterations == 0 || !sum_used(main_symbol)) return t.str();
+        for (int j = 0; j < sum.stride; ++j) {
+            const std::string v = "symxg_sum_data[" + q + " * " + std::to_string(sum.stride) + " + " + std::to_string(j) + "]";
+            t << "        ind[" << (sum.first_symbol + j) << "] = symxg_df(" << v << "); in32[" << (sum.first_symbol + j)
+              << "] = (float)" << v << ";\n";
+        }
+        return t.str();
+    };
+    auto load_cache_df = [&](const std::string& q) {
+        std::ostringstream t;
+        t << "        symxg_df c[" << std::max(1, K) << "]; float c32[" << std::max(1, K) << "];\n";
+        if (K > 0)
+            t << "        for (int k = 0; k < " << K << "; ++k) { const float2 v = cache[((long long)" << q << " * " << K
+              << "LL + k) * n + e]; c[k] = symxg_df(v.x, v.y); c32[k] = v.x; }\n";
+        else
+            t << "        c[0] = symxg_df(0.0); c32[0] = 0.0f;\n";
+        return t.str();
+    };
+    auto head_df = [&]() {
+        std::ostringstream t;
+        t << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
+        t << "    const float2* __restrict__ cache = reinterpret_cast<const float2*>(cache_raw);\n";
+        t << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
+        t << "    symxg_df ind[" << NS << "]; float in32[" << NS << "];\n";
+        t << "    for (int i = 0; i < " << NS << "; ++i) { ind[i] = symxg_df(in[i]); in32[i] = ind[i].hi; }\n";
+        return t.str();
+    };
+    auto cond_check_df = [&](const std::string& zero_writes) {
+        if (cond < 0) return std::string();
+        std::ostringstream t;
+        t << "    {\n" << set_sum_df("0") << load_cache_df("0")
+          << "        symxg_df cv[1]; symxg_eval_cond_df(ind, c, cv);\n        if (!(cv[0] > symxg_df(0.0))) {\n"
+          << zero_writes << "            return;\n        }\n    }\n";
+        return t.str();
+    };
+    const std::string sig_df =
+        "(long long n, const int* __restrict__ conn, const double* const* __restrict__ maps, "
+        "const double* __restrict__ cache_raw, double* __restrict__ E";
+    {
+        s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_egh_df32" << sig_df
+          << ", double* __restrict__ G, float* __restrict__ H)\n{\n" << head_df();
+        std::ostringstream zw;
+        zw << "            E[e] = 0.0;\n            for (int i = 0; i < " << NG << "; ++i) G[e * " << NG
+           << "LL + i] = 0.0;\n            for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = 0.0f;\n";
+        s << cond_check_df(zw.str());
+        s << "    symxg_df eg[" << (NG + 1) << "];\n    float h[" << NH << "];\n";
+        if (acc) {
+            s << "    for (int i = 0; i < " << NH << "; ++i) h[i] = 0.0f;\n";
+            s << "    for (int q = 0; q < " << NQ << "; ++q) {\n";
+        } else {
+            s << "    { const int q = 0; (void)q;\n";
+        }
+        s << set_sum_df("q") << load_cache_df("q");
+        s << "        symxg_eval_eg_df(ind, c, eg);\n        symxg_eval_h_f32(in32, c32, h);\n    }\n";
+        s << "    E[e] = symxg_to_double(eg[0]);\n";
+        // 16-byte stores where the rows allow it (one element's outputs are contiguous)
+        if (NG % 2 == 0)
+            s << "    if ((reinterpret_cast<unsigned long long>(G) & 15ull) == 0ull) {\n"
+              << "        double2* G2 = reinterpret_cast<double2*>(G + e * " << NG << "LL);\n"
+              << "        for (int i = 0; i < " << NG / 2 << "; ++i) G2[i] = make_double2(symxg_to_double(eg[1 + 2 * i]), "
+              << "symxg_to_double(eg[2 + 2 * i]));\n    } else\n";
+        s << "    for (int i = 0; i < " << NG << "; ++i) G[e * " << NG << "LL + i] = symxg_to_double(eg[1 + i]);\n";
+        if (NH % 4 == 0)
+            s << "    if ((reinterpret_cast<unsigned long long>(H) & 15ull) == 0ull) {\n"
+              << "        float4* H4 = reinterpret_cast<float4*>(H + e * " << NH << "LL);\n"
+              << "        for (int i = 0; i < " << NH / 4 << "; ++i) H4[i] = make_float4(h[4 * i], h[4 * i + 1], h[4 * i + 2], "
+              << "h[4 * i + 3]);\n    } else\n";
+        s << "    for (int i = 0; i < " << NH << "; ++i) H[e * " << NH << "LL + i] = h[i];\n}\n";
+    }
+    {
+        s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_e_df" << sig_df << ")\n{\n" << head_df();
+        s << cond_check_df("            E[e] = 0.0;\n");
+        s << "    symxg_df ev[1];\n";
+        if (acc) s << "    for (int q = 0; q < " << NQ << "; ++q) {\n";
+        else s << "    { const int q = 0; (void)q;\n";
+        s << set_sum_df("q") << load_cache_df("q");
+        s << "        symxg_eval_e_df(ind, c, ev);\n    }\n    E[e] = symxg_to_double(ev[0]);\n}\n";
+    }
+
     // energy-only kernel (line search)
     s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_e" << sig_common << ")\n{\n";
     s << "    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n    if (e >= n) return;\n";
@@ -467,24 +574,47 @@ struct SolverImpl {
         ck(cudaStreamSynchronize(stream), "synchronize");
     }
 
-    void launch_eval(int mode /*0 f64 H, 1 f32 H, 2 energy only*/)
+    // The element kernels of the mixed path read the hoisted cache as double-float pairs, the
+    // FP64 kernels as doubles: convert in place, or recompute the doubles, when the path changes.
+    void ensure_cache(CompiledPotential& cp, bool df)
+    {
+        if (cp.n_cache == 0 || cp.n_elements == 0 || cp.cache_df == df) return;
+        long long n = cp.n_elements;
+        if (df) {
+            long long count = n * cp.n_qp * cp.n_cache;
+            double* c = cp.cache.p;
+            void* args[] = {&count, &c};
+            cp.module->launch("symxg_cache_to_df", dim3((unsigned)((count + 255) / 256)), dim3(256), 0, stream, args);
+        } else {
+            const int32_t* conn = cp.conn.p;
+            const double* const* maps = cp.map_ptrs.p;
+            double* cache = cp.cache.p;
+            void* args[] = {&n, &conn, &maps, &cache};
+            cp.module->launch("symxg_pre", dim3((unsigned)((n + 127) / 128)), dim3(128), 0, stream, args);
+        }
+        cp.cache_df = df;
+    }
+
+    // mode: 0 E+g+H in FP64, 1 mixed (E+g double-float, H FP32), 2 E only FP64, 3 E only double-float
+    void launch_eval(int mode)
     {
         for (auto& cp : pots) {
             if (cp.n_elements == 0) continue;
+            ensure_cache(cp, mode == 1 || mode == 3);
             long long n = cp.n_elements;
             const int32_t* conn = cp.conn.p;
             const double* const* maps = cp.map_ptrs.p;
             const double* cache = cp.cache.p;
             double* E = E_el.p + cp.e_off;
             const unsigned grid = (unsigned)((n + 127) / 128);
-            if (mode == 2) {
+            if (mode >= 2) {
                 void* args[] = {&n, &conn, &maps, &cache, &E};
-                cp.module->launch("symxg_e", dim3(grid), dim3(128), 0, stream, args);
+                cp.module->launch(mode == 2 ? "symxg_e" : "symxg_e_df", dim3(grid), dim3(128), 0, stream, args);
             } else {
                 double* G = g_el.p + cp.g_off * 3;
                 void* H = mode == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
                 void* args[] = {&n, &conn, &maps, &cache, &E, &G, &H};
-                cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_f32", dim3(grid), dim3(128), 0, stream, args);
+                cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_df32", dim3(grid), dim3(128), 0, stream, args);
             }
         }
     }
@@ -873,6 +1003,7 @@ void NewtonsMethod::upload()
         double* cache = cp.cache.p;
         void* args[] = {&n, &conn, &maps, &cache};
         cp.module->launch("symxg_pre", dim3((unsigned)((n + 127) / 128)), dim3(128), 0, I.stream, args);
+        cp.cache_df = false;
     }
     ck(cudaStreamSynchronize(I.stream), "synchronize");
     h2d_bytes_ = bytes;
@@ -1188,7 +1319,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             double E_thr = E0 + expected * step;
             int a = 0;
             for (; a < S.max_backtracking_armijo_iterations; ++a) {
-                I.launch_eval(2);
+                I.launch_eval(mode == 1 ? 3 : 2);  // the energy in the precision of the step's E and g
                 symxg::launch_sum(I.E_el.p, I.n_elements_total, I.partials.p, I.tickets.p + 4, I.scalars.p, s);
                 I.read_scalars(1);
                 const double E1 = I.h_scalars[0];

@@ -135,6 +135,33 @@ def test_mixed_element_hessians_within_float_tolerance(sg):
     assert np.max(np.abs(H32 - H64)) <= 1e-5 * np.max(np.abs(H64))
 
 
+@pytest.mark.parametrize("case", ["tet4_6p", "hex8_3"])
+def test_mixed_energy_gradient_double_float_accuracy(sg, case):
+    """The mixed path evaluates element energies and gradients in double-float (about 48
+    significant bits): within 1e-12 of the FP64 path, element by element; the line-search
+    energy (its own kernel) likewise."""
+    from symx_gb300 import problems
+
+    p, s = make(sg, case, precision="mixed")
+    # a deformed state (at rest the element energies are rounding noise around zero)
+    x = p["X"] + 5e-4 * problems.normal(26, p["X"].size).reshape(-1, 3)
+    s.set_state(x, p["x0"], p["v0"])
+    E32, g32, _ = s.element_outputs(0, project=False)
+    s.set_settings(precision="fp64")
+    E64, g64, _ = s.element_outputs(0, project=False)
+    assert np.max(np.abs(E32 - E64)) <= 1e-12 * np.max(np.abs(E64))
+    assert np.max(np.abs(g32 - g64)) <= 1e-12 * np.max(np.abs(g64))
+    # whole solves: the mixed solve still lands on the FP64 solution
+    s.set_state(p["x_init"], p["x0"], p["v0"])
+    st64 = s.solve()
+    x64 = s.get_positions()
+    s.set_settings(precision="mixed")
+    s.set_state(p["x_init"], p["x0"], p["v0"])
+    st32 = s.solve()
+    assert st32["solver_return"] == 0 and st64["solver_return"] == 0
+    assert np.max(np.abs(s.get_positions() - x64)) <= 1e-6 * np.max(np.abs(x64 - p["x0"]))
+
+
 @pytest.mark.parametrize("dtype,tol", [("float64", 1e-9), ("float32", 1e-4)])
 def test_project_pd_kernel_matches_reference(sg, golden, dtype, tol):
     import torch
