@@ -192,6 +192,13 @@ std::shared_ptr<CudaModule> CudaModule::build(const std::string& source, const s
     return m;
 }
 
+std::shared_ptr<CudaModule> CudaModule::load(const std::string& cubin)
+{
+    auto m = std::shared_ptr<CudaModule>(new CudaModule());
+    check_drv(driver().load(&m->module_, cubin.data()), "cuModuleLoadData");
+    return m;
+}
+
 CudaModule::~CudaModule()
 {
     if (module_) driver().unload(module_);

@@ -31,6 +31,8 @@ public:
     // Throws std::runtime_error with the NVRTC log on failure.
     static std::shared_ptr<CudaModule> build(const std::string& source, const std::string& cache_dir,
                                              const std::vector<std::string>& extra_options, CompileInfo* info = nullptr);
+    // Load an already compiled CUBIN image into the current device's primary context.
+    static std::shared_ptr<CudaModule> load(const std::string& cubin);
     ~CudaModule();
     // Launch `kernel` with `args` (pointers to each argument, as cuLaunchKernel takes them).
     void launch(const std::string& kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t stream, void** args);

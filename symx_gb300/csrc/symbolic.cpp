@@ -3,6 +3,7 @@
 #include "symbolic.h"
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <stdexcept>
@@ -240,6 +241,13 @@ bool Scalar::is_constant() const
     const Op o = (*graph)[expr_id].op;
     return o == Op::Zero || o == Op::One || o == Op::Const;
 }
+std::string Scalar::get_checksum() const
+{
+    char buf[17];
+    std::snprintf(buf, sizeof(buf), "%016llx", (unsigned long long)graph->hash({expr_id}));
+    return buf;
+}
+
 void Scalar::set_value(double v) const
 {
     if (!is_symbol()) throw std::runtime_error("symx: set_value on a non-symbol");

@@ -116,6 +116,9 @@ public:
     int32_t get_symbol_idx() const { return graph->symbol_index(expr_id); }
     void set_value(double v) const;
     double eval() const { return graph->eval(expr_id); }
+    // Reproducible hash of the part of the graph this expression depends on (hex string),
+    // the cache id of a Compiled<T> (reference: symx/src/symbol/Scalar.h:75).
+    std::string get_checksum() const;
     Scalar make_constant(double v) const { return Scalar(graph->constant(v), graph); }
     Scalar get_zero() const { return Scalar(0, graph); }
     Scalar get_one() const { return Scalar(1, graph); }

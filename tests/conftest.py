@@ -29,3 +29,20 @@ def golden():
         return np.load(os.path.join(d, name + ".npz"), allow_pickle=False)
 
     return load
+
+
+@pytest.fixture(scope="session")
+def compiled_test(lib):
+    """tests/cpp/test_compiled.cpp built against the library (C++ Compiled<T> API)."""
+    import subprocess
+
+    from symx_gb300.build import cuda_home
+
+    libdir = os.path.join(ROOT, "symx_gb300", "_build")
+    exe = os.path.join(libdir, "test_compiled")
+    cuda = cuda_home()
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(cuda, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "test_compiled.cpp"), "-o", exe, "-L" + libdir, "-lsymxg",
+                    "-Wl,-rpath," + libdir, "-L" + os.path.join(cuda, "lib64"), "-lcudart",
+                    "-Wl,-rpath," + os.path.join(cuda, "lib64")], check=True)
+    return exe

@@ -203,6 +203,18 @@ def test_cpp_generated_kernels_compile_with_nvrtc(cpp_test, tmp_path):
     assert "nvrtc PASS" in r.stdout
 
 
+def test_cpp_compiled_generates_and_caches_without_a_device(compiled_test, tmp_path):
+    """Compiled<double> without a GPU: the kernel is generated and NVRTC-compiled, its
+    source, CUBIN and cache record are written, and loading fails with a clear error."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present: the GPU test covers Compiled<T>")
+    r = subprocess.run([compiled_test, "nogpu", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "compiled PASS" in r.stdout
+
+
 def test_host_build_of_projection_matches_reference(golden, tmp_path):
     """The device projection code built for the host: full and translation-deflated
     decompositions against the reference's project_to_PD_inplace on the 12x12 fixtures
