@@ -112,6 +112,12 @@ def workload_name(name, p):
             f"{p['conn'].shape[0]:,} elements)")
 
 
+def projection_kernel(p):
+    if p["conn"].shape[1] == 4:
+        return "k_project_pd_deflated<float,12> + k_project_pd_listed<float,12> (fallback list)"
+    return "k_project_pd_pairs<float,24> (one warp per matrix, pair-block parallel Jacobi)"
+
+
 def spmv_roofline(solver, torch, sg, n_rep=30):
     """Time the BCSR SpMV kernel (the PCG's dominant HBM-bound kernel) on the assembled
     mixed-precision Hessian of the workload, with CUDA events on its stream."""
@@ -288,7 +294,7 @@ def run_ours(args):
         "spmv_standalone": {"kernel": "k_bcsr_spmv<float>", "algorithmic_bytes": rf["algorithmic_bytes"],
                             "launch_seconds": rf["seconds"], "achieved_gbs": round(achieved_standalone, 1),
                             "frac": round(achieved_standalone / peak, 4)},
-        "projection": {"kernel": "k_project_pd_deflated<float,12> + k_project_pd_listed<float,12> (fallback list)", "launch_seconds": t_proj, "launches": int(n_proj),
+        "projection": {"kernel": projection_kernel(p), "launch_seconds": t_proj, "launches": int(n_proj),
                        "matrices_per_launch": int(p["conn"].shape[0]),
                        "ns_per_matrix": round(t_proj / p["conn"].shape[0] * 1e9, 3) if n_proj else None},
         "clocks": clocks.summary(),

@@ -264,31 +264,116 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
         }
 }
 
-// Large element matrices (24 x 24 for Hex8): one warp per matrix, A and V in shared memory
-// (rows padded to N + 1 so that row and column accesses are both free of bank conflicts),
-// parallel cyclic Jacobi in the round-robin ("circle method") order: a sweep is N - 1 rounds
-// of N / 2 disjoint pairs; in each round every pair's rotation is formed from the current
-// A (same formula and convergence test as the register kernels), then all rows, all columns
-// and all eigenvector columns of the round's pairs are rotated by the lanes together.
+// Large element matrices (24 x 24 for Hex8): one warp per matrix, parallel cyclic Jacobi in
+// the round-robin ("circle method") order: a sweep is N - 1 rounds of N / 2 disjoint index
+// pairs, and one round applies all N / 2 rotations at once, A <- J^T A J with J block diagonal
+// over the pairs.  Written per 2 x 2 block of pairs (k, l) this is B_kl <- R_k^T B_kl R_l, so
+//   * lane k < N / 2 forms pair k's rotation from its diagonal block (same formula and
+//     convergence test as the register kernels) and updates that block in place;
+//   * the N/2 (N/2 - 1) / 2 off-diagonal blocks of the upper triangle are spread over the
+//     lanes; each lane reads its four entries, applies both rotations and writes them back,
+//     with the entry offsets of every round taken from a per-block table in shared memory;
+//   * lane i keeps row i of the eigenvector matrix V in registers (the rounds are unrolled,
+//     so the column pairs are compile-time indices) and rotates it with the round's (c, s)
+//     taken from the owning lanes by shuffles.
+// Only the upper triangle of A in shared memory is kept up to date.  No two lanes touch the
+// same entry within a round, so one __syncwarp per round suffices.
 template <typename T>
-struct ProjWarpCfg {
-    static constexpr int warps = sizeof(T) == 4 ? 8 : 4;  // 38.4 KB of shared memory per block
+struct ProjPairsCfg {
+    static constexpr int warps = sizeof(T) == 4 ? 8 : 4;
 };
 
-template <typename T, int N>
-__global__ void __launch_bounds__(ProjWarpCfg<T>::warps * 32)
-    k_project_pd_warp(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged)
+// Pair k of round r (position N - 1 is fixed, the others rotate), as (p, q) with p < q.
+template <int N>
+__host__ __device__ __forceinline__ void rr_pair(int r, int k, int& p, int& q)
 {
-    static_assert(N % 2 == 0 && N <= 32, "even N up to 32");
-    constexpr int W = ProjWarpCfg<T>::warps;
-    constexpr int LD = N + 1, NP = N / 2, nb = N / 3;
-    __shared__ T sA[W][N * LD];
-    __shared__ T sV[W][N * LD];
-    __shared__ T sc[W][NP], ss[W][NP], sl[W][N];
-    __shared__ int sp[W][NP], sq[W][NP];
+    int a = r, b = N - 1;
+    if (k != 0) {
+        a = r + k;
+        if (a >= N - 1) a -= N - 1;
+        b = r - k + N - 1;
+        if (b >= N - 1) b -= N - 1;
+    }
+    p = a < b ? a : b;
+    q = a < b ? b : a;
+}
+
+// Off-diagonal block b of the upper triangle over pairs, as (k, l), k < l (row-major order).
+template <int NP>
+__device__ __forceinline__ void off_block(int b, int& k, int& l)
+{
+    k = 0;
+    l = 0;
+    for (int kk = 0; kk < NP; ++kk) {
+        const int n = NP - 1 - kk;
+        if (b < n) {
+            k = kk;
+            l = kk + 1 + b;
+            return;
+        }
+        b -= n;
+    }
+}
+
+// sum_k w[k] * row[k] with 16-byte shared-memory loads (row 16-byte aligned)
+template <int N>
+__device__ __forceinline__ float row_dot(const float (&w)[N], const float* row)
+{
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; k += 4) {
+        const float4 r = *reinterpret_cast<const float4*>(row + k);
+        acc = fmaf(w[k], r.x, acc);
+        acc = fmaf(w[k + 1], r.y, acc);
+        acc = fmaf(w[k + 2], r.z, acc);
+        acc = fmaf(w[k + 3], r.w, acc);
+    }
+    return acc;
+}
+template <int N>
+__device__ __forceinline__ double row_dot(const double (&w)[N], const double* row)
+{
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < N; k += 2) {
+        const double2 r = *reinterpret_cast<const double2*>(row + k);
+        acc = fma(w[k], r.x, acc);
+        acc = fma(w[k + 1], r.y, acc);
+    }
+    return acc;
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32)
+    k_project_pd_pairs(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged)
+{
+    static_assert(N % 6 == 0 && N <= 32, "N a multiple of 6 up to 30 (3 x 3 blocks, pairs, 16-byte rows)");
+    constexpr int W = ProjPairsCfg<T>::warps;
+    constexpr int LD = N + 1, NP = N / 2, NR = N - 1, NOFF = NP * (NP - 1) / 2, SLOTS = (NOFF + 31) / 32, nb = N / 3;
+    __shared__ __align__(16) T sA[W][N * LD];
+    __shared__ uint2 sTab[NR][SLOTS][32];  // per round, slot and lane: 4 x 16-bit entry offsets
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    for (int e = threadIdx.x; e < NR * SLOTS * 32; e += blockDim.x) {
+        const int r = e / (SLOTS * 32), j = (e / 32) % SLOTS, ln = e % 32, b = ln + 32 * j;
+        uint2 v = make_uint2(0u, 0u);
+        if (b < NOFF) {
+            int k, l, pk, qk, pl, ql;
+            off_block<NP>(b, k, l);
+            rr_pair<N>(r, k, pk, qk);
+            rr_pair<N>(r, l, pl, ql);
+            auto up = [](int i, int jj) { return (unsigned)(i < jj ? i * LD + jj : jj * LD + i); };
+            v.x = up(pk, pl) | (up(pk, ql) << 16);
+            v.y = up(qk, pl) | (up(qk, ql) << 16);
+        }
+        sTab[r][j][ln] = v;
+    }
+    int bk[SLOTS], bl[SLOTS];
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j) off_block<NP>(lane + 32 * j < NOFF ? lane + 32 * j : 0, bk[j], bl[j]);
+    __syncthreads();
+
     T* A = sA[w];
-    T* V = sV[w];
     int nc = 0;
     constexpr int max_sweeps = 2 * symxg_dev::JacobiTol<T>::max_double_sweeps;
     for (int64_t m = (int64_t)blockIdx.x * W + w; m < count; m += (int64_t)gridDim.x * W) {
@@ -300,10 +385,11 @@ __global__ void __launch_bounds__(ProjWarpCfg<T>::warps * 32)
             const T v = h[idx];
             A[i * LD + j] = v;
             f += v * v;
-            V[(idx / N) * LD + idx % N] = (idx / N == idx % N) ? T(1) : T(0);
         }
-        // every lane must take the same decisions below (the loops hold full-warp __syncwarp):
-        // the sums are reduced, then lane 0's value is broadcast
+        T v[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = lane == i ? T(1) : T(0);
+        // every lane takes the same decisions below: sums are reduced, then lane 0's broadcast
         f = (T)__shfl_sync(0xffffffffu, warp_sum(f), 0);
         __syncwarp();
         int sweep = 0;
@@ -311,65 +397,75 @@ __global__ void __launch_bounds__(ProjWarpCfg<T>::warps * 32)
             T off = T(0);
             for (int idx = lane; idx < N * N; idx += 32) {
                 const int i = idx / N, j = idx % N;
-                if (i != j) off += A[i * LD + j] * A[i * LD + j];
+                if (i < j) off += A[i * LD + j] * A[i * LD + j];
             }
-            off = (T)__shfl_sync(0xffffffffu, warp_sum(off), 0);
+            off = T(2) * (T)__shfl_sync(0xffffffffu, warp_sum(off), 0);
             if (!(off > symxg_dev::JacobiTol<T>::rel2() * f)) break;
-            for (int r = 0; r < N - 1; ++r) {
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                T c = T(1), s = T(0);
                 if (lane < NP) {
-                    const int a = lane == 0 ? r : (r + lane) % (N - 1);
-                    const int b = lane == 0 ? N - 1 : (r - lane + N - 1) % (N - 1);
-                    const int p = min(a, b), q = max(a, b);
-                    const T t = symxg_dev::jacobi_t(A[p * LD + p], A[q * LD + q], A[p * LD + q]);
-                    const T c = symxg_dev::inv_hypot1(t);
-                    sc[w][lane] = c;
-                    ss[w][lane] = t * c;
-                    sp[w][lane] = p;
-                    sq[w][lane] = q;
+                    int p, q;
+                    rr_pair<N>(r, lane, p, q);
+                    const T app = A[p * LD + p], aqq = A[q * LD + q], apq = A[p * LD + q];
+                    const T t = symxg_dev::jacobi_t(app, aqq, apq);
+                    c = symxg_dev::inv_hypot1(t);
+                    s = t * c;
+                    A[p * LD + p] = app - t * apq;
+                    A[q * LD + q] = aqq + t * apq;
+                    A[p * LD + q] = T(0);
                 }
-                __syncwarp();
-                for (int idx = lane; idx < NP * N; idx += 32) {  // rows p, q
-                    const int k = idx / N, j = idx % N, p = sp[w][k], q = sq[w][k];
-                    const T c = sc[w][k], sn = ss[w][k], apj = A[p * LD + j], aqj = A[q * LD + j];
-                    A[p * LD + j] = c * apj - sn * aqj;
-                    A[q * LD + j] = sn * apj + c * aqj;
+#pragma unroll
+                for (int j = 0; j < SLOTS; ++j) {
+                    const T ck = __shfl_sync(0xffffffffu, c, bk[j]), sk = __shfl_sync(0xffffffffu, s, bk[j]);
+                    const T cl = __shfl_sync(0xffffffffu, c, bl[j]), sl = __shfl_sync(0xffffffffu, s, bl[j]);
+                    if ((j + 1) * 32 <= NOFF || lane + 32 * j < NOFF) {
+                        const uint2 e = sTab[r][j][lane];
+                        const unsigned e00 = e.x & 0xffffu, e01 = e.x >> 16, e10 = e.y & 0xffffu, e11 = e.y >> 16;
+                        const T b00 = A[e00], b01 = A[e01], b10 = A[e10], b11 = A[e11];
+                        const T r00 = ck * b00 - sk * b10, r01 = ck * b01 - sk * b11;  // rows of pair k
+                        const T r10 = sk * b00 + ck * b10, r11 = sk * b01 + ck * b11;
+                        A[e00] = cl * r00 - sl * r01;  // columns of pair l
+                        A[e01] = sl * r00 + cl * r01;
+                        A[e10] = cl * r10 - sl * r11;
+                        A[e11] = sl * r10 + cl * r11;
+                    }
                 }
-                __syncwarp();
-                for (int idx = lane; idx < NP * N; idx += 32) {  // columns p, q
-                    const int k = idx / N, i = idx % N, p = sp[w][k], q = sq[w][k];
-                    const T c = sc[w][k], sn = ss[w][k], aip = A[i * LD + p], aiq = A[i * LD + q];
-                    A[i * LD + p] = c * aip - sn * aiq;
-                    A[i * LD + q] = sn * aip + c * aiq;
-                }
-                for (int idx = lane; idx < NP * N; idx += 32) {  // eigenvector columns p, q
-                    const int k = idx / N, i = idx % N, p = sp[w][k], q = sq[w][k];
-                    const T c = sc[w][k], sn = ss[w][k], vip = V[i * LD + p], viq = V[i * LD + q];
-                    V[i * LD + p] = c * vip - sn * viq;
-                    V[i * LD + q] = sn * vip + c * viq;
+#pragma unroll
+                for (int k = 0; k < NP; ++k) {
+                    int p, q;
+                    rr_pair<N>(r, k, p, q);
+                    const T ck = __shfl_sync(0xffffffffu, c, k), sk = __shfl_sync(0xffffffffu, s, k);
+                    const T vp = v[p], vq = v[q];
+                    v[p] = ck * vp - sk * vq;
+                    v[q] = sk * vp + ck * vq;
                 }
                 __syncwarp();
             }
         }
         if (sweep == max_sweeps) nc = 1;
+        T lam = T(0);
         bool mine = false;
         if (lane < N) {
-            T l = A[lane * LD + lane];
-            if (l < eps) {
+            lam = A[lane * LD + lane];
+            if (lam < eps) {
                 mine = true;
-                l = mirroring ? -l : eps;
+                lam = mirroring ? -lam : eps;
             }
-            sl[w][lane] = l;
         }
         const bool changed = __any_sync(0xffffffffu, mine);
-        __syncwarp();
         if (changed) {
-            for (int idx = lane; idx < N * N; idx += 32) {
-                const int blk = idx / 9, r = idx % 9;
-                const int i = (blk / nb) * 3 + r / 3, j = (blk % nb) * 3 + r % 3;
-                T acc = T(0);
-#pragma unroll 4
-                for (int k = 0; k < N; ++k) acc += V[i * LD + k] * sl[w][k] * V[j * LD + k];
-                h[idx] = acc;
+            __syncwarp();  // eigenvalues read before V overwrites A
+            if (lane < N) {
+#pragma unroll
+                for (int k = 0; k < N; ++k) A[lane * N + k] = v[k];
+            }
+#pragma unroll
+            for (int k = 0; k < N; ++k) v[k] *= __shfl_sync(0xffffffffu, lam, k);  // row i of V diag(lambda)
+            __syncwarp();
+            if (lane < N) {
+                const int i = lane, bi = (i / 3) * nb, ri = (i % 3) * 3;
+                for (int j = 0; j < N; ++j) h[(bi + j / 3) * 9 + ri + j % 3] = row_dot<N>(v, A + j * N);
             }
         }
         __syncwarp();  // the next matrix reuses this warp's shared memory
@@ -1468,8 +1564,11 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
         case 9: k_project_pd_unrolled<T, 9><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
         case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
         case 24: {
-            constexpr int W = ProjWarpCfg<T>::warps;
-            k_project_pd_warp<T, 24><<<blocks_for(count, W), W * 32, 0, s>>>(H, count, eps, mirroring, not_converged);
+            constexpr int threads = ProjPairsCfg<T>::warps * 32;
+            static const unsigned grid = resident_grid(k_project_pd_pairs<T, 24>, threads);
+            const unsigned need = blocks_for(count, ProjPairsCfg<T>::warps);
+            k_project_pd_pairs<T, 24><<<need < grid ? need : grid, threads, 0, s>>>(H, count, eps, mirroring,
+                                                                                   not_converged);
             break;
         }
         default:

@@ -1190,7 +1190,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             timer.start("project_to_PD");
             for (auto& cp : I.pots) {
                 cudaEvent_t a = nullptr, b = nullptr;
-                const bool timed = S.time_kernels && cp.nb * 3 == 12;
+                const bool timed = S.time_kernels;
                 if (timed) {
                     cudaEventCreate(&a);
                     cudaEventCreate(&b);
@@ -1200,7 +1200,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
                                             S.project_to_pd_use_mirroring, I.flags.p, s, I.proj_scratch());
                 if (timed) {
                     cudaEventRecord(b, s);
-                    pending_kernel_events.push_back({std::string("project_pd_12_") + (sizeof(T) == 4 ? "f32" : "f64"), a, b});
+                    pending_kernel_events.push_back({"project_pd_" + std::to_string(3 * cp.nb) + (sizeof(T) == 4 ? "_f32" : "_f64"), a, b});
                 }
             }
             timer.stop();
