@@ -149,6 +149,9 @@ CONFIGS = {
     "tet4_6p": dict(kind="tet4", cells=(6, 5, 4), h=0.01, perturb=0.05, seed=11),
     "hex8_3": dict(kind="hex8", cells=(3, 3, 2), h=0.01, perturb=0.0, seed=12,
                    youngs_lognormal_sigma=0.5),
+    # Smaller Hex8 slab (65,536 elements) for kernel profiles.
+    "hex8_64x64x16": dict(kind="hex8", cells=(64, 64, 16), h=0.01, perturb=0.0, seed=5,
+                          youngs_lognormal_sigma=0.5),
     "tet4_32": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.0, seed=3),
     "tet4_40": dict(kind="tet4", cells=(40, 40, 40), h=0.01, perturb=0.0, seed=4),
 }
