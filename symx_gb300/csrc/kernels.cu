@@ -269,33 +269,43 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
 // pairs, and one round applies all N / 2 rotations at once, A <- J^T A J with J block diagonal
 // over the pairs.  Written per 2 x 2 block of pairs (k, l) this is B_kl <- R_k^T B_kl R_l, so
 //   * lane k < N / 2 forms pair k's rotation from its diagonal block (same formula and
-//     convergence test as the register kernels) and updates that block in place;
+//     convergence test as the register kernels), updates that block in place and publishes
+//     (c, s) in shared memory;
 //   * the N/2 (N/2 - 1) / 2 off-diagonal blocks of the upper triangle are spread over the
 //     lanes; each lane reads its four entries, applies both rotations and writes them back,
 //     with the entry offsets of every round taken from a per-block table in shared memory;
-//   * lane i keeps row i of the eigenvector matrix V in registers (the rounds are unrolled,
-//     so the column pairs are compile-time indices) and rotates it with the round's (c, s)
-//     taken from the owning lanes by shuffles.
+//   * lane i keeps row i of the eigenvector matrix V in registers, its columns held in "slot"
+//     order: in every round pair k occupies slots (2k, 2k + 1), and the round-robin step from
+//     one round to the next is a fixed permutation of the slots (a rotation of the N - 1
+//     moving ones), so the round loop stays rolled (the kernel fits the instruction cache)
+//     while every register index is a compile-time constant.  After N - 1 rounds the slots
+//     are back in their initial order, slot_index() below.
 // Only the upper triangle of A in shared memory is kept up to date.  No two lanes touch the
-// same entry within a round, so one __syncwarp per round suffices.
+// same entry within a round.
 template <typename T>
 struct ProjPairsCfg {
     static constexpr int warps = sizeof(T) == 4 ? 8 : 4;
+    static constexpr int min_blocks = 4;  // float: 64 registers, 32 warps per SM
 };
 
-// Pair k of round r (position N - 1 is fixed, the others rotate), as (p, q) with p < q.
+// Pair k of round r as (a, b): position N - 1 is fixed, the others rotate.
 template <int N>
-__host__ __device__ __forceinline__ void rr_pair(int r, int k, int& p, int& q)
+__host__ __device__ __forceinline__ void rr_pair(int r, int k, int& a, int& b)
 {
-    int a = r, b = N - 1;
+    a = r + k;
+    if (a >= N - 1) a -= N - 1;
+    b = N - 1;
     if (k != 0) {
-        a = r + k;
-        if (a >= N - 1) a -= N - 1;
         b = r - k + N - 1;
         if (b >= N - 1) b -= N - 1;
     }
-    p = a < b ? a : b;
-    q = a < b ? b : a;
+}
+
+// Index held by V slot s at the start of every sweep: pair k of round 0 is (k, N - 1 - k).
+template <int N>
+__host__ __device__ constexpr int slot_index(int s)
+{
+    return (s & 1) ? N - 1 - s / 2 : s / 2;
 }
 
 // Off-diagonal block b of the upper triangle over pairs, as (k, l), k < l (row-major order).
@@ -314,6 +324,17 @@ __device__ __forceinline__ void off_block(int b, int& k, int& l)
         b -= n;
     }
 }
+
+template <typename T>
+struct Pair2;
+template <>
+struct Pair2<float> {
+    using type = float2;
+};
+template <>
+struct Pair2<double> {
+    using type = double2;
+};
 
 // sum_k w[k] * row[k] with 16-byte shared-memory loads (row 16-byte aligned)
 template <int N>
@@ -344,27 +365,29 @@ __device__ __forceinline__ double row_dot(const double (&w)[N], const double* ro
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32)
+__global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::min_blocks)
     k_project_pd_pairs(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged)
 {
     static_assert(N % 6 == 0 && N <= 32, "N a multiple of 6 up to 30 (3 x 3 blocks, pairs, 16-byte rows)");
+    using T2 = typename Pair2<T>::type;
     constexpr int W = ProjPairsCfg<T>::warps;
     constexpr int LD = N + 1, NP = N / 2, NR = N - 1, NOFF = NP * (NP - 1) / 2, SLOTS = (NOFF + 31) / 32, nb = N / 3;
     __shared__ __align__(16) T sA[W][N * LD];
-    __shared__ uint2 sTab[NR][SLOTS][32];  // per round, slot and lane: 4 x 16-bit entry offsets
+    __shared__ __align__(16) T2 sCS[W][NP];  // (c, s) of the round's rotations
+    __shared__ uint2 sTab[NR][SLOTS][32];     // per round, slot and lane: 4 x 16-bit entry offsets
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     for (int e = threadIdx.x; e < NR * SLOTS * 32; e += blockDim.x) {
         const int r = e / (SLOTS * 32), j = (e / 32) % SLOTS, ln = e % 32, b = ln + 32 * j;
         uint2 v = make_uint2(0u, 0u);
         if (b < NOFF) {
-            int k, l, pk, qk, pl, ql;
+            int k, l, ak, bk, al, bl;
             off_block<NP>(b, k, l);
-            rr_pair<N>(r, k, pk, qk);
-            rr_pair<N>(r, l, pl, ql);
+            rr_pair<N>(r, k, ak, bk);
+            rr_pair<N>(r, l, al, bl);
             auto up = [](int i, int jj) { return (unsigned)(i < jj ? i * LD + jj : jj * LD + i); };
-            v.x = up(pk, pl) | (up(pk, ql) << 16);
-            v.y = up(qk, pl) | (up(qk, ql) << 16);
+            v.x = up(ak, al) | (up(ak, bl) << 16);
+            v.y = up(bk, al) | (up(bk, bl) << 16);
         }
         sTab[r][j][ln] = v;
     }
@@ -374,6 +397,7 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32)
     __syncthreads();
 
     T* A = sA[w];
+    T2* CS = sCS[w];
     int nc = 0;
     constexpr int max_sweeps = 2 * symxg_dev::JacobiTol<T>::max_double_sweeps;
     for (int64_t m = (int64_t)blockIdx.x * W + w; m < count; m += (int64_t)gridDim.x * W) {
@@ -388,7 +412,7 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32)
         }
         T v[N];
 #pragma unroll
-        for (int i = 0; i < N; ++i) v[i] = lane == i ? T(1) : T(0);
+        for (int s = 0; s < N; ++s) v[s] = lane == slot_index<N>(s) ? T(1) : T(0);
         // every lane takes the same decisions below: sums are reduced, then lane 0's broadcast
         f = (T)__shfl_sync(0xffffffffu, warp_sum(f), 0);
         __syncwarp();
@@ -401,45 +425,55 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32)
             }
             off = T(2) * (T)__shfl_sync(0xffffffffu, warp_sum(off), 0);
             if (!(off > symxg_dev::JacobiTol<T>::rel2() * f)) break;
-#pragma unroll
+#pragma unroll 1
             for (int r = 0; r < NR; ++r) {
-                T c = T(1), s = T(0);
                 if (lane < NP) {
                     int p, q;
                     rr_pair<N>(r, lane, p, q);
-                    const T app = A[p * LD + p], aqq = A[q * LD + q], apq = A[p * LD + q];
+                    const int pq = p < q ? p * LD + q : q * LD + p;
+                    const T app = A[p * LD + p], aqq = A[q * LD + q], apq = A[pq];
                     const T t = symxg_dev::jacobi_t(app, aqq, apq);
-                    c = symxg_dev::inv_hypot1(t);
-                    s = t * c;
+                    const T c = symxg_dev::inv_hypot1(t);
                     A[p * LD + p] = app - t * apq;
                     A[q * LD + q] = aqq + t * apq;
-                    A[p * LD + q] = T(0);
+                    A[pq] = T(0);
+                    T2 cs;
+                    cs.x = c;
+                    cs.y = t * c;
+                    CS[lane] = cs;
                 }
+                __syncwarp();
 #pragma unroll
                 for (int j = 0; j < SLOTS; ++j) {
-                    const T ck = __shfl_sync(0xffffffffu, c, bk[j]), sk = __shfl_sync(0xffffffffu, s, bk[j]);
-                    const T cl = __shfl_sync(0xffffffffu, c, bl[j]), sl = __shfl_sync(0xffffffffu, s, bl[j]);
                     if ((j + 1) * 32 <= NOFF || lane + 32 * j < NOFF) {
                         const uint2 e = sTab[r][j][lane];
+                        const T2 rk = CS[bk[j]], rl = CS[bl[j]];
                         const unsigned e00 = e.x & 0xffffu, e01 = e.x >> 16, e10 = e.y & 0xffffu, e11 = e.y >> 16;
                         const T b00 = A[e00], b01 = A[e01], b10 = A[e10], b11 = A[e11];
-                        const T r00 = ck * b00 - sk * b10, r01 = ck * b01 - sk * b11;  // rows of pair k
-                        const T r10 = sk * b00 + ck * b10, r11 = sk * b01 + ck * b11;
-                        A[e00] = cl * r00 - sl * r01;  // columns of pair l
-                        A[e01] = sl * r00 + cl * r01;
-                        A[e10] = cl * r10 - sl * r11;
-                        A[e11] = sl * r10 + cl * r11;
+                        const T r00 = rk.x * b00 - rk.y * b10, r01 = rk.x * b01 - rk.y * b11;  // rows of pair k
+                        const T r10 = rk.y * b00 + rk.x * b10, r11 = rk.y * b01 + rk.x * b11;
+                        A[e00] = rl.x * r00 - rl.y * r01;  // columns of pair l
+                        A[e01] = rl.y * r00 + rl.x * r01;
+                        A[e10] = rl.x * r10 - rl.y * r11;
+                        A[e11] = rl.y * r10 + rl.x * r11;
                     }
                 }
 #pragma unroll
-                for (int k = 0; k < NP; ++k) {
-                    int p, q;
-                    rr_pair<N>(r, k, p, q);
-                    const T ck = __shfl_sync(0xffffffffu, c, k), sk = __shfl_sync(0xffffffffu, s, k);
-                    const T vp = v[p], vq = v[q];
-                    v[p] = ck * vp - sk * vq;
-                    v[q] = sk * vp + ck * vq;
+                for (int k = 0; k < NP; ++k) {  // eigenvector columns: pair k in slots (2k, 2k + 1)
+                    const T2 cs = CS[k];
+                    const T vp = v[2 * k], vq = v[2 * k + 1];
+                    v[2 * k] = cs.x * vp - cs.y * vq;
+                    v[2 * k + 1] = cs.y * vp + cs.x * vq;
                 }
+                // next round's slot order: new[2k] = old[2k + 2], new[N - 2] = old[N - 1],
+                // new[3] = old[0], new[2k + 1] = old[2k - 1] (k >= 2), slot 1 fixed
+                const T v0 = v[0];
+#pragma unroll
+                for (int k = 0; k < NP - 1; ++k) v[2 * k] = v[2 * k + 2];
+                v[N - 2] = v[N - 1];
+#pragma unroll
+                for (int k = NP - 1; k >= 2; --k) v[2 * k + 1] = v[2 * k - 1];
+                v[3] = v0;
                 __syncwarp();
             }
         }
@@ -458,10 +492,10 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32)
             __syncwarp();  // eigenvalues read before V overwrites A
             if (lane < N) {
 #pragma unroll
-                for (int k = 0; k < N; ++k) A[lane * N + k] = v[k];
+                for (int s = 0; s < N; ++s) A[lane * N + s] = v[s];
             }
 #pragma unroll
-            for (int k = 0; k < N; ++k) v[k] *= __shfl_sync(0xffffffffu, lam, k);  // row i of V diag(lambda)
+            for (int s = 0; s < N; ++s) v[s] *= __shfl_sync(0xffffffffu, lam, slot_index<N>(s));  // V diag(lambda)
             __syncwarp();
             if (lane < N) {
                 const int i = lane, bi = (i / 3) * nb, ri = (i % 3) * 3;
