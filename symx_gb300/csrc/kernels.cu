@@ -1001,15 +1001,26 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
     if (warp == 0) {
         if (lane == 0) {
             const unsigned last = seq + n_stages + (run_ahead ? NS : 0);  // one past the last stage to copy now
+            // block range of stage g, loaded one stage ahead so that the load overlaps the
+            // wait for the ring slot
+            auto range = [&](unsigned g, int& kb, int& ke) {
+                const int r0 = row_begin + (int)(g % (unsigned)n_stages) * S;
+                kb = B.staged.row_ptr_ext[r0];
+                ke = B.staged.row_ptr_ext[r0 + S];
+            };
+            int next_kb = 0, next_ke = 0;
+            if (issued < last) range(issued, next_kb, next_ke);
             for (unsigned g = issued; g < last && !*abort_flag; ++g) {
                 const unsigned s = g % NS, use = g / NS;
                 const int j = (int)(g % (unsigned)n_stages);
+                const int kb = next_kb, ke = next_ke;
+                if (g + 1 < last) range(g + 1, next_kb, next_ke);
                 if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1)) {
                     *abort_flag = 1;
                     break;
                 }
                 const int r0 = row_begin + j * S;
-                const int kb4 = B.staged.row_ptr_ext[r0] & ~3, ke4 = (B.staged.row_ptr_ext[r0 + S] + 3) & ~3;
+                const int kb4 = kb & ~3, ke4 = (ke + 3) & ~3;
                 const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
                 unsigned char* st = ss.stage0 + s * stage_bytes;
                 const uint32_t fb = smem_addr(&ss.full[s]);
@@ -1045,12 +1056,37 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
             const int rowA = r0 + la, rowB = r0 + lb;
             const bool vA = rowA < row_end, vB = rowB < row_end;
             float a[3], b[3];
-            two_range_products<float>(vA ? rp[la] - kb4 : 0, vA ? rp[la + 1] - kb4 : 0, vB ? rp[lb] - kb4 : 0,
-                                      vB ? rp[lb + 1] - kb4 : 0, lane16,
-                                      reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4),
-                                      reinterpret_cast<const float*>(st), StridedBcsr{CAP}, pv, a, b);
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+            const int kbA = vA ? rp[la] - kb4 : 0, keA = vA ? rp[la + 1] - kb4 : 0;
+            const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
+            const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
+            const float* __restrict__ svals = reinterpret_cast<const float*>(st);
+            if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
+                // rows of at most 16 blocks: each lane takes at most one block of each row into
+                // registers and the stage is released before the gathers, so the ring slot is
+                // refilled while this warp waits on L2
+                const int kA = kbA + lane16, kB = kbB + lane16;
+                const bool hA = kA < keA, hB = kB < keB;
+                const int cA = hA ? scols[kA] : 0, cB = hB ? scols[kB] : 0;
+                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
+                float mA[9], mB[9];
+#pragma unroll
+                for (int m = 0; m < 9; ++m) {
+                    mA[m] = hA ? svals[m * CAP + kA] : 0.0f;
+                    mB[m] = hB ? svals[m * CAP + kB] : 0.0f;
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
+                a[1] = mA[3] * xA.x + mA[4] * xA.y + mA[5] * xA.z;
+                a[2] = mA[6] * xA.x + mA[7] * xA.y + mA[8] * xA.z;
+                b[0] = mB[0] * xB.x + mB[1] * xB.y + mB[2] * xB.z;
+                b[1] = mB[3] * xB.x + mB[4] * xB.y + mB[5] * xB.z;
+                b[2] = mB[6] * xB.x + mB[7] * xB.y + mB[8] * xB.z;
+            } else {
+                two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, pv, a, b);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+            }
             const float qd = half_warp_transpose_sum<float>(a, b, lane16);
             const int idx = lane16 >> 1;  // 0..2 row A, 3..5 row B
             if (!(lane16 & 1) && idx < 6) {
@@ -1058,7 +1094,8 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
                 if (idx < 3 ? vA : vB) {
                     const int64_t o = 4 * (int64_t)row + d;
                     const float zo = kCg ? __ldcg(z + o) : z[o];
-                    const float pd = first ? zo : fmaf(beta, kCg ? __ldcg(p_old + o) : p_old[o], zo);  // direction()'s bits
+                    const float po = first ? 0.0f : (kCg ? __ldcg(p_old + o) : p_old[o]);
+                    const float pd = first ? zo : fmaf(beta, po, zo);  // direction()'s bits
                     p_new[o] = pd;
                     B.q[o] = qd;
                     pq.add_prod(pd, qd);
@@ -1301,42 +1338,30 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         alpha = rz / pAp;
         const float a = (float)alpha;
         DotAcc<float> rra, rza;
-        // two rows per thread and pass, all loads of both issued before either row's math
-        for (int i = row_begin + (int)threadIdx.x; i < row_end; i += 2 * blockDim.x) {
-            const int j = i + blockDim.x;
-            const bool has_j = j < row_end;
-            Row4<float> xs[2], rs[2], ps[2], qs[2];
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                if (k == 1 && !has_j) break;
-                const int row = k ? j : i;
-                xs[k] = ld4(B.x + 4 * row);
-                rs[k] = ld4(B.r + 4 * row);
-                ps[k] = ld4(p_new + 4 * row);
-                qs[k] = ld4(B.q + 4 * row);
-            }
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                if (k == 1 && !has_j) break;
-                const int row = k ? j : i;
-                Row4<float> x = xs[k], r = rs[k];
-                x.x = fmaf(a, ps[k].x, x.x);
-                x.y = fmaf(a, ps[k].y, x.y);
-                x.z = fmaf(a, ps[k].z, x.z);
-                r.x = fmaf(-a, qs[k].x, r.x);
-                r.y = fmaf(-a, qs[k].y, r.y);
-                r.z = fmaf(-a, qs[k].z, r.z);
-                const Row4<float> z = apply_block_jacobi(B.Dinv, row, r);
-                st4(B.x + 4 * row, x);
-                st4(B.r + 4 * row, r);
-                st4(B.z + 4 * row, z);
-                rra.add_prod(r.x, r.x);
-                rra.add_prod(r.y, r.y);
-                rra.add_prod(r.z, r.z);
-                rza.add_prod(r.x, z.x);
-                rza.add_prod(r.y, z.y);
-                rza.add_prod(r.z, z.z);
-            }
+        // one row per thread and pass, all its loads (preconditioner block included) issued
+        // before its math
+        for (int i = row_begin + (int)threadIdx.x; i < row_end; i += blockDim.x) {
+            Row4<float> x = ld4(B.x + 4 * i), r = ld4(B.r + 4 * i);
+            const Row4<float> pp = ld4(p_new + 4 * i), q = ld4(B.q + 4 * i);
+            const Row4<float> m0 = ld4(B.Dinv + 12 * (int64_t)i), m1 = ld4(B.Dinv + 12 * (int64_t)i + 4),
+                              m2 = ld4(B.Dinv + 12 * (int64_t)i + 8);
+            x.x = fmaf(a, pp.x, x.x);
+            x.y = fmaf(a, pp.y, x.y);
+            x.z = fmaf(a, pp.z, x.z);
+            r.x = fmaf(-a, q.x, r.x);
+            r.y = fmaf(-a, q.y, r.y);
+            r.z = fmaf(-a, q.z, r.z);
+            const Row4<float> z{m0.x * r.x + m0.y * r.y + m0.z * r.z, m1.x * r.x + m1.y * r.y + m1.z * r.z,
+                                m2.x * r.x + m2.y * r.y + m2.z * r.z, 0.0f};
+            st4(B.x + 4 * i, x);
+            st4(B.r + 4 * i, r);
+            st4(B.z + 4 * i, z);
+            rra.add_prod(r.x, r.x);
+            rra.add_prod(r.y, r.y);
+            rra.add_prod(r.z, r.z);
+            rza.add_prod(r.x, z.x);
+            rza.add_prod(r.y, z.y);
+            rza.add_prod(r.z, z.z);
         }
         const double brr = rra.block_sum(sh);
         const double brz = rza.block_sum(sh);
