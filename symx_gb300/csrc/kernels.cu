@@ -140,10 +140,11 @@ __global__ void k_dot_mixed(const T* __restrict__ a, const double* __restrict__ 
 // ---------------------------------------------------------------- projection
 template <typename T, int N>
 __global__ void __launch_bounds__(128) k_project_pd_unrolled(T* __restrict__ H, int64_t count, T eps, int mirroring,
-                                                             int* not_converged)
+                                                             int* not_converged, const int64_t* __restrict__ sel)
 {
-    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= count) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t m = sel ? sel[k] : k;
     int nc = 0;
     T* h = H + m * (N * N);
     // Tet4-sized matrices of translation-invariant energies: 9 x 9 decomposition (the
@@ -167,10 +168,12 @@ __global__ void __launch_bounds__(128) k_project_pd_unrolled(T* __restrict__ H, 
 template <typename T, int N>
 __global__ void __launch_bounds__(128) k_project_pd_deflated(T* __restrict__ H, int64_t count, T eps, int mirroring,
                                                              int* not_converged, int64_t* __restrict__ fallback,
-                                                             unsigned long long* n_fallback)
+                                                             unsigned long long* n_fallback,
+                                                             const int64_t* __restrict__ sel)
 {
-    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= count) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t m = sel ? sel[k] : k;
     int nc = 0;
     if (symxg_dev::project_pd_deflated<T, N / 3>(H + m * (N * N), eps, mirroring != 0, &nc) < 0)
         fallback[atomicAdd(n_fallback, 1ull)] = m;
@@ -195,14 +198,50 @@ __global__ void __launch_bounds__(128) k_project_pd_listed(T* __restrict__ H, co
     if (nc) *not_converged = 1;
 }
 
+// Progressive projection (NewtonsMethod.cpp:305-329): flag the element gradient blocks of
+// every DoF block whose gradient max-abs is at least thr (gflag zeroed before); counts the
+// other blocks in *n_inactive.
+__global__ void k_ppn_mark_blocks(int n_blocks, const double* __restrict__ grad, double thr,
+                                  const int64_t* __restrict__ gptr, const int32_t* __restrict__ gcontrib,
+                                  uint8_t* __restrict__ gflag, unsigned long long* n_inactive)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_blocks) return;
+    const double m = fmax(fabs(grad[3 * v]), fmax(fabs(grad[3 * v + 1]), fabs(grad[3 * v + 2])));
+    if (!(m >= thr)) {
+        atomicAdd(n_inactive, 1ull);
+        return;
+    }
+    for (int64_t c = gptr[v]; c < gptr[v + 1]; ++c) gflag[gcontrib[c]] = 1;
+}
+
+// Elements of one potential not projected yet in this evaluation and touching a flagged
+// gradient block (every unprojected one when gflag is null), as
+// ElementHessians::_project_to_PD_for_update selects them (ElementHessians.cpp:104-131): marked
+// projected and appended to sel (count in *n_sel).  The list order varies from run to run;
+// each element's projection does not depend on it.
+__global__ void k_select_elements(int64_t n_el, int nb, const uint8_t* __restrict__ gflag, uint8_t* __restrict__ is_proj,
+                                  int64_t* __restrict__ sel, unsigned long long* n_sel)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_el || is_proj[e]) return;
+    bool take = gflag == nullptr;
+    for (int a = 0; a < nb && !take; ++a) take = gflag[e * nb + a] != 0;
+    if (!take) return;
+    is_proj[e] = 1;
+    sel[atomicAdd(n_sel, 1ull)] = e;
+}
+
 // Generic N (up to 24) with thread-private arrays; used for large element matrices.
 template <typename T>
 __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, int N, int64_t count, T eps,
-                                                           int mirroring, int* not_converged)
+                                                           int mirroring, int* not_converged,
+                                                           const int64_t* __restrict__ sel)
 {
     constexpr int NMAX = 24;
-    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= count) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t m = sel ? sel[k] : k;
     T* h = H + m * (int64_t)N * N;
     const int nb = N / 3;
     auto bm = [nb](int i, int j) { return (((i / 3) * nb + (j / 3)) * 3 + (i % 3)) * 3 + (j % 3); };
@@ -366,7 +405,8 @@ __device__ __forceinline__ double row_dot(const double (&w)[N], const double* ro
 
 template <typename T, int N>
 __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::min_blocks)
-    k_project_pd_pairs(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged)
+    k_project_pd_pairs(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged,
+                       const int64_t* __restrict__ sel)
 {
     static_assert(N % 6 == 0 && N <= 32, "N a multiple of 6 up to 30 (3 x 3 blocks, pairs, 16-byte rows)");
     using T2 = typename Pair2<T>::type;
@@ -400,8 +440,8 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
     T2* CS = sCS[w];
     int nc = 0;
     constexpr int max_sweeps = 2 * symxg_dev::JacobiTol<T>::max_double_sweeps;
-    for (int64_t m = (int64_t)blockIdx.x * W + w; m < count; m += (int64_t)gridDim.x * W) {
-        T* h = H + m * (int64_t)(N * N);
+    for (int64_t item = (int64_t)blockIdx.x * W + w; item < count; item += (int64_t)gridDim.x * W) {
+        T* h = H + (sel ? sel[item] : item) * (int64_t)(N * N);
         T f = T(0);
         for (int idx = lane; idx < N * N; idx += 32) {  // block-major storage, read in order
             const int blk = idx / 9, r = idx % 9;
@@ -943,6 +983,23 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uin
                  "l"(src), "r"(bytes), "r"(bar)
                  : "memory");
 }
+// L2 policy for data read once per pass (the matrix values and columns): its lines are the
+// first to go, so the PCG vectors the pass gathers and the update phase rewrites stay in L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy()
+{
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ void bulk_copy_g2s_stream(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar,
+                                                     uint64_t pol)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar), "l"(pol)
+        : "memory");
+}
 
 // Bytes of one shared-memory stage: nine value slots and one column slot of `cap` entries,
 // then stage_rows + 4 row_ptr entries, rounded to 128.
@@ -952,10 +1009,19 @@ __host__ __device__ __forceinline__ size_t staged_stage_bytes(int cap, int stage
 }
 
 // Shared-memory layout of a staged block: full barriers, empty barriers (kStagedMaxStages
-// each), then the ring of stages.
+// each), the chunk held by each ring slot, the per-chunk partial sums of the consumer warps
+// (kStagedPartSlots chunks in flight at most, with a count of the warps that stored theirs),
+// then the ring of stages.  The chunk slots and partials are used by the persistent kernel.
+constexpr int kStagedPartSlots = 2 * kStagedMaxStages;
+constexpr size_t kStagedHeaderBytes =
+    (16 * kStagedMaxStages + 4 * kStagedMaxStages + 4 * kStagedPartSlots +
+     8 * kStagedPartSlots * kStagedConsumerWarps + 127) / 128 * 128;
 struct StagedShared {
     uint64_t* full;
     uint64_t* empty;
+    int* chunk;        // [kStagedMaxStages] chunk index of the stage in each slot, -1: end of a pass
+    unsigned* wcount;  // [kStagedPartSlots] consumer warps that stored their partial
+    float2* wpart;     // [kStagedPartSlots][kStagedConsumerWarps] float-float warp partials
     unsigned char* stage0;
 };
 __device__ __forceinline__ StagedShared staged_shared(unsigned char* smem)
@@ -963,11 +1029,15 @@ __device__ __forceinline__ StagedShared staged_shared(unsigned char* smem)
     StagedShared ss;
     ss.full = reinterpret_cast<uint64_t*>(smem);
     ss.empty = ss.full + kStagedMaxStages;
-    ss.stage0 = smem + 16 * kStagedMaxStages;
+    ss.chunk = reinterpret_cast<int*>(smem + 16 * kStagedMaxStages);
+    ss.wcount = reinterpret_cast<unsigned*>(smem + 20 * kStagedMaxStages);
+    ss.wpart = reinterpret_cast<float2*>(smem + 20 * kStagedMaxStages + 4 * kStagedPartSlots);
+    ss.stage0 = smem + kStagedHeaderBytes;
     return ss;
 }
 __device__ __forceinline__ void staged_init_barriers(const StagedShared& ss, int stages)
 {
+    if (threadIdx.x < kStagedPartSlots) ss.wcount[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         for (int s = 0; s < stages; ++s) {
             mbar_init(smem_addr(&ss.full[s]), 1);
@@ -1008,6 +1078,7 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
                 kb = B.staged.row_ptr_ext[r0];
                 ke = B.staged.row_ptr_ext[r0 + S];
             };
+            const uint64_t pol = l2_evict_first_policy();
             int next_kb = 0, next_ke = 0;
             if (issued < last) range(issued, next_kb, next_ke);
             for (unsigned g = issued; g < last && !*abort_flag; ++g) {
@@ -1027,8 +1098,9 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
                 mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
                 if (span) {
                     for (int m = 0; m < 9; ++m)
-                        bulk_copy_g2s(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4, span, fb);
-                    bulk_copy_g2s(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb);
+                        bulk_copy_g2s_stream(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4,
+                                             span, fb, pol);
+                    bulk_copy_g2s_stream(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb, pol);
                 }
                 bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0, (uint32_t)(S + 4) * 4u, fb);
                 issued = g + 1;
@@ -1116,6 +1188,329 @@ __device__ __forceinline__ void staged_drain(const PcgBuffers<float>& B, const S
     const unsigned NS = (unsigned)B.staged.stages;
     for (unsigned g = issued > NS ? issued - NS : 0; g < issued; ++g)
         mbar_wait(smem_addr(&ss.full[g % NS]), (g / NS) & 1);
+}
+
+// ---- dynamic schedule of the persistent kernel's product pass
+// The rows are cut into chunks of stage_rows rows (one stage each).  In every pass the
+// blocks claim chunks, kClaimChunks at a time, from a counter of that pass (atomicAdd; a
+// value past the last chunk ends the block's pass), so a block on a slower SM simply takes
+// fewer chunks and all blocks reach the grid barrier together.  The producer thread issues
+// the claim of its next unit when it starts the first stage of the current one, so the
+// claim's round trip, and the load of the next unit's row range after it, overlap the waits
+// for ring slots.  After the end marker of pass li it runs on into pass li + 1 until the
+// ring is full; it never claims from a pass beyond li + 1.  Three counters rotate (pass k
+// uses ctr[k % 3]); ctr[(li + 2) % 3] is cleared by block 0 between the two grid barriers of
+// pass li, when no block can still claim from pass li - 1 and none can claim from pass
+// li + 2 yet.
+//
+// p.q stays bitwise reproducible: each consumer warp sums its products of a chunk in a fixed
+// shuffle tree, the last of the 15 warps to finish a chunk adds the warp sums in warp order
+// and stores the chunk's float-float sum at part[chunk], and after the barrier every block
+// adds part[0 .. n_chunks) in one fixed order.  None of it depends on which block took which
+// chunk.
+constexpr int kClaimChunks = 2;
+struct DynProducer {
+    int it = 0;         // pass of the next stage to issue
+    int c = -1;         // its chunk, or -1: the end marker of pass `it`
+    int unit0 = 0;      // first chunk of the claimed unit holding c, and one past its last
+    int unit_end = 0;
+    int rp[kClaimChunks + 1];  // row_ptr at the unit's chunk boundaries
+    bool have = false;  // false: nothing claimed yet for pass `it`
+    bool pending = false;   // a claim for the unit after this one is in flight
+    int next_it = 0;
+    unsigned next_v = 0;
+    int end_it = -1;    // pass of the last end marker issued, and the stage numbers of the
+    unsigned end_g = 0, end_g_prev = 0;  // last two end markers
+};
+
+// Take the claim value v of pass `it` as the current unit (loads its row range).
+__device__ __forceinline__ void dyn_take(const PcgBuffers<float>& B, int n_chunks, int it, unsigned v, DynProducer& P)
+{
+    P.it = it;
+    P.have = true;
+    if (v >= (unsigned)n_chunks) {
+        P.c = -1;
+        return;
+    }
+    P.c = P.unit0 = (int)v;
+    P.unit_end = min((int)v + kClaimChunks, n_chunks);
+    const int S = B.staged.stage_rows;
+#pragma unroll
+    for (int k = 0; k <= kClaimChunks; ++k)
+        if (P.unit0 + k <= P.unit_end) P.rp[k] = __ldcg(B.staged.row_ptr_ext + (P.unit0 + k) * S);
+}
+
+__device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B, const StagedShared& ss, int li,
+                                                     unsigned* ctr, int n_chunks, const float* __restrict__ p_old,
+                                                     float* __restrict__ p_new, bool first, float beta, unsigned& seq,
+                                                     unsigned& issued, DynProducer& P, volatile int* abort_flag,
+                                                     float2* __restrict__ part)
+{
+    const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
+    const size_t stage_bytes = staged_stage_bytes(CAP, S);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint64_t pol = l2_evict_first_policy();
+            while (!*abort_flag) {
+                // once the end marker of pass li is out (in this pass or, running ahead, in the
+                // previous one), stop when every ring slot that pass li's consumers free is taken
+                if (P.end_it >= li) {
+                    const unsigned e = P.end_it == li ? P.end_g : P.end_g_prev;
+                    if (issued > e + (unsigned)NS) break;
+                }
+                if (!P.have) {  // nothing claimed ahead (launch start, or after a stop)
+                    if (P.it > li + 1) break;
+                    dyn_take(B, n_chunks, P.it, atomicAdd(&ctr[P.it % 3], (unsigned)kClaimChunks), P);
+                }
+                // claim the unit after this one now: its round trip overlaps the slot waits
+                if (!P.pending && (P.c < 0 || P.c == P.unit0)) {
+                    const int nit = P.c < 0 ? P.it + 1 : P.it;
+                    if (nit <= li + 1) {
+                        P.next_it = nit;
+                        P.next_v = atomicAdd(&ctr[nit % 3], (unsigned)kClaimChunks);
+                        P.pending = true;
+                    }
+                }
+                const unsigned g = issued, s = g % NS, use = g / NS;
+                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                ss.chunk[s] = P.c;  // published to the consumers by the arrive's release
+                const uint32_t fb = smem_addr(&ss.full[s]);
+                if (P.c >= 0) {
+                    const int r0 = P.c * S, j = P.c - P.unit0;
+                    int kb = P.rp[0], ke = P.rp[1];  // constant indices only: P stays in registers
+#pragma unroll
+                    for (int k = 1; k < kClaimChunks; ++k)
+                        if (j == k) {
+                            kb = P.rp[k];
+                            ke = P.rp[k + 1];
+                        }
+                    const int kb4 = kb & ~3, ke4 = (ke + 3) & ~3;
+                    const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
+                    unsigned char* st = ss.stage0 + s * stage_bytes;
+                    mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
+                    if (span) {
+                        for (int m = 0; m < 9; ++m)
+                            bulk_copy_g2s_stream(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4,
+                                                 span, fb, pol);
+                        bulk_copy_g2s_stream(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb,
+                                             pol);
+                    }
+                    bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0,
+                                  (uint32_t)(S + 4) * 4u, fb);
+                } else {
+                    mbar_arrive(fb);
+                }
+                issued = g + 1;
+                if (P.c < 0) {
+                    P.end_it = P.it;
+                    P.end_g_prev = P.end_g;
+                    P.end_g = g;
+                }
+                // next stage: the unit's next chunk, else the claimed unit, else claim at the top
+                if (P.c >= 0 && P.c + 1 < P.unit_end) {
+                    P.c += 1;
+                } else if (P.pending) {
+                    P.pending = false;
+                    dyn_take(B, n_chunks, P.next_it, P.next_v, P);
+                } else {
+                    P.it = P.c < 0 ? P.it + 1 : P.it;
+                    P.have = false;
+                }
+            }
+        }
+    } else {
+        const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
+        const int la = 4 * cw + half, lb = la + 2;
+        const int idx = lane16 >> 1;                 // epilogue: 0..2 row A, 3..5 row B
+        const bool owner = !(lane16 & 1) && idx < 6;  // the lane that finishes one component
+        const float* __restrict__ z = B.z;
+        auto pv = [z, p_old, beta, first](int c) { return direction_cg(z, p_old, beta, first, c); };
+        const int n = B.n_blocks;
+        // p.q of the last chunk, published while the next chunk's gathers are in flight:
+        // warp sum in a fixed tree, then the last warp of the block to publish a chunk adds
+        // the 15 warp sums in warp order and stores the chunk's partial
+        FF pend{0.f, 0.f};
+        int pend_c = -1;
+        unsigned pend_ps = 0;
+        auto publish = [&]() {
+            FF t = pend;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_down(t, o));
+            if (lane == 0) {
+                volatile float2* wp = ss.wpart + pend_ps * kStagedConsumerWarps;
+                wp[cw].x = t.hi;
+                wp[cw].y = t.lo;
+                __threadfence_block();
+                if (atomicAdd(&ss.wcount[pend_ps], 1u) == kStagedConsumerWarps - 1) {
+                    __threadfence_block();
+                    FF sum{wp[0].x, wp[0].y};
+                    for (int w = 1; w < kStagedConsumerWarps; ++w) sum = ff_add(sum, FF{wp[w].x, wp[w].y});
+                    part[pend_c] = make_float2(sum.hi, sum.lo);
+                    ss.wcount[pend_ps] = 0;
+                }
+            }
+            pend_c = -1;
+        };
+        for (;;) {
+            const unsigned g = seq, s = g % NS;
+            // one decision per warp: the product below shuffles over the full warp
+            const bool stop = __any_sync(0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1));
+            if (stop) {
+                *abort_flag = 1;
+                break;
+            }
+            const int c = *(volatile int*)&ss.chunk[s];
+            seq = g + 1;
+            if (c < 0) {  // end of this pass
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                if (pend_c >= 0) publish();
+                break;
+            }
+            const int r0 = c * S;
+            const int rowA = r0 + la, rowB = r0 + lb;
+            const bool vA = rowA < n, vB = rowB < n;
+            // this lane's own component: its loads go out with the gathers below
+            const bool own = owner && (idx < 3 ? vA : vB);
+            const int64_t o = 4 * (int64_t)(idx < 3 ? rowA : rowB) + idx % 3;
+            float zo = 0.f, po = 0.f;
+            if (own) {
+                zo = __ldcg(z + o);
+                if (!first) po = __ldcg(p_old + o);
+            }
+            const unsigned char* st = ss.stage0 + s * stage_bytes;
+            const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
+            const int kb4 = rp[0] & ~3;
+            float a[3], b[3];
+            const int kbA = vA ? rp[la] - kb4 : 0, keA = vA ? rp[la + 1] - kb4 : 0;
+            const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
+            const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
+            const float* __restrict__ svals = reinterpret_cast<const float*>(st);
+            if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
+                // rows of at most 16 blocks: each lane takes at most one block of each row into
+                // registers and the stage is released before the gathers
+                const int kA = kbA + lane16, kB = kbB + lane16;
+                const bool hA = kA < keA, hB = kB < keB;
+                const int cA = hA ? scols[kA] : 0, cB = hB ? scols[kB] : 0;
+                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
+                float mA[9], mB[9];
+#pragma unroll
+                for (int m = 0; m < 9; ++m) {
+                    mA[m] = hA ? svals[m * CAP + kA] : 0.0f;
+                    mB[m] = hB ? svals[m * CAP + kB] : 0.0f;
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                if (pend_c >= 0) publish();  // in the shadow of the gathers
+                a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
+                a[1] = mA[3] * xA.x + mA[4] * xA.y + mA[5] * xA.z;
+                a[2] = mA[6] * xA.x + mA[7] * xA.y + mA[8] * xA.z;
+                b[0] = mB[0] * xB.x + mB[1] * xB.y + mB[2] * xB.z;
+                b[1] = mB[3] * xB.x + mB[4] * xB.y + mB[5] * xB.z;
+                b[2] = mB[6] * xB.x + mB[7] * xB.y + mB[8] * xB.z;
+            } else {
+                if (pend_c >= 0) publish();
+                two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, pv, a, b);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+            }
+            const float qd = half_warp_transpose_sum<float>(a, b, lane16);
+            FF t{0.f, 0.f};
+            if (own) {
+                const float pd = first ? zo : fmaf(beta, po, zo);  // direction_cg()'s bits
+                p_new[o] = pd;
+                B.q[o] = qd;
+                t = ff_prod(pd, qd);
+            }
+            pend = t;
+            pend_c = c;
+            pend_ps = g % kStagedPartSlots;
+        }
+    }
+}
+
+// Block-wide float-float sums of two values per thread in a fixed tree; valid in thread 0.
+__device__ __forceinline__ void block_sum2_ff(FF a, FF b, double* sh, FF& ra, FF& rb)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = ff_add(a, ff_shfl_down(a, o));
+        b = ff_add(b, ff_shfl_down(b, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float* shf = reinterpret_cast<float*>(sh);  // 4 floats per warp
+    __syncthreads();
+    if (lane == 0) {
+        shf[4 * warp] = a.hi;
+        shf[4 * warp + 1] = a.lo;
+        shf[4 * warp + 2] = b.hi;
+        shf[4 * warp + 3] = b.lo;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        a = lane < nw ? FF{shf[4 * lane], shf[4 * lane + 1]} : FF{0.f, 0.f};
+        b = lane < nw ? FF{shf[4 * lane + 2], shf[4 * lane + 3]} : FF{0.f, 0.f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = ff_add(a, ff_shfl_down(a, o));
+            b = ff_add(b, ff_shfl_down(b, o));
+        }
+    }
+    ra = a;
+    rb = b;
+}
+
+// Sums of two arrays of gridDim.x float-float block partials, in one fixed order (the same
+// in every block), returned to every thread.
+__device__ void sum_grid_partials2_ff(const float2* pa, const float2* pb, double* sh, double& a, double& b)
+{
+    FF va{0.f, 0.f}, vb{0.f, 0.f};
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+        const float2 x = __ldcg(pa + i), y = __ldcg(pb + i);
+        va = ff_add(va, FF{x.x, x.y});
+        vb = ff_add(vb, FF{y.x, y.y});
+    }
+    FF ra, rb;
+    block_sum2_ff(va, vb, sh, ra, rb);
+    __shared__ double result[2];
+    if (threadIdx.x == 0) {
+        result[0] = (double)ra.hi + (double)ra.lo;
+        result[1] = (double)rb.hi + (double)rb.lo;
+    }
+    __syncthreads();
+    a = result[0];
+    b = result[1];
+}
+
+// Sum of the n float-float chunk partials in one fixed order (the same in every block),
+// returned to every thread.
+__device__ double sum_chunk_partials(const float2* part, int n, double* sh)
+{
+    FF a{0.f, 0.f};
+    int i = threadIdx.x;
+    for (; i + 3 * (int)blockDim.x < n; i += 4 * blockDim.x) {
+        const float2 v0 = __ldcg(part + i), v1 = __ldcg(part + i + blockDim.x), v2 = __ldcg(part + i + 2 * blockDim.x),
+                     v3 = __ldcg(part + i + 3 * blockDim.x);
+        a = ff_add(a, FF{v0.x, v0.y});
+        a = ff_add(a, FF{v1.x, v1.y});
+        a = ff_add(a, FF{v2.x, v2.y});
+        a = ff_add(a, FF{v3.x, v3.y});
+    }
+    for (; i < n; i += blockDim.x) {
+        const float2 v = __ldcg(part + i);
+        a = ff_add(a, FF{v.x, v.y});
+    }
+    DotAcc<float> acc;
+    acc.v = a;
+    const double r = acc.block_sum(sh);
+    __shared__ double result;
+    if (threadIdx.x == 0) result = r;
+    __syncthreads();
+    return result;
 }
 
 __global__ void __launch_bounds__(kStagedThreads, 1)
@@ -1218,40 +1613,41 @@ __global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __
 
 // ---------------------------------------------------------------- persistent PCG
 // The whole PCG loop in one cooperative launch (all blocks resident): per iteration the
-// staged product pass, a grid barrier, p.Ap from every block's partial (each block sums the
-// partials itself in index order, so all blocks hold the same alpha), the update of the
-// block's own rows (x, r, z, r.r, r.z), a second grid barrier, and the convergence test and
-// beta, computed identically in every block.  The iteration and its stopping rules are
-// those of k_pcg_spmv + k_pcg_update.  Plain (L1-cached) loads are safe across iterations:
-// the barrier's acquire at GPU scope, ordered before every thread of the block by
-// __syncthreads, makes the other blocks' writes visible to them (the guarantee a grid
-// synchronization gives).  Grid barrier words: bar[0] counts arrivals over the
-// whole launch, bar[1] is the released generation; both are zero at launch.  Every wait is
-// bounded; a block that gives up flags PcgState::wait_failed and leaves the loop.
+// staged product pass over dynamically claimed chunks (staged_spmv_pass_dyn), a grid
+// barrier, p.Ap from the chunk partials (every block sums them itself in one fixed order,
+// so all blocks hold the same alpha), the update of the block's own rows (x, r, z, r.r, r.z;
+// rows split evenly over the blocks), a second grid barrier, and the convergence test and
+// beta, computed identically in every block.  The iteration and its stopping rules are those
+// of k_pcg_spmv + k_pcg_update.  Plain (L1-cached) loads are safe across iterations: the
+// barrier's acquire at GPU scope, ordered before every thread of the block by __syncthreads,
+// makes the other blocks' writes visible to them (the guarantee a grid synchronization
+// gives).  Grid barrier word bar[0] counts arrivals over the whole launch (zero at launch):
+// barrier k is passed when it reaches k * gridDim.x.  Every wait is bounded; a block that
+// gives up flags PcgState::wait_failed and leaves the loop.
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* ok_flag)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned target = generation + 1;
+        const unsigned target = (generation + 1) * gridDim.x;
         __threadfence();
-        const unsigned arrived = atomicAdd(&bar[0], 1u) + 1u;
-        if (arrived == gridDim.x * target) {
-            __threadfence();
-            atomicExch(&bar[1], target);
-        }
+        red_release_add(&bar[0], 1u);
         bool ok = true;
-        for (long long polls = 0; ld_acquire(&bar[1]) < target; ++polls) {
+        for (long long polls = 0; ld_acquire(&bar[0]) < target; ++polls) {
             if (polls > kMaxBarrierPolls) {
                 ok = false;
                 break;
             }
-            __nanosleep(64);
+            __nanosleep(32);
         }
         __threadfence();
         *ok_flag = ok ? 1 : 0;
@@ -1261,34 +1657,10 @@ __device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* 
     return *ok_flag != 0;
 }
 
-// Sum over the gridDim.x partials, in index order and the same tree in every block.
-__device__ double sum_grid_partials(const double* partials, double* sh)
+// Chunks of the persistent kernel's product pass (one stage of rows each).
+__host__ __device__ __forceinline__ int pcg_chunks(int n_blocks, int stage_rows)
 {
-    double v = 0.0;
-    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) v += __ldcg(partials + i);
-    v = block_reduce<false>(v, sh);
-    __shared__ double result;
-    if (threadIdx.x == 0) result = v;
-    __syncthreads();
-    return result;
-}
-
-// The same for two partial arrays at once (one pass over both, two block reductions).
-__device__ void sum_grid_partials2(const double* pa, const double* pb, double* sh, double& a, double& b)
-{
-    double va = 0.0, vb = 0.0;
-    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
-        va += __ldcg(pa + i);
-        vb += __ldcg(pb + i);
-    }
-    va = block_reduce<false>(va, sh);
-    __shared__ double result[2];
-    if (threadIdx.x == 0) result[0] = va;
-    vb = block_reduce<false>(vb, sh);
-    if (threadIdx.x == 0) result[1] = vb;
-    __syncthreads();
-    a = result[0];
-    b = result[1];
+    return (n_blocks + stage_rows - 1) / stage_rows;
 }
 
 __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffers<float> B)
@@ -1306,30 +1678,32 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
     __syncthreads();
     volatile int* abort_flag = &aborted;
     unsigned* bar = B.tickets + 6;
+    unsigned* ctr = B.tickets + 8;  // chunk counters of three consecutive passes
     unsigned generation = 0, seq = 0, issued = 0;
+    DynProducer P;
     const unsigned G = gridDim.x;
-    double* part_pq = B.partials;
-    double* part_rr = B.partials + G;
-    double* part_rz = B.partials + 2 * G;
-    const int row_begin = blockIdx.x * B.staged.rows_per_block;
-    const int row_end = min(row_begin + B.staged.rows_per_block, B.n_blocks);
+    const int n_chunks = pcg_chunks(B.n_blocks, B.staged.stage_rows);
+    float2* part_pq = reinterpret_cast<float2*>(B.partials);
+    float2* part_rr = reinterpret_cast<float2*>(B.partials + n_chunks);
+    float2* part_rz = part_rr + G;
+    const int row_begin = (int)((int64_t)blockIdx.x * B.n_blocks / G);
+    const int row_end = (int)((int64_t)(blockIdx.x + 1) * B.n_blocks / G);
     double rz = st0.rz, alpha = 0.0, beta = 0.0, pAp = 0.0, rr = 0.0, error = st0.error;
     int iteration = st0.iteration, converged = 0, indefinite = 0;
     bool failed = false;
-    while (true) {
+    for (int li = 0;; ++li) {
         float* p_old = (iteration & 1) ? B.p : B.p2;
         float* p_new = (iteration & 1) ? B.p2 : B.p;
         const bool first = iteration == 0;
-        DotAcc<float> pq;
-        staged_spmv_pass<false>(B, ss, p_old, p_new, first, first ? 0.f : (float)beta, seq, issued, true, abort_flag,
-                                pq);
-        const double bpq = pq.block_sum(sh);
-        if (threadIdx.x == 0) part_pq[blockIdx.x] = bpq;
+        staged_spmv_pass_dyn(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : (float)beta, seq, issued, P,
+                             abort_flag, part_pq);
         if (!grid_barrier(bar, generation, &barrier_ok) || *abort_flag) {
             failed = true;
             break;
         }
-        pAp = sum_grid_partials(part_pq, sh);
+        // no block claims from pass li - 1 any more, none from pass li + 2 before the next barrier
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ctr[(li + 2) % 3], 0u);
+        pAp = sum_chunk_partials(part_pq, n_chunks, sh);
         if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
             indefinite = 1;
             iteration += 1;
@@ -1363,18 +1737,18 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
             rza.add_prod(r.y, z.y);
             rza.add_prod(r.z, z.z);
         }
-        const double brr = rra.block_sum(sh);
-        const double brz = rza.block_sum(sh);
+        FF brr, brz;
+        block_sum2_ff(rra.v, rza.v, sh, brr, brz);
         if (threadIdx.x == 0) {
-            part_rr[blockIdx.x] = brr;
-            part_rz[blockIdx.x] = brz;
+            part_rr[blockIdx.x] = make_float2(brr.hi, brr.lo);
+            part_rz[blockIdx.x] = make_float2(brz.hi, brz.lo);
         }
         if (!grid_barrier(bar, generation, &barrier_ok)) {
             failed = true;
             break;
         }
         double rz_new;
-        sum_grid_partials2(part_rr, part_rz, sh, rr, rz_new);
+        sum_grid_partials2_ff(part_rr, part_rz, sh, rr, rz_new);
         iteration += 1;
         error = sqrt(rr / st0.bb);
         if (error < st0.abs_tol || error / st0.error0 < st0.rel_tol) {
@@ -1602,14 +1976,14 @@ void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, 
 
 template <typename T>
 void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s,
-                       ProjectionScratch scratch)
+                       ProjectionScratch scratch, const int64_t* sel)
 {
     if (count <= 0) return;
     if (N == 12 && scratch.fallback && scratch.n_fallback) {
         const cudaError_t e = cudaMemsetAsync(scratch.n_fallback, 0, sizeof(unsigned long long), s);
         if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
         k_project_pd_deflated<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged,
-                                                                              scratch.fallback, scratch.n_fallback);
+                                                                              scratch.fallback, scratch.n_fallback, sel);
         check_launch("project_pd_deflated");
         static const unsigned listed_grid = resident_grid(k_project_pd_listed<T, 12>, 128);
         k_project_pd_listed<T, 12><<<listed_grid, 128, 0, s>>>(H, scratch.fallback, scratch.n_fallback, eps, mirroring,
@@ -1618,21 +1992,21 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
         return;
     }
     switch (N) {
-        case 3: k_project_pd_unrolled<T, 3><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
-        case 6: k_project_pd_unrolled<T, 6><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
-        case 9: k_project_pd_unrolled<T, 9><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
-        case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged); break;
+        case 3: k_project_pd_unrolled<T, 3><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
+        case 6: k_project_pd_unrolled<T, 6><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
+        case 9: k_project_pd_unrolled<T, 9><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
+        case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
         case 24: {
             constexpr int threads = ProjPairsCfg<T>::warps * 32;
             static const unsigned grid = resident_grid(k_project_pd_pairs<T, 24>, threads);
             const unsigned need = blocks_for(count, ProjPairsCfg<T>::warps);
             k_project_pd_pairs<T, 24><<<need < grid ? need : grid, threads, 0, s>>>(H, count, eps, mirroring,
-                                                                                   not_converged);
+                                                                                   not_converged, sel);
             break;
         }
         default:
             if (N > 24 || N % 3 != 0) throw std::runtime_error("symx_gb300: projection supports N = 3k <= 24");
-            k_project_pd_generic<T><<<blocks_for(count, 64), 64, 0, s>>>(H, N, count, eps, mirroring, not_converged);
+            k_project_pd_generic<T><<<blocks_for(count, 64), 64, 0, s>>>(H, N, count, eps, mirroring, not_converged, sel);
     }
     check_launch("project_pd");
 }
@@ -1655,6 +2029,22 @@ void launch_gather_gradient(int n_blocks, const int64_t* ptr, const int32_t* con
 {
     k_gather_gradient<<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, ptr, contrib, gel, g);
     check_launch("gather_gradient");
+}
+
+void launch_ppn_mark_blocks(int n_blocks, const double* grad, double thr, const int64_t* gptr, const int32_t* gcontrib,
+                            uint8_t* gflag, unsigned long long* n_inactive, cudaStream_t s)
+{
+    if (n_blocks <= 0) return;
+    k_ppn_mark_blocks<<<blocks_for(n_blocks, 256), 256, 0, s>>>(n_blocks, grad, thr, gptr, gcontrib, gflag, n_inactive);
+    check_launch("ppn_mark_blocks");
+}
+
+void launch_select_elements(int64_t n_el, int nb, const uint8_t* gflag, uint8_t* is_proj, int64_t* sel,
+                            unsigned long long* n_sel, cudaStream_t s)
+{
+    if (n_el <= 0) return;
+    k_select_elements<<<blocks_for(n_el, 256), 256, 0, s>>>(n_el, nb, gflag, is_proj, sel, n_sel);
+    check_launch("select_elements");
 }
 
 template <typename T>
@@ -1709,7 +2099,7 @@ void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
 void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s)
 {
     if (!B.staged.persistent) throw std::runtime_error("symx_gb300: persistent PCG not planned for this matrix");
-    const cudaError_t e = cudaMemsetAsync(B.tickets + 6, 0, 2 * sizeof(unsigned), s);
+    const cudaError_t e = cudaMemsetAsync(B.tickets + 6, 0, 5 * sizeof(unsigned), s);
     if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
     PcgBuffers<float> arg = B;
     void* args[] = {&arg};
@@ -1742,10 +2132,10 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
         }
         const size_t stage_bytes = staged_stage_bytes((int)cap, S);
         const int64_t budget =
-            std::min<int64_t>(optin, per_sm_bytes / per_sm - 1024) - 16 * kStagedMaxStages - 1024;  // static smem
+            std::min<int64_t>(optin, per_sm_bytes / per_sm - 1024) - (int64_t)kStagedHeaderBytes - 1024;  // static smem
         const int stages = (int)std::min<int64_t>(kStagedMaxStages, budget / (int64_t)stage_bytes);
         if (stages < 2 || cap > (1 << 24)) continue;
-        const size_t smem = 16 * kStagedMaxStages + (size_t)stages * stage_bytes;
+        const size_t smem = kStagedHeaderBytes + (size_t)stages * stage_bytes;
         if (cudaFuncSetAttribute(k_pcg_spmv_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
             cudaGetLastError();
             continue;
@@ -1765,7 +2155,7 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
                 cudaSuccess &&
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_solve, k_pcg_solve_staged, kStagedThreads, smem) ==
                 cudaSuccess &&
-            resident_solve >= per_sm && 3 * grid <= 2 * kPcgMaxPartials)
+            resident_solve >= per_sm && pcg_chunks(n, S) + 2 * grid <= 2 * kPcgMaxPartials)
             st.persistent = 1;
         cudaGetLastError();
         st.stages = stages;
@@ -1878,7 +2268,8 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
 
 #define SYMXG_INSTANTIATE(T)                                                                                          \
     template void launch_dot_mixed<T>(const T*, const double*, int64_t, double*, unsigned*, double*, cudaStream_t);  \
-    template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t, ProjectionScratch);              \
+    template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t, ProjectionScratch,               \
+                                       const int64_t*);                                                                 \
     template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, int64_t, cudaStream_t); \
     template void launch_block_jacobi_setup<T>(int, const int32_t*, const T*, int64_t, T*, cudaStream_t);              \
     template void launch_pcg_init<T>(const PcgBuffers<T>&, const double*, cudaStream_t);                               \

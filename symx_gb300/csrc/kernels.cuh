@@ -53,9 +53,19 @@ struct ProjectionScratch {
     int64_t* fallback = nullptr;
     unsigned long long* n_fallback = nullptr;
 };
+// sel: when given, project the `count` matrices H[sel[k]] instead of H[0 .. count).
 template <typename T>
 void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s,
-                       ProjectionScratch scratch = ProjectionScratch{});
+                       ProjectionScratch scratch = ProjectionScratch{}, const int64_t* sel = nullptr);
+
+// Progressive projection: flag (gflag[gblock] = 1) the element gradient blocks of the DoF
+// blocks with max |grad| >= thr, counting the other blocks in *n_inactive; then list the
+// elements of one potential not projected yet that touch a flagged block (all unprojected
+// ones when gflag is null), marking them.
+void launch_ppn_mark_blocks(int n_blocks, const double* grad, double thr, const int64_t* gptr, const int32_t* gcontrib,
+                            uint8_t* gflag, unsigned long long* n_inactive, cudaStream_t s);
+void launch_select_elements(int64_t n_el, int nb, const uint8_t* gflag, uint8_t* is_proj, int64_t* sel,
+                            unsigned long long* n_sel, cudaStream_t s);
 
 // BCSR values are stored component-major: component m (row-major inside the 3x3 block) of
 // block k is vals[m * vstride + k], vstride >= nnzb.  vstride == kTiledBcsr selects the
@@ -98,7 +108,7 @@ struct PcgBuffers {
     T* p2;
     T* q;
     double* partials;   // kPcgPartials doubles x 2
-    unsigned* tickets;  // 4 counters
+    unsigned* tickets;  // counters: 16 for the persistent kernel, 8 otherwise
     PcgState* state;
     // Staged SpMV (float, strided layout only; stages == 0: not used).  The producer copies
     // each stage's rows with bulk copies, which read these padded copies of row_ptr and cols.
@@ -156,7 +166,8 @@ StagedSizes plan_staged_spmv(int n_blocks, const int32_t* row_ptr_host, PcgBuffe
 
 // All PCG iterations (after launch_pcg_init) in one cooperative launch of the staged kernel:
 // runs until convergence, p.Ap <= 0 or state->max_iterations, then sets state->done.  Only
-// when B.staged.persistent; uses tickets[6..7] (cleared here) as its grid barrier.
+// when B.staged.persistent; uses tickets[6..10] (cleared here): its grid barrier and the
+// chunk counters of its dynamically scheduled product passes.
 void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s);
 
 // On the PCG solution du (4 values per block row) and double vectors with 3 per row:

@@ -512,6 +512,12 @@ struct SolverImpl {
     // projection: indices of the 12 x 12 element Hessians that need the full decomposition
     DevBuf<int64_t> proj_fallback;
     DevBuf<unsigned long long> proj_n_fallback;
+    // Progressive projection: per element "projected in this evaluation", per element gradient
+    // block "touches an active DoF block", the selected elements of one potential, and counters
+    // (inactive DoF blocks, then the selection count of each potential)
+    DevBuf<uint8_t> ppn_is_proj, ppn_gflag;
+    DevBuf<int64_t> ppn_sel;
+    DevBuf<unsigned long long> ppn_counts;
     symxg::ProjectionScratch proj_scratch()
     {
         symxg::ProjectionScratch ps;
@@ -909,8 +915,8 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
     I.g_el.alloc(std::max<int64_t>(1, I.n_gblocks * 3));
     I.partials.alloc(2 * symxg::kPcgMaxPartials);
     I.scalars.alloc(16);
-    I.tickets.alloc(8);
-    ck(cudaMemset(I.tickets.p, 0, sizeof(unsigned) * 8), "memset");
+    I.tickets.alloc(16);
+    ck(cudaMemset(I.tickets.p, 0, sizeof(unsigned) * 16), "memset");
     I.pcg_state.alloc(1);
     I.flags.alloc(4);
     {

@@ -56,6 +56,9 @@ struct NewtonSettings {
     ProjectionToPD projection_mode = ProjectionToPD::ProjectedNewton;
     double projection_eps = 1e-10;
     bool project_to_pd_use_mirroring = false;
+    int project_on_demand_countdown = 4;   // ProjectOnDemand: Newton iterations projected after a failure
+    double ppn_tightening_factor = 0.5;    // Progressive: threshold factor after a failed direction
+    double ppn_release_factor = 2.0;       // Progressive: threshold factor after a successful one
     LinearSolver linear_solver = LinearSolver::BDPCG;
     int cg_max_iterations = 10000;
     double cg_abs_tolerance = 1e-12;
