@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SYMXG_ABI_VERSION 2
+#define SYMXG_ABI_VERSION 3
 
 /* status codes */
 #define SYMXG_OK 0
@@ -30,6 +30,12 @@ extern "C" {
 #define SYMXG_ERR_RUNTIME 2 /* CUDA, NVRTC or internal failure; see symxg_last_error() */
 
 /* arithmetic of the Hessian path */
+/* projection modes (symx::ProjectionToPD): no projection, every element Hessian, all of them
+ * for a few iterations after a failed direction, or those near large gradients */
+#define SYMXG_PROJECTION_NEWTON 0
+#define SYMXG_PROJECTION_PROJECTED_NEWTON 1
+#define SYMXG_PROJECTION_ON_DEMAND 2
+#define SYMXG_PROJECTION_PROGRESSIVE 3
 #define SYMXG_PRECISION_FP64 0
 #define SYMXG_PRECISION_MIXED 1 /* FP32 element Hessians, projection, BCSR and PCG vectors;
                                    FP64 energy, gradient, residual, line search, dot sums */
@@ -82,7 +88,7 @@ typedef struct symxg_newton_settings {
     int32_t enable_armijo_backtracking;
     double line_search_armijo_beta;
     int32_t max_backtracking_armijo_iterations;
-    int32_t project_to_pd;           /* 1 ProjectedNewton (default), 0 plain Newton */
+    int32_t project_to_pd;           /* SYMXG_PROJECTION_*: symx::ProjectionToPD (solver_utils.h:137-142) */
     double projection_eps;
     int32_t project_to_pd_use_mirroring;
     int32_t cg_max_iterations;
@@ -91,6 +97,9 @@ typedef struct symxg_newton_settings {
     double bailout_residual;
     int32_t precision;               /* SYMXG_PRECISION_* */
     int32_t time_kernels;            /* 1: record CUDA events around PCG SpMV and projection launches */
+    int32_t project_on_demand_countdown; /* ProjectOnDemand: iterations projected after a failure (4) */
+    double ppn_tightening_factor;    /* Progressive: threshold factor after a failed direction (0.5) */
+    double ppn_release_factor;       /* Progressive: threshold factor after a successful one (2.0) */
 } symxg_newton_settings;
 
 typedef struct symxg_solve_stats {
@@ -115,6 +124,8 @@ typedef struct symxg_solve_stats {
     int64_t pcg_solve_iterations;    /* with time_kernels: PCG iterations run by the one-launch PCG ... */
     double pcg_solve_seconds;        /* ... and the device time of those launches */
     int32_t cg_iterations_per_newton[16]; /* PCG iterations of the first 16 linear solves (0 after) */
+    int64_t n_hessians;              /* element Hessians of the Newton iterations that found a direction */
+    int64_t n_projected_hessians;    /* ... and how many of them were projected */
 } symxg_solve_stats;
 
 /* message of the last failing call on this thread ("" if none) */

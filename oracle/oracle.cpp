@@ -474,6 +474,39 @@ void project_all(Problem& P, double eps, bool mirroring, double* t)
     if (t) *t += seconds_since(t0);
 }
 
+// Projection of the element Hessians not yet projected in this evaluation: all of them
+// (active == nullptr), or those with a node whose block row is active
+// (ElementHessians.cpp:69-182).  Slots [0, ne) of is_proj are the elastic elements, then one
+// per vertex (inertia or gravity) and one per boundary vertex; `count` adds the elements
+// projected.
+void project_selected(Problem& P, double eps, bool mirroring, std::vector<uint8_t>& is_proj, const uint8_t* active,
+                      long long& count)
+{
+    const int nn = P.nodes, n = 3 * nn;
+    std::vector<uint8_t> pick(P.ne, 0);
+    for (int e = 0; e < P.ne; ++e) {
+        if (is_proj[e]) continue;
+        bool take = active == nullptr;
+        for (int a = 0; a < nn && !take; ++a) take = active[P.conn[e * nn + a]] != 0;
+        if (take) {
+            pick[e] = 1;
+            is_proj[e] = 1;
+            ++count;
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 64) num_threads(P.n_threads)
+    for (int e = 0; e < P.ne; ++e)
+        if (pick[e]) project_pd(n, &P.Hel[(size_t)e * n * n], eps, mirroring);
+    for (int v = 0; v < P.nv; ++v) {
+        const size_t k = (size_t)P.ne + v;
+        if (!is_proj[k] && (active == nullptr || active[v])) { is_proj[k] = 1; ++count; }
+    }
+    for (int i = 0; i < P.nbc; ++i) {
+        const size_t k = (size_t)P.ne + P.nv + i;
+        if (!is_proj[k] && (active == nullptr || active[P.bc_idx[i]])) { is_proj[k] = 1; ++count; }
+    }
+}
+
 // Block-Jacobi preconditioner (BlockedSparseMatrix.h:1146-1278): the symmetric 3x3
 // inverse of each diagonal block via the cofactors of its upper triangle.
 void block_jacobi_setup(Problem& P)
@@ -608,6 +641,12 @@ struct oracle_settings {
     double armijo_beta;
     int max_armijo;
     double bailout_residual;
+    // ProjectionToPD (solver_utils.h:137-142): 0 Newton, 1 ProjectedNewton, 2 ProjectOnDemand,
+    // 3 Progressive; and their parameters (solver_utils.h:219-228)
+    int projection_mode;
+    int project_on_demand_countdown;
+    double ppn_tightening_factor;
+    double ppn_release_factor;
 };
 
 struct oracle_stats {
@@ -618,6 +657,9 @@ struct oracle_stats {
     double final_residual;
     double final_energy;
     double t_eval, t_project, t_assembly, t_linear_solve, t_line_search, t_total;
+    // element Hessians evaluated / projected over the solve, the inertia (or gravity) and
+    // boundary potentials' one-vertex elements included (NewtonsMethod.cpp:219-227)
+    long long n_hessians, n_projected_hessians;
 };
 
 void oracle_default_settings(oracle_settings* s)
@@ -636,6 +678,10 @@ void oracle_default_settings(oracle_settings* s)
     s->armijo_beta = 1e-4;
     s->max_armijo = 20;
     s->bailout_residual = 1e-10;
+    s->projection_mode = 1;
+    s->project_on_demand_countdown = 4;
+    s->ppn_tightening_factor = 0.5;
+    s->ppn_release_factor = 2.0;
 }
 
 int oracle_num_threads(void)
@@ -759,6 +805,12 @@ int oracle_solve(void* h, const oracle_settings* s, oracle_stats* st)
     int result = -1;  // running
     int it = -1;
     double E0 = 0.0, residual = 0.0;
+    const int mode = s->projection_mode;
+    int pdn_countdown = 0;
+    double ppn_threshold = -1.0;
+    std::vector<uint8_t> is_proj((size_t)P.ne + P.nv + P.nbc), active(P.nv);
+    const long long n_all_hessians = (long long)P.ne + P.nv + P.nbc;
+    long long n_proj = 0;
     while (result < 0) {
         ++it;
         if (it == s->max_iterations) { result = s->max_iterations_as_success ? 0 : 2; break; }
@@ -771,19 +823,64 @@ int oracle_solve(void* h, const oracle_settings* s, oracle_stats* st)
             if (residual < s->residual_tolerance_abs) { result = 0; break; }
             if (it > 0 && residual / res0 < s->residual_tolerance_rel) { result = 0; break; }
         }
-        project_all(P, s->projection_eps, s->mirroring != 0, &st->t_project);
-        assemble(P, &st->t_assembly);
-        auto tl = Clock::now();
-        const double forcing = std::min(1e-2, residual * std::min(0.5, std::sqrt(residual)));
-        const double abs_tol = std::max(forcing, s->cg_abs_tolerance);
-        for (size_t i = 0; i < n; ++i) rhs[i] = -grad[i];
-        PCGOut po = pcg(P, du.data(), rhs.data(), abs_tol, s->cg_rel_tolerance, s->cg_max_iterations);
-        st->t_linear_solve += seconds_since(tl);
-        st->cg_iterations += po.iters;
-        if (!po.converged) { result = 4; break; }
+        // projection and solve until the direction descends or nothing is left to project
+        // (NewtonsMethod.cpp:133-186, _project_and_assemble :257-341, _increase_projection
+        // :343-358, _decrease_projection :359-373).  Element Hessians of this evaluation start
+        // unprojected; the inertia/gravity and boundary potentials' one-vertex elements are
+        // counted like the reference's (their projection changes nothing the oracle keeps).
+        std::fill(is_proj.begin(), is_proj.end(), 0);
         double du_dot_g = 0.0, du_max = 0.0;
-        for (size_t i = 0; i < n; ++i) { du_dot_g += du[i] * grad[i]; du_max = std::max(du_max, std::fabs(du[i])); }
-        if (!(du_dot_g < 0.0)) { result = 5; break; }
+        while (true) {
+            bool all_projected = false;
+            const auto tp = Clock::now();
+            if (mode == 1 || (mode == 2 && pdn_countdown > 0)) {
+                project_selected(P, s->projection_eps, s->mirroring != 0, is_proj, nullptr, n_proj);
+                all_projected = true;
+            } else if (mode == 3 && ppn_threshold > 0.0) {
+                if (ppn_threshold < 1e-12) ppn_threshold = 0.0;
+                all_projected = true;
+                for (int v = 0; v < P.nv; ++v) {
+                    const double m = std::max(std::fabs(grad[3 * v]), std::max(std::fabs(grad[3 * v + 1]), std::fabs(grad[3 * v + 2])));
+                    active[v] = m >= ppn_threshold ? 1 : 0;
+                    if (!active[v]) all_projected = false;
+                }
+                project_selected(P, s->projection_eps, s->mirroring != 0, is_proj, active.data(), n_proj);
+            }
+            st->t_project += seconds_since(tp);
+            assemble(P, &st->t_assembly);
+            auto tl = Clock::now();
+            const double forcing = std::min(1e-2, residual * std::min(0.5, std::sqrt(residual)));
+            const double abs_tol = std::max(forcing, s->cg_abs_tolerance);
+            for (size_t i = 0; i < n; ++i) rhs[i] = -grad[i];
+            PCGOut po = pcg(P, du.data(), rhs.data(), abs_tol, s->cg_rel_tolerance, s->cg_max_iterations);
+            st->t_linear_solve += seconds_since(tl);
+            st->cg_iterations += po.iters;
+            const bool can_project_more = mode != 0 && !all_projected;
+            if (!po.converged && !can_project_more) { result = 4; break; }
+            bool descends = false;
+            if (po.converged) {
+                du_dot_g = 0.0;
+                for (size_t i = 0; i < n; ++i) du_dot_g += du[i] * grad[i];
+                descends = du_dot_g < 0.0;
+                if (!descends && !can_project_more) { result = 5; break; }
+            }
+            if (po.converged && descends) break;
+            if (mode == 2) pdn_countdown = s->project_on_demand_countdown;
+            if (mode == 3) {
+                if (ppn_threshold < 0.0) ppn_threshold = residual;
+                ppn_threshold *= s->ppn_tightening_factor;
+                // Deviation: a zero threshold cannot tighten and the reference would retry the
+                // same solve forever; a threshold below 1e-12 projects everything next time.
+                if (ppn_threshold == 0.0) ppn_threshold = 1e-13;
+            }
+        }
+        if (result >= 0) break;
+        st->n_hessians += n_all_hessians;  // counted once the direction is found
+        st->n_projected_hessians += n_proj;
+        n_proj = 0;
+        if (mode == 2) pdn_countdown--;
+        if (mode == 3) ppn_threshold *= s->ppn_release_factor;
+        for (size_t i = 0; i < n; ++i) du_max = std::max(du_max, std::fabs(du[i]));
         if (it >= s->min_iterations && du_max < s->step_tolerance) { result = 0; break; }
         // Armijo backtracking (no step cap, no max-step or validity callbacks)
         auto tls = Clock::now();

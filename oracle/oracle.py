@@ -19,6 +19,8 @@ class Settings(C.Structure):
         ("cg_max_iterations", C.c_int), ("cg_abs_tolerance", C.c_double),
         ("cg_rel_tolerance", C.c_double), ("armijo_beta", C.c_double), ("max_armijo", C.c_int),
         ("bailout_residual", C.c_double),
+        ("projection_mode", C.c_int), ("project_on_demand_countdown", C.c_int),
+        ("ppn_tightening_factor", C.c_double), ("ppn_release_factor", C.c_double),
     ]
 
 
@@ -28,6 +30,7 @@ class Stats(C.Structure):
         ("ls_bt_iterations", C.c_int), ("final_residual", C.c_double), ("final_energy", C.c_double),
         ("t_eval", C.c_double), ("t_project", C.c_double), ("t_assembly", C.c_double),
         ("t_linear_solve", C.c_double), ("t_line_search", C.c_double), ("t_total", C.c_double),
+        ("n_hessians", C.c_longlong), ("n_projected_hessians", C.c_longlong),
     ]
 
     def as_dict(self):

@@ -19,7 +19,7 @@
 //   symx_ref_harness elem    <in.bin> <out.bin>            per-element NH Tet4 [E, g(12), H(144)]
 //   symx_ref_harness project <in.bin> <out.bin>            project_to_PD_inplace on n x n matrices
 //   symx_ref_harness eval    <problem.bin> <outdir> <thr>  E, grad, element Hessians, BCSR triplets
-//   symx_ref_harness solve   <problem.bin> <outdir> <thr> [max_newton] [cg_rel_tol]
+//   symx_ref_harness solve   <problem.bin> <outdir> <thr> [max_newton] [cg_rel_tol] [projection mode]
 #include <symx>
 #include <Eigen/Sparse>
 
@@ -296,7 +296,8 @@ int mode_eval(const std::string& pfile, const std::string& outdir, int n_threads
     return 0;
 }
 
-int mode_solve(const std::string& pfile, const std::string& outdir, int n_threads, int max_newton, double cg_rel_tol)
+int mode_solve(const std::string& pfile, const std::string& outdir, int n_threads, int max_newton, double cg_rel_tol,
+               int projection)
 {
     Problem p = load_problem(pfile);
     std::vector<int> numbered = numbered_connectivity(p);
@@ -306,7 +307,10 @@ int mode_solve(const std::string& pfile, const std::string& outdir, int n_thread
     auto t_setup0 = std::chrono::steady_clock::now();
     NewtonsMethod newton(G, ctx);
     auto t_setup1 = std::chrono::steady_clock::now();
-    newton.settings.projection_mode = ProjectionToPD::ProjectedNewton;
+    newton.settings.projection_mode = projection == 0   ? ProjectionToPD::Newton
+                                      : projection == 2 ? ProjectionToPD::ProjectOnDemand
+                                      : projection == 3 ? ProjectionToPD::Progressive
+                                                        : ProjectionToPD::ProjectedNewton;
     newton.settings.projection_eps = 1e-10;
     newton.settings.project_to_pd_use_mirroring = false;
     newton.settings.linear_solver = LinearSolver::BDPCG;
@@ -336,6 +340,8 @@ int mode_solve(const std::string& pfile, const std::string& outdir, int n_thread
        << ",\n  \"newton_iterations\": " << newton.get_last_solve_stats().newton_iterations
        << ",\n  \"cg_iterations\": " << newton.get_last_solve_stats().cg_iterations
        << ",\n  \"ls_bt_iterations\": " << newton.get_last_solve_stats().ls_bt_iterations
+       << ",\n  \"n_hessians\": " << newton.get_last_solve_stats().n_hessians
+       << ",\n  \"n_projected_hessians\": " << newton.get_last_solve_stats().n_projected_hessians
        << ",\n  \"timers\": {";
     bool first = true;
     for (const auto& label : L.get_timer_labels()) {
@@ -363,7 +369,8 @@ int main(int argc, char** argv)
     if (mode == "solve") {
         const int max_newton = argc > 5 ? std::atoi(argv[5]) : -1;
         const double cg_rel = argc > 6 ? std::atof(argv[6]) : 1e-3;
-        return mode_solve(argv[2], argv[3], n_threads, max_newton, cg_rel);
+        const int projection = argc > 7 ? std::atoi(argv[7]) : 1;  // 0 Newton, 1 projected, 2 on demand, 3 progressive
+        return mode_solve(argv[2], argv[3], n_threads, max_newton, cg_rel, projection);
     }
     std::cerr << "unknown mode " << mode << "\n";
     return 1;

@@ -53,6 +53,8 @@ class NewtonSettings(C.Structure):
         ("project_to_pd_use_mirroring", C.c_int32), ("cg_max_iterations", C.c_int32),
         ("cg_abs_tolerance", C.c_double), ("cg_rel_tolerance", C.c_double),
         ("bailout_residual", C.c_double), ("precision", C.c_int32), ("time_kernels", C.c_int32),
+        ("project_on_demand_countdown", C.c_int32), ("ppn_tightening_factor", C.c_double),
+        ("ppn_release_factor", C.c_double),
     ]
 
 
@@ -68,6 +70,7 @@ class SolveStats(C.Structure):
         ("project_launches", C.c_int64), ("project_seconds", C.c_double),
         ("pcg_solve_iterations", C.c_int64), ("pcg_solve_seconds", C.c_double),
         ("cg_iterations_per_newton", C.c_int32 * 16),
+        ("n_hessians", C.c_int64), ("n_projected_hessians", C.c_int64),
     ]
 
     def as_dict(self):

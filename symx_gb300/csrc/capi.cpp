@@ -146,6 +146,8 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
     for (size_t i = 0; i < st.cg_iterations_per_newton.size() && i < 16; ++i)
         o->cg_iterations_per_newton[i] = st.cg_iterations_per_newton[i];
     o->d2h_bytes = st.d2h_bytes;
+    o->n_hessians = (int64_t)st.n_hessians;
+    o->n_projected_hessians = (int64_t)st.n_projected_hessians;
     for (const auto& kv : st.kernels) {
         if (kv.first.rfind("pcg_spmv", 0) == 0) {
             o->spmv_launches += kv.second.first;
@@ -237,6 +239,9 @@ void symxg_default_settings(symxg_newton_settings* s)
     s->bailout_residual = d.bailout_residual;
     s->precision = SYMXG_PRECISION_FP64;
     s->time_kernels = 0;
+    s->project_on_demand_countdown = d.project_on_demand_countdown;
+    s->ppn_tightening_factor = d.ppn_tightening_factor;
+    s->ppn_release_factor = d.ppn_release_factor;
 }
 
 int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, symxg_solver** out)
@@ -363,7 +368,12 @@ int symxg_set_settings(symxg_solver* s, const symxg_newton_settings* c)
         t.enable_armijo_backtracking = c->enable_armijo_backtracking != 0;
         t.line_search_armijo_beta = c->line_search_armijo_beta;
         t.max_backtracking_armijo_iterations = c->max_backtracking_armijo_iterations;
-        t.projection_mode = c->project_to_pd ? symx::ProjectionToPD::ProjectedNewton : symx::ProjectionToPD::Newton;
+        if (c->project_to_pd < SYMXG_PROJECTION_NEWTON || c->project_to_pd > SYMXG_PROJECTION_PROGRESSIVE)
+            throw std::invalid_argument("unknown projection mode");
+        t.projection_mode = static_cast<symx::ProjectionToPD>(c->project_to_pd);
+        t.project_on_demand_countdown = c->project_on_demand_countdown;
+        t.ppn_tightening_factor = c->ppn_tightening_factor;
+        t.ppn_release_factor = c->ppn_release_factor;
         t.projection_eps = c->projection_eps;
         t.project_to_pd_use_mirroring = c->project_to_pd_use_mirroring != 0;
         t.cg_max_iterations = c->cg_max_iterations;

@@ -1128,6 +1128,50 @@ void NewtonsMethod::element_outputs(int p, bool project, double* E, double* g, d
 
 namespace {
 
+// Progressive projection step (NewtonsMethod.cpp:305-329 with
+// ElementHessians::project_to_PD_for_update__selectively, ElementHessians.cpp:69-182): the DoF
+// blocks whose gradient max-abs reaches `thr` are active; every element not projected yet in
+// this evaluation (is_proj cleared when `fresh`) that touches an active block is projected.
+// Sets all_projected when every block is active; returns the number of elements projected.
+template <typename T>
+uint64_t ppn_project(SolverImpl& I, const NewtonSettings& S, cudaStream_t s, double thr, bool fresh,
+                     bool& all_projected)
+{
+    const size_t np = I.pots.size();
+    if (I.ppn_is_proj.n != (size_t)std::max<int64_t>(1, I.n_elements_total)) {
+        I.ppn_is_proj.alloc(std::max<int64_t>(1, I.n_elements_total));
+        I.ppn_sel.alloc(std::max<int64_t>(1, I.n_elements_total));
+        I.ppn_gflag.alloc(std::max<int64_t>(1, I.n_gblocks));
+        fresh = true;
+    }
+    I.ppn_counts.alloc(1 + np);
+    if (fresh) ck(cudaMemsetAsync(I.ppn_is_proj.p, 0, I.ppn_is_proj.n, s), "memset");
+    ck(cudaMemsetAsync(I.ppn_gflag.p, 0, I.ppn_gflag.n, s), "memset");
+    ck(cudaMemsetAsync(I.ppn_counts.p, 0, sizeof(unsigned long long) * (1 + np), s), "memset");
+    symxg::launch_ppn_mark_blocks(I.n_blocks, I.grad.p, thr, I.gptr.p, I.gcontrib.p, I.ppn_gflag.p, I.ppn_counts.p, s);
+    for (size_t k = 0; k < np; ++k) {
+        const auto& cp = I.pots[k];
+        symxg::launch_select_elements(cp.n_elements, cp.nb, I.ppn_gflag.p + cp.g_off, I.ppn_is_proj.p + cp.e_off,
+                                      I.ppn_sel.p + cp.e_off, I.ppn_counts.p + 1 + k, s);
+    }
+    std::vector<unsigned long long> counts(1 + np);
+    ck(cudaMemcpyAsync(counts.data(), I.ppn_counts.p, sizeof(unsigned long long) * (1 + np), cudaMemcpyDeviceToHost, s),
+       "copy counts");
+    ck(cudaStreamSynchronize(s), "synchronize");
+    all_projected = counts[0] == 0;
+    uint64_t total = 0;
+    for (size_t k = 0; k < np; ++k) {
+        const auto& cp = I.pots[k];
+        const int64_t n = (int64_t)counts[1 + k];
+        if (n > 0)
+            symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, n, (T)S.projection_eps,
+                                        S.project_to_pd_use_mirroring, I.flags.p, s, I.proj_scratch(),
+                                        I.ppn_sel.p + cp.e_off);
+        total += (uint64_t)n;
+    }
+    return total;
+}
+
 template <typename T>
 SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int verbosity)
 {
@@ -1157,8 +1201,6 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     if constexpr (std::is_same<T, float>::value) B.staged = I.staged;
     T* du = V[0].p;
 
-    if (S.projection_mode != ProjectionToPD::ProjectedNewton && S.projection_mode != ProjectionToPD::Newton)
-        throw std::runtime_error("symx_gb300: projection modes ProjectOnDemand/Progressive are not implemented");
     if (S.linear_solver != LinearSolver::BDPCG) throw std::runtime_error("symx_gb300: only the BDPCG linear solver is implemented");
 
     double res0 = std::numeric_limits<double>::max();
@@ -1167,6 +1209,8 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     struct PendingEvent { std::string name; cudaEvent_t a, b; };
     std::vector<PendingEvent> pending_kernel_events;
     int it = -1;
+    int pdn_countdown = 0;        // ProjectOnDemand: iterations left with full projection
+    double ppn_threshold = -1.0;  // Progressive: gradient threshold (-1: not determined yet)
     ck(cudaMemsetAsync(I.flags.p, 0, sizeof(int), s), "memset");
     while (result == SolverReturn::Running) {
         ++it;
@@ -1191,119 +1235,162 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             if (residual < S.residual_tolerance_abs) { result = SolverReturn::Successful; break; }
             if (it > 0 && residual / res0 < S.residual_tolerance_rel) { result = SolverReturn::Successful; break; }
         }
-        // projection and assembly
-        if (S.projection_mode == ProjectionToPD::ProjectedNewton) {
+        // projection, assembly and solve until the direction descends or nothing is left to
+        // project (NewtonsMethod.cpp:133-186; _project_and_assemble :257-341; the adaptive
+        // modes' _increase_projection / _decrease_projection :343-373).  Element Hessians of
+        // this evaluation start unprojected; the global matrix is re-assembled from them after
+        // each projection (the reference adds the projected-minus-original differences instead,
+        // ElementHessians.cpp:258-294: the same matrix up to rounding).
+        uint64_t n_projected_it = 0;
+        bool projected_all = false;
+        bool ppn_cleared = false;
+        double du_dot_grad = 0.0, du_max = 0.0;
+        for (;;) {
+            bool all_projected = false;
             timer.start("project_to_PD");
-            for (auto& cp : I.pots) {
-                cudaEvent_t a = nullptr, b = nullptr;
-                const bool timed = S.time_kernels;
-                if (timed) {
-                    cudaEventCreate(&a);
-                    cudaEventCreate(&b);
-                    cudaEventRecord(a, s);
+            if (S.projection_mode == ProjectionToPD::ProjectedNewton ||
+                (S.projection_mode == ProjectionToPD::ProjectOnDemand && pdn_countdown > 0)) {
+                if (!projected_all) {
+                    for (auto& cp : I.pots) {
+                        cudaEvent_t a = nullptr, b = nullptr;
+                        const bool timed = S.time_kernels;
+                        if (timed) {
+                            cudaEventCreate(&a);
+                            cudaEventCreate(&b);
+                            cudaEventRecord(a, s);
+                        }
+                        symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements,
+                                                    (T)S.projection_eps, S.project_to_pd_use_mirroring, I.flags.p, s,
+                                                    I.proj_scratch());
+                        if (timed) {
+                            cudaEventRecord(b, s);
+                            pending_kernel_events.push_back(
+                                {"project_pd_" + std::to_string(3 * cp.nb) + (sizeof(T) == 4 ? "_f32" : "_f64"), a, b});
+                        }
+                    }
+                    n_projected_it = (uint64_t)I.n_elements_total;
+                    projected_all = true;
                 }
-                symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)S.projection_eps,
-                                            S.project_to_pd_use_mirroring, I.flags.p, s, I.proj_scratch());
-                if (timed) {
-                    cudaEventRecord(b, s);
-                    pending_kernel_events.push_back({"project_pd_" + std::to_string(3 * cp.nb) + (sizeof(T) == 4 ? "_f32" : "_f64"), a, b});
-                }
+                all_projected = true;
+            } else if (S.projection_mode == ProjectionToPD::Progressive && ppn_threshold > 0.0) {
+                if (ppn_threshold < 1e-12) ppn_threshold = 0.0;
+                n_projected_it += ppn_project<T>(I, S, s, ppn_threshold, !ppn_cleared, all_projected);
+                ppn_cleared = true;
             }
             timer.stop();
-            st.n_projected_hessians += (uint64_t)I.n_elements_total;
-        }
-        st.n_hessians += (uint64_t)I.n_elements_total;
-        timer.start("assembly");
-        symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.vstride, s);
-        symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.vstride, I.Dinv<T>(), s);
-        timer.stop();
-        // linear solve: block-Jacobi PCG with the reference's forcing sequence
-        timer.start("linear_system_solve");
-        const double forcing = std::min(1e-2, residual * std::min(0.5, std::sqrt(residual)));
-        PcgState init{};
-        init.abs_tol = std::max(forcing, S.cg_abs_tolerance);
-        init.rel_tol = S.cg_rel_tolerance;
-        init.max_iterations = S.cg_max_iterations;
-        ck(cudaMemcpyAsync(I.pcg_state.p, &init, sizeof(PcgState), cudaMemcpyHostToDevice, s), "pcg state");
-        symxg::launch_pcg_init<T>(B, I.grad.p, s);
-        int launched = 0, chunk = 8;
-        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spmv_ev;
-        bool persistent = false;
-        if constexpr (std::is_same<T, float>::value) persistent = B.staged.persistent != 0;
-        if (persistent) {  // every iteration in one cooperative launch
-            cudaEvent_t a = nullptr, b = nullptr;
-            if (S.time_kernels) {
-                cudaEventCreate(&a);
-                cudaEventCreate(&b);
-                cudaEventRecord(a, s);
-            }
-            if constexpr (std::is_same<T, float>::value) symxg::launch_pcg_solve_persistent(B, s);
-            if (S.time_kernels) cudaEventRecord(b, s);
-            ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
-            ck(cudaStreamSynchronize(s), "synchronize");
-            if (S.time_kernels) {
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, b);
-                auto& kt = st.kernels["pcg_solve_f32"];
-                kt.first += I.h_state->iteration;
-                kt.second += ms * 1e-3;
-                cudaEventDestroy(a);
-                cudaEventDestroy(b);
-            }
-        }
-        while (!persistent) {
-            for (int k = 0; k < chunk; ++k) {
+            timer.start("assembly");
+            symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.vstride, s);
+            symxg::launch_block_jacobi_setup<T>(I.n_blocks, I.diag_slot.p, I.vals<T>(), I.vstride, I.Dinv<T>(), s);
+            timer.stop();
+            // linear solve: block-Jacobi PCG with the reference's forcing sequence
+            timer.start("linear_system_solve");
+            const double forcing = std::min(1e-2, residual * std::min(0.5, std::sqrt(residual)));
+            PcgState init{};
+            init.abs_tol = std::max(forcing, S.cg_abs_tolerance);
+            init.rel_tol = S.cg_rel_tolerance;
+            init.max_iterations = S.cg_max_iterations;
+            ck(cudaMemcpyAsync(I.pcg_state.p, &init, sizeof(PcgState), cudaMemcpyHostToDevice, s), "pcg state");
+            symxg::launch_pcg_init<T>(B, I.grad.p, s);
+            int launched = 0, chunk = 8;
+            std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spmv_ev;
+            bool persistent = false;
+            if constexpr (std::is_same<T, float>::value) persistent = B.staged.persistent != 0;
+            if (persistent) {  // every iteration in one cooperative launch
+                cudaEvent_t a = nullptr, b = nullptr;
                 if (S.time_kernels) {
-                    cudaEvent_t a, b;
                     cudaEventCreate(&a);
                     cudaEventCreate(&b);
                     cudaEventRecord(a, s);
-                    symxg::launch_pcg_spmv<T>(B, launched + k, s);
-                    cudaEventRecord(b, s);
-                    spmv_ev.push_back({a, b});
-                    symxg::launch_pcg_update<T>(B, launched + k, s);
-                } else {
-                    symxg::launch_pcg_iteration<T>(B, launched + k, s);
                 }
-            }
-            launched += chunk;
-            ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
-            ck(cudaStreamSynchronize(s), "synchronize");
-            if (I.h_state->done || launched > S.cg_max_iterations + 1) break;
-            chunk = std::min(chunk * 2, 64);
-        }
-        timer.stop();
-        const PcgState ps = *I.h_state;
-        if (ps.wait_failed) throw std::runtime_error("symx_gb300: a bounded wait in the PCG kernels gave up");
-        if (S.time_kernels) {
-            auto& kt = st.kernels[std::string("pcg_spmv_") + (sizeof(T) == 4 ? "f32" : "f64")];
-            for (size_t k = 0; k < spmv_ev.size(); ++k) {
-                if ((int)k < ps.iteration) {  // launches after convergence returned at once
+                if constexpr (std::is_same<T, float>::value) symxg::launch_pcg_solve_persistent(B, s);
+                if (S.time_kernels) cudaEventRecord(b, s);
+                ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
+                ck(cudaStreamSynchronize(s), "synchronize");
+                if (S.time_kernels) {
                     float ms = 0.f;
-                    cudaEventElapsedTime(&ms, spmv_ev[k].first, spmv_ev[k].second);
-                    kt.first += 1;
+                    cudaEventElapsedTime(&ms, a, b);
+                    auto& kt = st.kernels["pcg_solve_f32"];
+                    kt.first += I.h_state->iteration;
                     kt.second += ms * 1e-3;
+                    cudaEventDestroy(a);
+                    cudaEventDestroy(b);
                 }
-                cudaEventDestroy(spmv_ev[k].first);
-                cudaEventDestroy(spmv_ev[k].second);
             }
+            while (!persistent) {
+                for (int k = 0; k < chunk; ++k) {
+                    if (S.time_kernels) {
+                        cudaEvent_t a, b;
+                        cudaEventCreate(&a);
+                        cudaEventCreate(&b);
+                        cudaEventRecord(a, s);
+                        symxg::launch_pcg_spmv<T>(B, launched + k, s);
+                        cudaEventRecord(b, s);
+                        spmv_ev.push_back({a, b});
+                        symxg::launch_pcg_update<T>(B, launched + k, s);
+                    } else {
+                        symxg::launch_pcg_iteration<T>(B, launched + k, s);
+                    }
+                }
+                launched += chunk;
+                ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
+                ck(cudaStreamSynchronize(s), "synchronize");
+                if (I.h_state->done || launched > S.cg_max_iterations + 1) break;
+                chunk = std::min(chunk * 2, 64);
+            }
+            timer.stop();
+            const PcgState ps = *I.h_state;
+            if (ps.wait_failed) throw std::runtime_error("symx_gb300: a bounded wait in the PCG kernels gave up");
+            if (S.time_kernels) {
+                auto& kt = st.kernels[std::string("pcg_spmv_") + (sizeof(T) == 4 ? "f32" : "f64")];
+                for (size_t k = 0; k < spmv_ev.size(); ++k) {
+                    if ((int)k < ps.iteration) {  // launches after convergence returned at once
+                        float ms = 0.f;
+                        cudaEventElapsedTime(&ms, spmv_ev[k].first, spmv_ev[k].second);
+                        kt.first += 1;
+                        kt.second += ms * 1e-3;
+                    }
+                    cudaEventDestroy(spmv_ev[k].first);
+                    cudaEventDestroy(spmv_ev[k].second);
+                }
+            }
+            st.cg_iterations += ps.iteration;
+            st.cg_iterations_per_newton.push_back(ps.iteration);
+            if (verbosity > 0) std::printf("#CG: %4d | ", ps.iteration);
+            const bool can_project_more = S.projection_mode != ProjectionToPD::Newton && !all_projected;
+            if (!ps.converged && !can_project_more) {
+                result = SolverReturn::LinearSystemSolveFailure;
+                break;
+            }
+            bool descends = false;
+            if (ps.converged) {
+                symxg::launch_dot_rows4<T>(du, I.grad.p, I.n_blocks, I.partials.p, I.tickets.p + 4, I.scalars.p + 2, s);
+                symxg::launch_max_abs_rows4<T>(du, I.n_blocks, I.partials.p, I.tickets.p + 4, I.scalars.p + 3, s);
+                I.read_scalars(4);
+                du_dot_grad = I.h_scalars[2];
+                du_max = I.h_scalars[3];
+                descends = du_dot_grad < 0.0;
+                if (!descends && !can_project_more) {
+                    result = SolverReturn::StepDoesNotDescend;
+                    break;
+                }
+            }
+            if (ps.converged && descends) break;
+            // more projection, then retry
+            if (S.projection_mode == ProjectionToPD::ProjectOnDemand) pdn_countdown = S.project_on_demand_countdown;
+            if (S.projection_mode == ProjectionToPD::Progressive) {
+                if (ppn_threshold < 0.0) ppn_threshold = residual;
+                ppn_threshold *= S.ppn_tightening_factor;
+                // a zero threshold cannot tighten (the reference would retry the same solve
+                // forever): a threshold below 1e-12 projects every element on the next try
+                if (ppn_threshold == 0.0) ppn_threshold = 1e-13;
+            }
+            if (verbosity > 0) std::printf("retrying with more projection | ");
         }
-        st.cg_iterations += ps.iteration;
-        st.cg_iterations_per_newton.push_back(ps.iteration);
-        if (verbosity > 0) std::printf("#CG: %4d | ", ps.iteration);
-        if (!ps.converged) {
-            result = SolverReturn::LinearSystemSolveFailure;
-            break;
-        }
-        symxg::launch_dot_rows4<T>(du, I.grad.p, I.n_blocks, I.partials.p, I.tickets.p + 4, I.scalars.p + 2, s);
-        symxg::launch_max_abs_rows4<T>(du, I.n_blocks, I.partials.p, I.tickets.p + 4, I.scalars.p + 3, s);
-        I.read_scalars(4);
-        const double du_dot_grad = I.h_scalars[2];
-        double du_max = I.h_scalars[3];
-        if (!(du_dot_grad < 0.0)) {
-            result = SolverReturn::StepDoesNotDescend;
-            break;
-        }
+        if (result != SolverReturn::Running) break;
+        st.n_hessians += (uint64_t)I.n_elements_total;
+        st.n_projected_hessians += n_projected_it;
+        if (S.projection_mode == ProjectionToPD::ProjectOnDemand) pdn_countdown--;
+        if (S.projection_mode == ProjectionToPD::Progressive) ppn_threshold *= S.ppn_release_factor;
         if (verbosity > 0) std::printf("du: %.1e | ", du_max);
         if (it >= S.min_iterations && du_max < S.step_tolerance) {
             result = SolverReturn::Successful;

@@ -152,6 +152,10 @@ CONFIGS = {
     # Smaller Hex8 slab (65,536 elements) for kernel profiles.
     "hex8_64x64x16": dict(kind="hex8", cells=(64, 64, 16), h=0.01, perturb=0.0, seed=5,
                           youngs_lognormal_sigma=0.5),
+    # Newton guess compressed to half height (plus a seeded 10% spacing jitter): the
+    # unprojected Hessian is indefinite, so the adaptive projection modes retry and project.
+    "tet4_5c": dict(kind="tet4", cells=(5, 4, 4), h=0.01, perturb=0.0, seed=13, init_compress_y=0.5,
+                    init_perturb=0.1),
     "tet4_32": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.0, seed=3),
     "tet4_40": dict(kind="tet4", cells=(40, 40, 40), h=0.01, perturb=0.0, seed=4),
 }
@@ -187,9 +191,14 @@ def step_problem(name_or_cfg, *, youngs=1e5, poisson=0.3, density=1000.0, dt=1.0
     if cfg.get("perturb", 0.0) > 0.0:
         x0 = x0 + (cfg["perturb"] * h) * (2.0 * uniform01(seed * 1000 + 2, nv * 3) - 1.0).reshape(nv, 3)
     bc_idx = np.nonzero(X[:, 0] <= 1e-12)[0].astype(np.int32)
+    x_init = x0.copy()
+    if cfg.get("init_compress_y", 1.0) != 1.0:
+        x_init[:, 1] *= cfg["init_compress_y"]
+    if cfg.get("init_perturb", 0.0) > 0.0:
+        x_init += (cfg["init_perturb"] * h) * (2.0 * uniform01(seed * 1000 + 4, nv * 3) - 1.0).reshape(nv, 3)
     return dict(
         name=cfg.get("name", name_or_cfg if isinstance(name_or_cfg, str) else "custom"),
-        X=X, x0=x0, v0=v0, x_init=x0.copy(), mass=mass, conn=conn, mu=mu, lam=lam,
+        X=X, x0=x0, v0=v0, x_init=x_init, mass=mass, conn=conn, mu=mu, lam=lam,
         bc_idx=bc_idx, bc_target=X[bc_idx].copy(), dt=float(dt),
         gravity=np.asarray(gravity, dtype=np.float64), k_bc=float(k_bc),
     )

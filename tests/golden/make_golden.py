@@ -15,6 +15,7 @@ Fixtures:
   doc_hessian_kat.npz  the 12x12 NH Hessian printed in docs/source/compilation.md:269-281
   <case>_eval.npz      E, gradient, element Hessians, BCSR triplets at the initial state
   <case>_solve.npz     final positions and iteration counts of NewtonsMethod::solve
+  tet4_5c_modes.npz    NewtonsMethod::solve in each ProjectionToPD mode (indefinite start)
 """
 from __future__ import annotations
 
@@ -180,9 +181,37 @@ def make_case(tmp, case, solve_iters=(1, -1), keep_triplets=True):
     return out, sol
 
 
+MODES = {0: "newton", 1: "projected", 2: "on_demand", 3: "progressive"}
+
+
+def make_modes(tmp, case="tet4_5c"):
+    """NewtonsMethod::solve in each ProjectionToPD mode on a case whose unprojected Hessian is
+    indefinite: final positions, return code, iteration counts and projected-Hessian counts."""
+    p = problems.step_problem(case)
+    pfile = os.path.join(tmp, f"{case}.bin")
+    write_problem(pfile, p)
+    out = {}
+    for mode, tag in MODES.items():
+        sd = os.path.join(tmp, f"{case}_mode{mode}")
+        os.makedirs(sd, exist_ok=True)
+        subprocess.run([HARNESS, "solve", pfile, sd, "1", "-1", "1e-3", str(mode)], check=False, timeout=120,
+                       stdout=open(os.path.join(sd, "log.txt"), "w"))
+        stats = json.load(open(os.path.join(sd, "stats.json")))
+        out[f"x_{tag}"] = np.fromfile(os.path.join(sd, "x_final.bin"), dtype=np.float64).reshape(-1, 3)
+        for k in ("return", "newton_iterations", "cg_iterations", "ls_bt_iterations", "n_hessians",
+                  "n_projected_hessians"):
+            out[f"{k}_{tag}"] = stats[k]
+    np.savez_compressed(os.path.join(HERE, f"{case}_modes.npz"), **out)
+    return out
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -f oracle/Makefile.ref -j8")
+    if sys.argv[1:] == ["modes"]:  # only the projection-mode fixture
+        with tempfile.TemporaryDirectory() as tmp:
+            print(make_modes(tmp))
+        return
     with tempfile.TemporaryDirectory() as tmp:
         rows, out = make_elem(tmp)
         make_project(tmp, out)
@@ -191,6 +220,7 @@ def main():
         make_case(tmp, "tet4_6p")
         make_case(tmp, "hex8_3")
         make_case(tmp, "tet4_10", keep_triplets=False)
+        make_modes(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 

@@ -68,6 +68,26 @@ def test_oracle_problem_matches_reference(golden, case):
     assert np.linalg.norm(x - sol["x_full"]) / np.linalg.norm(sol["x_full"] - p["x0"]) < 1e-10
 
 
+MODES = {0: "newton", 1: "projected", 2: "on_demand", 3: "progressive"}
+REF_TO_ORACLE_RETURN = {0: 0, 5: 4, 7: 5}  # SolverReturn values (solver_utils.h:15-26) -> oracle codes
+
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+def test_oracle_projection_modes_match_reference(golden, mode):
+    """NewtonsMethod::solve in each ProjectionToPD mode from an indefinite start (tet4_5c):
+    the same return code, Newton and CG iterations, Hessian and projected-Hessian counts, and
+    final positions as the reference."""
+    d, tag = golden("tet4_5c_modes"), MODES[mode]
+    p = problems.step_problem("tet4_5c")
+    P = O.Problem(p, 1)
+    st = P.solve(O.default_settings(cg_rel_tolerance=1e-3, projection_mode=mode))
+    assert st["solver_return"] == REF_TO_ORACLE_RETURN[int(d[f"return_{tag}"])]
+    for k in ("newton_iterations", "cg_iterations", "n_hessians", "n_projected_hessians"):
+        assert st[k] == int(d[f"{k}_{tag}"]), k
+    x = P.get_x()
+    assert np.linalg.norm(x - d[f"x_{tag}"]) / np.linalg.norm(d[f"x_{tag}"] - p["x0"]) < 1e-10
+
+
 def test_oracle_pcg_solves_assembled_system():
     import scipy.sparse.linalg as spla
 
@@ -131,7 +151,7 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(capi.EXPORTS) == declared
     for name in declared:
         assert hasattr(lib, name), name
-    assert lib.symxg_abi_version() == 2
+    assert lib.symxg_abi_version() == 3
 
 
 def test_invalid_arguments_are_reported(lib):
@@ -162,6 +182,9 @@ def test_invalid_arguments_are_reported(lib):
     s = capi.NewtonSettings()
     lib.symxg_default_settings(C.byref(s))
     assert s.residual_tolerance_abs == 1e-6 and s.cg_rel_tolerance == 1e-4 and s.max_backtracking_armijo_iterations == 20
+    # projection modes and their parameters: symx::NewtonSettings defaults (solver_utils.h:219-228)
+    assert s.project_to_pd == 1 and s.project_on_demand_countdown == 4
+    assert s.ppn_tightening_factor == 0.5 and s.ppn_release_factor == 2.0
 
 
 # ------------------------------------------------------------------ C++ API

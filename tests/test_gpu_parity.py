@@ -127,6 +127,50 @@ def test_newton_mixed_converges_to_fp64_solution(sg, golden, case):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr - p["x0"]) < 1e-4
 
 
+MODES = {0: "newton", 1: "projected", 2: "on_demand", 3: "progressive"}
+
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+def test_projection_modes_fp64_match_reference(sg, golden, mode):
+    """Every ProjectionToPD mode from an indefinite start (tet4_5c: the Newton guess squeezed
+    to half height), FP64, against the reference: the same return code, Newton iterations and
+    Hessian / projected-Hessian counts, CG iterations within 3 %, positions within 1e-8 of the
+    displacement (plain Newton fails with LinearSystemSolveFailure in its second iteration,
+    as the reference does)."""
+    p, s = make(sg, "tet4_5c")
+    s.set_settings(project_to_pd=mode)
+    st = s.solve()
+    d, tag = golden("tet4_5c_modes"), MODES[mode]
+    assert st["solver_return"] == int(d[f"return_{tag}"])
+    for k in ("newton_iterations", "n_hessians", "n_projected_hessians"):
+        assert st[k] == int(d[f"{k}_{tag}"]), (k, st[k], int(d[f"{k}_{tag}"]))
+    cg = int(d[f"cg_iterations_{tag}"])
+    assert abs(st["cg_iterations"] - cg) <= 2 + 0.03 * cg
+    x, xr = s.get_positions(), d[f"x_{tag}"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr - p["x0"]) < 1e-8
+
+
+@pytest.mark.parametrize("mode", [2, 3])
+def test_projection_modes_mixed_converge(sg, golden, mode):
+    """The adaptive modes in mixed precision: converged, fewer Hessians projected than
+    evaluated, positions within 1e-6 relative of the reference's solution in that mode."""
+    p, s = make(sg, "tet4_5c", precision="mixed")
+    s.set_settings(project_to_pd=mode)
+    st = s.solve()
+    assert st["solver_return"] == 0 and st["final_residual"] < 1e-6
+    assert 0 < st["n_projected_hessians"] < st["n_hessians"]
+    x, xr = s.get_positions(), golden("tet4_5c_modes")[f"x_{MODES[mode]}"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
+
+
+def test_unknown_projection_mode_rejected(sg):
+    from symx_gb300.capi import SymxgError
+
+    _, s = make(sg, "tet4_3")
+    with pytest.raises(SymxgError, match="projection mode"):
+        s.set_settings(project_to_pd=4)
+
+
 def test_mixed_element_hessians_within_float_tolerance(sg):
     p, s = make(sg, "tet4_6p", precision="mixed")
     _, _, H32 = s.element_outputs(0, project=False)
