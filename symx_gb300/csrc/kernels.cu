@@ -1134,12 +1134,12 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
             const float* __restrict__ svals = reinterpret_cast<const float*>(st);
             if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
                 // rows of at most 16 blocks: each lane takes at most one block of each row into
-                // registers and the stage is released before the gathers, so the ring slot is
-                // refilled while this warp waits on L2
+                // registers and the stage is released before the gathers are issued (the
+                // arrive's release semantics would wait for them), so the ring slot is refilled
+                // while this warp waits on L2
                 const int kA = kbA + lane16, kB = kbB + lane16;
                 const bool hA = kA < keA, hB = kB < keB;
                 const int cA = hA ? scols[kA] : 0, cB = hB ? scols[kB] : 0;
-                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
                 float mA[9], mB[9];
 #pragma unroll
                 for (int m = 0; m < 9; ++m) {
@@ -1148,6 +1148,7 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
                 }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
                 a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
                 a[1] = mA[3] * xA.x + mA[4] * xA.y + mA[5] * xA.z;
                 a[2] = mA[6] * xA.x + mA[7] * xA.y + mA[8] * xA.z;
@@ -1330,9 +1331,9 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
         const float* __restrict__ z = B.z;
         auto pv = [z, p_old, beta, first](int c) { return direction_cg(z, p_old, beta, first, c); };
         const int n = B.n_blocks;
-        // p.q of the last chunk, published while the next chunk's gathers are in flight:
-        // warp sum in a fixed tree, then the last warp of the block to publish a chunk adds
-        // the 15 warp sums in warp order and stores the chunk's partial
+        // p.q of the last chunk, published during the next stage: warp sum in a fixed tree,
+        // then the last warp of the block to publish a chunk adds the 15 warp sums in warp
+        // order and stores the chunk's partial
         FF pend{0.f, 0.f};
         int pend_c = -1;
         unsigned pend_ps = 0;
@@ -1374,14 +1375,8 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
             const int r0 = c * S;
             const int rowA = r0 + la, rowB = r0 + lb;
             const bool vA = rowA < n, vB = rowB < n;
-            // this lane's own component: its loads go out with the gathers below
             const bool own = owner && (idx < 3 ? vA : vB);
             const int64_t o = 4 * (int64_t)(idx < 3 ? rowA : rowB) + idx % 3;
-            float zo = 0.f, po = 0.f;
-            if (own) {
-                zo = __ldcg(z + o);
-                if (!first) po = __ldcg(p_old + o);
-            }
             const unsigned char* st = ss.stage0 + s * stage_bytes;
             const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
             const int kb4 = rp[0] & ~3;
@@ -1390,13 +1385,16 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
             const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
             const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
             const float* __restrict__ svals = reinterpret_cast<const float*>(st);
+            // The slot release (an mbarrier arrive, release semantics) and the partial's
+            // publication (a block-scope fence) wait for this thread's outstanding memory
+            // operations, so both go before any global load of this stage is issued.
+            float zo = 0.f, po = 0.f;
             if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
                 // rows of at most 16 blocks: each lane takes at most one block of each row into
-                // registers and the stage is released before the gathers
+                // registers, releases the stage, then gathers
                 const int kA = kbA + lane16, kB = kbB + lane16;
                 const bool hA = kA < keA, hB = kB < keB;
                 const int cA = hA ? scols[kA] : 0, cB = hB ? scols[kB] : 0;
-                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
                 float mA[9], mB[9];
 #pragma unroll
                 for (int m = 0; m < 9; ++m) {
@@ -1405,7 +1403,12 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                 }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
-                if (pend_c >= 0) publish();  // in the shadow of the gathers
+                if (pend_c >= 0) publish();
+                if (own) {
+                    zo = __ldcg(z + o);
+                    if (!first) po = __ldcg(p_old + o);
+                }
+                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
                 a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
                 a[1] = mA[3] * xA.x + mA[4] * xA.y + mA[5] * xA.z;
                 a[2] = mA[6] * xA.x + mA[7] * xA.y + mA[8] * xA.z;
@@ -1417,6 +1420,10 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                 two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, pv, a, b);
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                if (own) {
+                    zo = __ldcg(z + o);
+                    if (!first) po = __ldcg(p_old + o);
+                }
             }
             const float qd = half_warp_transpose_sum<float>(a, b, lane16);
             FF t{0.f, 0.f};
