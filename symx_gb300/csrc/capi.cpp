@@ -152,7 +152,7 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
         if (kv.first.rfind("pcg_spmv", 0) == 0) {
             o->spmv_launches += kv.second.first;
             o->spmv_seconds += kv.second.second;
-        } else if (kv.first.rfind("project_pd", 0) == 0) {
+        } else if (kv.first.rfind("project_pd_12_", 0) == 0) {  // the 12 x 12 (Tet4) launches only
             o->project_launches += kv.second.first;
             o->project_seconds += kv.second.second;
         } else if (kv.first.rfind("pcg_solve", 0) == 0) {

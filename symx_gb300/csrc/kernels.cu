@@ -1329,7 +1329,12 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
         const int idx = lane16 >> 1;                 // epilogue: 0..2 row A, 3..5 row B
         const bool owner = !(lane16 & 1) && idx < 6;  // the lane that finishes one component
         const float* __restrict__ z = B.z;
-        auto pv = [z, p_old, beta, first](int c) { return direction_cg(z, p_old, beta, first, c); };
+        // The pass gathers z only and forms w = A z; the owning lane then sets
+        // p = z + beta p_old and q = w + beta q_old (A p_old = q_old), half the gathered bytes
+        // of forming A (z + beta p_old) directly.  Equal in exact arithmetic; in float the
+        // recursive q differs from A p by rounding carried over iterations, which the outer
+        // Newton loop's FP64 residual corrects like the rest of the FP32 solve's error.
+        auto pv = [z](int c) { return ld4cg(z + 4 * c); };
         const int n = B.n_blocks;
         // p.q of the last chunk, published during the next stage: warp sum in a fixed tree,
         // then the last warp of the block to publish a chunk adds the 15 warp sums in warp
@@ -1388,7 +1393,7 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
             // The slot release (an mbarrier arrive, release semantics) and the partial's
             // publication (a block-scope fence) wait for this thread's outstanding memory
             // operations, so both go before any global load of this stage is issued.
-            float zo = 0.f, po = 0.f;
+            float zo = 0.f, po = 0.f, qo = 0.f;
             if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
                 // rows of at most 16 blocks: each lane takes at most one block of each row into
                 // registers, releases the stage, then gathers
@@ -1406,7 +1411,10 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                 if (pend_c >= 0) publish();
                 if (own) {
                     zo = __ldcg(z + o);
-                    if (!first) po = __ldcg(p_old + o);
+                    if (!first) {
+                        po = __ldcg(p_old + o);
+                        qo = __ldcg(B.q + o);
+                    }
                 }
                 const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
                 a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
@@ -1422,15 +1430,19 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                 if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
                 if (own) {
                     zo = __ldcg(z + o);
-                    if (!first) po = __ldcg(p_old + o);
+                    if (!first) {
+                        po = __ldcg(p_old + o);
+                        qo = __ldcg(B.q + o);
+                    }
                 }
             }
-            const float qd = half_warp_transpose_sum<float>(a, b, lane16);
+            const float wd = half_warp_transpose_sum<float>(a, b, lane16);
             FF t{0.f, 0.f};
             if (own) {
-                const float pd = first ? zo : fmaf(beta, po, zo);  // direction_cg()'s bits
+                const float pd = first ? zo : fmaf(beta, po, zo);
+                const float qd = first ? wd : fmaf(beta, qo, wd);
                 p_new[o] = pd;
-                B.q[o] = qd;
+                B.q[o] = qd;  // only this lane reads and writes component o of q in a pass
                 t = ff_prod(pd, qd);
             }
             pend = t;
