@@ -235,11 +235,12 @@ def run_ours(args):
     spmv_bytes = rf["nnzb"] * (9 * 4 + 4) + (rf["n_block_rows"] + 1) * 4 + 4 * n3 * 4
     n_spmv = sum(x["spmv_launches"] for x in stats)
     t_spmv = sum(x["spmv_seconds"] for x in stats) / max(1, n_spmv)
-    # the one-launch PCG (k_pcg_solve_staged): per iteration the staged SpMV bytes plus the
+    # the one-launch PCG (k_pcg_solve_staged): per iteration the product pass (matrix; z, p_old
+    # and q_old read, p and q written: 5 vectors, as it forms q = A z + beta q_old) plus the
     # update's (read x, r, p, q: 4 x 16 B and Dinv 48 B, write x, r, z: 3 x 16 B per row)
     n_pcg_it = sum(x["pcg_solve_iterations"] for x in stats)
     t_pcg_it = sum(x["pcg_solve_seconds"] for x in stats) / max(1, n_pcg_it)
-    pcg_it_bytes = spmv_bytes + 160 * rf["n_block_rows"]
+    pcg_it_bytes = spmv_bytes + n3 * 4 + 160 * rf["n_block_rows"]
     if n_pcg_it:
         kernel_name = "k_pcg_solve_staged (all PCG iterations in one cooperative launch; unit = one iteration)"
         roof_bytes, roof_t, roof_n, traffic_key = pcg_it_bytes, t_pcg_it, n_pcg_it, "k_pcg_solve_staged per iteration"

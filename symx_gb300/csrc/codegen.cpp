@@ -1,5 +1,7 @@
 #include "codegen.h"
 
+#include <functional>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -62,6 +64,13 @@ struct symxg_df {
     __device__ __forceinline__ void operator*=(const symxg_df& b);
 };
 __device__ __forceinline__ double symxg_to_double(const symxg_df& a) { return (double)a.hi + (double)a.lo; }
+// hoisted values read where they are used: (hi, lo) pairs of the mixed path's cache
+__device__ __forceinline__ symxg_df symxg_ldc_df(const float2* __restrict__ p, long long i)
+{
+    const float2 v = __ldg(p + i);
+    return symxg_df(v.x, v.y);
+}
+__device__ __forceinline__ float symxg_ldc_f(const float2* __restrict__ p, long long i) { return __ldg(&p[i].x); }
 __device__ __forceinline__ symxg_df symxg_df_fast(float a, float b)  // |a| >= |b|
 {
     const float s = __fadd_rn(a, b);
@@ -133,8 +142,10 @@ __device__ __forceinline__ T symxg_powi(T x, int n)
 
 std::string emit_device_function(const Expressions& g, const std::vector<int32_t>& outputs, const std::string& name,
                                  const std::string& T, bool accumulate, OpCount* count,
-                                 const std::unordered_map<int32_t, int32_t>* external)
+                                 const std::unordered_map<int32_t, int32_t>* external, const std::string& sink_macro,
+                                 const std::string& ext_load)
 {
+    std::function<void(int32_t)> emit_sink_;
     auto is_external = [&](int32_t i) { return external && external->count(i) > 0; };
     int32_t top = 0;
     for (int32_t o : outputs) top = std::max(top, o);
@@ -152,7 +163,10 @@ std::string emit_device_function(const Expressions& g, const std::vector<int32_t
         }
     }
     auto ref = [&](int32_t i) -> std::string {
-        if (is_external(i)) return "c[" + std::to_string(external->at(i)) + "]";
+        if (is_external(i)) {
+            if (!ext_load.empty()) return ext_load + "(cq, " + std::to_string(external->at(i)) + "LL * cn)";
+            return "c[" + std::to_string(external->at(i)) + "]";
+        }
         const Node& n = g[i];
         switch (n.op) {
             case Op::Zero: return "(" + T + ")0";
@@ -164,8 +178,35 @@ std::string emit_device_function(const Expressions& g, const std::vector<int32_t
     };
     OpCount oc;
     std::ostringstream s;
-    s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, const " << T
-      << "* __restrict__ c, " << T << "* __restrict__ out)\n{\n";
+    const bool sink = !sink_macro.empty();
+    const std::string cparam =
+        ext_load.empty() ? "const " + T + "* __restrict__ c" : "const float2* __restrict__ cq, long long cn";
+    if (sink)
+        s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, " << cparam << ", "
+          << T << "* __restrict__ out, int lq, bool st)\n{\n";
+    else
+        s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, " << cparam << ", "
+          << T << "* __restrict__ out)\n{\n";
+    // sink mode: every output goes to sink_macro(value, slot, lq, st, out) as soon as its node
+    // is computed, so no output has to stay live to the end
+    std::vector<std::vector<size_t>> slots_of;
+    if (sink) {
+        slots_of.resize(top + 1);
+        for (size_t k = 0; k < outputs.size(); ++k) slots_of[outputs[k]].push_back(k);
+        auto emit_sink = [&](int32_t i) {
+            s << "    { const " << T << " r_ = " << sink_macro << "_SUM(" << ref(i) << ");";
+            for (size_t k : slots_of[i]) s << " " << sink_macro << "_STORE(r_, " << k << ");";
+            s << " }\n";
+        };
+        for (int32_t i = 0; i <= top; ++i) {
+            if (slots_of[i].empty()) continue;
+            const Node& n = g[i];
+            const bool leaf = is_external(i) || n.op == Op::Zero || n.op == Op::One || n.op == Op::Const ||
+                              n.op == Op::Symbol;
+            if (leaf) emit_sink(i);
+        }
+        emit_sink_ = emit_sink;
+    }
     for (int32_t i = 0; i <= top; ++i) {
         if (!need[i] || is_external(i)) continue;
         const Node& n = g[i];
@@ -199,9 +240,11 @@ std::string emit_device_function(const Expressions& g, const std::vector<int32_t
                 break;
         }
         s << "    const " << T << " t" << i << " = " << e << ";\n";
+        if (sink && !slots_of[i].empty()) emit_sink_(i);
     }
-    for (size_t k = 0; k < outputs.size(); ++k)
-        s << "    out[" << k << "] " << (accumulate ? "+=" : "=") << " " << ref(outputs[k]) << ";\n";
+    if (!sink)
+        for (size_t k = 0; k < outputs.size(); ++k)
+            s << "    out[" << k << "] " << (accumulate ? "+=" : "=") << " " << ref(outputs[k]) << ";\n";
     s << "}\n";
     if (count) *count = oc;
     return s.str();

@@ -26,9 +26,17 @@ struct OpCount {
 // ("double" or "float").  Nodes listed in `external` are not computed: they are read as
 // c[slot] (values hoisted out of the kernel).  If `accumulate` is set, outputs are added to
 // `out` instead of assigned (summations).
+// With sink_macro = "M": the function takes (in, c, out, int lq, bool st) and passes each
+// output, as soon as its node is computed, through M_SUM(value) (e.g. a sum over the lanes
+// that evaluate the element's quadrature points) and M_STORE(result, slot) (macros the
+// caller defines; they see lq, st and out); nothing is written to out otherwise.
+// With ext_load = "f": the external values are not passed as an array c but read where they
+// are used, as f(cq, k * cn) from a float2 pointer cq with stride cn (the parameters that
+// replace c), so no per-thread copy of them is made.
 std::string emit_device_function(const Expressions& g, const std::vector<int32_t>& outputs, const std::string& name,
                                  const std::string& T, bool accumulate, OpCount* count = nullptr,
-                                 const std::unordered_map<int32_t, int32_t>* external = nullptr);
+                                 const std::unordered_map<int32_t, int32_t>* external = nullptr,
+                                 const std::string& sink_macro = "", const std::string& ext_load = "");
 
 // Prelude shared by all generated sources: guarded log, integer powers, infinities.
 std::string codegen_prelude();

@@ -115,6 +115,7 @@ struct CompiledPotential {
     DevBuf<int32_t> conn;
     DevBuf<const double*> map_ptrs;
     int n_cache = 0, n_qp = 1;      // hoisted values per element and quadrature point
+    int qp_lanes = 1;               // lanes per element of the mixed E+g+H kernel (one per quadrature point)
     bool cache_df = false;          // the cache holds (hi, lo) float pairs (mixed-precision kernels)
     DevBuf<double> cache;
     int64_t e_off = 0, g_off = 0, h_off = 0;  // offsets: elements, gradient blocks, Hessian blocks
@@ -213,11 +214,34 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
     s << emit_device_function(g, eg, "symxg_eval_eg", "double", acc, oeg, &ext);
     s << emit_device_function(g, h_bm, "symxg_eval_h_f64", "double", acc, oh, &ext);
     s << emit_device_function(g, h_bm, "symxg_eval_h_f32", "float", acc, nullptr, &ext);
+    // Elements with several quadrature points and no activity condition: the mixed E+g+H kernel
+    // gives each point its own lane (NQ lanes per element); every Hessian entry is summed over
+    // the lanes by a butterfly of shuffles as soon as it is computed and stored by one lane, so
+    // no NH-long accumulator array (local memory) is needed.
+    const bool qp_parallel = acc && cond < 0 && NQ <= 32 && (NQ & (NQ - 1)) == 0;
+    cp.qp_lanes = qp_parallel ? NQ : 1;
+    if (qp_parallel) {
+        s << "#define SYMXG_NQ " << NQ << "\n"
+          << "__device__ __forceinline__ float symxg_qsum(float v)\n{\n"
+          << "#pragma unroll\n    for (int o = 1; o < SYMXG_NQ; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);\n"
+          << "    return v;\n}\n"
+          << "__device__ __forceinline__ symxg_df symxg_qsum(symxg_df v)\n{\n"
+          << "#pragma unroll\n    for (int o = 1; o < SYMXG_NQ; o <<= 1)\n"
+          << "        v = v + symxg_df(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));\n"
+          << "    return v;\n}\n"
+          << "#define SYMXG_Q_SUM(v) symxg_qsum(v)\n"
+          << "#define SYMXG_Q_STORE(r, k) do { if (st && lq == (k) % SYMXG_NQ) out[(k)] = (r); } while (0)\n";
+        s << emit_device_function(g, h_bm, "symxg_eval_h_f32_q", "float", false, nullptr, &ext, "SYMXG_Q", "symxg_ldc_f");
+    }
     s << emit_device_function(g, e_only, "symxg_eval_e", "double", acc, oe, &ext);
     if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond", "double", false, nullptr, &ext);
     // mixed precision: energy and gradient in double-float (FP32 pipe), see the prelude
     s << emit_device_function(g, eg, "symxg_eval_eg_df", "symxg_df", acc, nullptr, &ext);
     s << emit_device_function(g, e_only, "symxg_eval_e_df", "symxg_df", acc, nullptr, &ext);
+    // the same reading the hoisted values from the cache where they are used (no per-thread copy)
+    s << emit_device_function(g, eg, "symxg_eval_eg_dfl", "symxg_df", acc, nullptr, &ext, "", "symxg_ldc_df");
+    s << emit_device_function(g, e_only, "symxg_eval_e_dfl", "symxg_df", acc, nullptr, &ext, "", "symxg_ldc_df");
+    s << emit_device_function(g, h_bm, "symxg_eval_h_f32l", "float", acc, nullptr, &ext, "", "symxg_ldc_f");
     if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond_df", "symxg_df", false, nullptr, &ext);
     if (K > 0) s << emit_device_function(g, frontier, "symxg_eval_pre", "double", false, nullptr, nullptr);
     if (sum.n_iterations > 0) {
@@ -381,7 +405,30 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
     const std::string sig_df =
         "(long long n, const int* __restrict__ conn, const double* const* __restrict__ maps, "
         "const double* __restrict__ cache_raw, double* __restrict__ E";
-    {
+    if (qp_parallel) {
+        // lane lq of an element evaluates quadrature point lq (the element of the last group is
+        // repeated past n, without stores, so every lane takes part in the shuffles)
+        s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_egh_df32" << sig_df
+          << ", double* __restrict__ G, float* __restrict__ H)\n{\n";
+        s << "    if (n <= 0) return;\n";
+        s << "    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n";
+        s << "    const int lq = (int)(t % SYMXG_NQ);\n    const bool st = t / SYMXG_NQ < n;\n";
+        s << "    const long long e = st ? t / SYMXG_NQ : n - 1;\n";
+        s << "    const float2* __restrict__ cache = reinterpret_cast<const float2*>(cache_raw);\n";
+        s << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
+        s << "    symxg_df ind[" << NS << "]; float in32[" << NS << "];\n";
+        s << "    for (int i = 0; i < " << NS << "; ++i) { ind[i] = symxg_df(in[i]); in32[i] = ind[i].hi; }\n";
+        s << "    {\n" << set_sum_df("lq");
+        s << "        const float2* __restrict__ cq = cache + (long long)lq * " << K << "LL * n + e;\n";
+        s << "        symxg_df eg[" << (NG + 1) << "];\n";
+        s << "        for (int i = 0; i < " << NG + 1 << "; ++i) eg[i] = symxg_df(0.0);\n";
+        s << "        symxg_eval_eg_dfl(ind, cq, n, eg);\n";
+        s << "#pragma unroll\n        for (int i = 0; i < " << NG + 1 << "; ++i) eg[i] = symxg_qsum(eg[i]);\n";
+        s << "        if (st && lq == 0) E[e] = symxg_to_double(eg[0]);\n";
+        s << "#pragma unroll\n        for (int i = 0; i < " << NG << "; ++i)\n"
+          << "            if (st && lq == i % SYMXG_NQ) G[e * " << NG << "LL + i] = symxg_to_double(eg[1 + i]);\n";
+        s << "        symxg_eval_h_f32_q(in32, cq, n, H + e * " << NH << "LL, lq, st);\n    }\n}\n";
+    } else {
         s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_egh_df32" << sig_df
           << ", double* __restrict__ G, float* __restrict__ H)\n{\n" << head_df();
         std::ostringstream zw;
@@ -395,8 +442,9 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
         } else {
             s << "    { const int q = 0; (void)q;\n";
         }
-        s << set_sum_df("q") << load_cache_df("q");
-        s << "        symxg_eval_eg_df(ind, c, eg);\n        symxg_eval_h_f32(in32, c32, h);\n    }\n";
+        s << set_sum_df("q");
+        s << "        const float2* __restrict__ cq = cache + (long long)q * " << K << "LL * n + e;\n";
+        s << "        symxg_eval_eg_dfl(ind, cq, n, eg);\n        symxg_eval_h_f32l(in32, cq, n, h);\n    }\n";
         s << "    E[e] = symxg_to_double(eg[0]);\n";
         // 16-byte stores where the rows allow it (one element's outputs are contiguous)
         if (NG % 2 == 0)
@@ -418,8 +466,9 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
         s << "    symxg_df ev[1];\n";
         if (acc) s << "    for (int q = 0; q < " << NQ << "; ++q) {\n";
         else s << "    { const int q = 0; (void)q;\n";
-        s << set_sum_df("q") << load_cache_df("q");
-        s << "        symxg_eval_e_df(ind, c, ev);\n    }\n    E[e] = symxg_to_double(ev[0]);\n}\n";
+        s << set_sum_df("q");
+        s << "        const float2* __restrict__ cq = cache + (long long)q * " << K << "LL * n + e;\n";
+        s << "        symxg_eval_e_dfl(ind, cq, n, ev);\n    }\n    E[e] = symxg_to_double(ev[0]);\n}\n";
     }
 
     // energy-only kernel (line search)
@@ -620,7 +669,9 @@ struct SolverImpl {
                 double* G = g_el.p + cp.g_off * 3;
                 void* H = mode == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
                 void* args[] = {&n, &conn, &maps, &cache, &E, &G, &H};
-                cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_df32", dim3(grid), dim3(128), 0, stream, args);
+                const unsigned grid_eh = mode == 1 ? (unsigned)((n * cp.qp_lanes + 127) / 128) : grid;
+                cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_df32", dim3(grid_eh), dim3(128), 0, stream,
+                                  args);
             }
         }
     }

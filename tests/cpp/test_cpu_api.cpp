@@ -153,6 +153,36 @@ static int nvrtc(const char* cache_dir)
         std::printf("mixed kernel: %zu source bytes -> %zu cubin bytes\n", ms[0].size(), cubin.size());
         if (cubin.size() < 1000) { std::printf("FAIL cubin too small\n"); return 1; }
     }
+    // a Hex8 element: eight quadrature points, so the mixed E+g+H kernel takes one lane per point
+    {
+        std::vector<std::array<double, 3>> hx;
+        for (int k = 0; k < 8; ++k) hx.push_back({double(k & 1), double((k >> 1) & 1), double((k >> 2) & 1)});
+        std::vector<std::array<double, 3>> hX = hx;
+        std::vector<int32_t> hexes = {0, 0, 1, 3, 2, 4, 5, 7, 6};
+        std::vector<double> hmu = {1.0}, hlam = {1.0};
+        auto G2 = GlobalPotential::create();
+        G2->add_potential("nh_hex", hexes, 9, [&](MappedWorkspace<double>& mws, Element& e) {
+            std::vector<Vector> xs = mws.make_vectors(hx, e.slice(1, 9));
+            std::vector<Vector> Xs = mws.make_vectors(hX, e.slice(1, 9));
+            Scalar m = mws.make_scalar(hmu, e[0]);
+            Scalar l = mws.make_scalar(hlam, e[0]);
+            return fem_integrator(mws, FEM_Element::Hex8, [&](Scalar& w, Vector& xi) {
+                Matrix F = fem_jacobian(FEM_Element::Hex8, xs, xi) * fem_jacobian(FEM_Element::Hex8, Xs, xi).inv();
+                Scalar lj = log(F.det());
+                return (0.5 * m * (F.frobenius_norm_sq() - 3.0) - m * lj + 0.5 * l * lj.powN(2)) *
+                       fem_jacobian(FEM_Element::Hex8, Xs, xi).det() * w;
+            });
+        });
+        G2->add_dof(hx);
+        const std::vector<std::string> hs = generate_element_kernel_sources(*G2);
+        if (hs.size() != 1 || hs[0].find("symxg_eval_h_f32_q") == std::string::npos) {
+            std::printf("FAIL the Hex8 source has no quadrature-parallel Hessian function\n");
+            return 1;
+        }
+        const std::string cubin = symxg::compile_cubin(hs[0], {});
+        std::printf("hex8 potential: %zu source bytes -> %zu cubin bytes\n", hs[0].size(), cubin.size());
+        if (cubin.size() < 1000) { std::printf("FAIL cubin too small\n"); return 1; }
+    }
     std::printf("nvrtc PASS\n");
     return 0;
 }

@@ -171,8 +171,11 @@ def test_unknown_projection_mode_rejected(sg):
         s.set_settings(project_to_pd=4)
 
 
-def test_mixed_element_hessians_within_float_tolerance(sg):
-    p, s = make(sg, "tet4_6p", precision="mixed")
+@pytest.mark.parametrize("case", ["tet4_6p", "hex8_3"])
+def test_mixed_element_hessians_within_float_tolerance(sg, case):
+    """FP32 element Hessians of the mixed path against the FP64 path (Hex8: summed over the
+    eight quadrature points by the lanes that evaluate them)."""
+    p, s = make(sg, case, precision="mixed")
     _, _, H32 = s.element_outputs(0, project=False)
     s.set_settings(precision="fp64")
     _, _, H64 = s.element_outputs(0, project=False)
