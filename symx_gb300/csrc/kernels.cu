@@ -180,6 +180,45 @@ __global__ void __launch_bounds__(128) k_project_pd_deflated(T* __restrict__ H, 
     if (nc) *not_converged = 1;
 }
 
+// Sorting pass of the 12 x 12 projection: matrices whose deflated part is positive definite
+// are done (left as they are: the projection would only lift their translation eigenvalues
+// to eps); the others are listed, translation-invariant ones in `pending` for
+// k_project_pd_deflated_listed and the rest in `fallback` for k_project_pd_listed (counts
+// zeroed before the launch), so the eigen-decompositions run in full warps.
+template <typename T, int N>
+__global__ void __launch_bounds__(128) k_project_pd_sort(const T* __restrict__ H, int64_t count,
+                                                         int64_t* __restrict__ fallback, unsigned long long* n_fallback,
+                                                         const int64_t* __restrict__ sel, int64_t* __restrict__ pending,
+                                                         unsigned long long* n_pending)
+{
+    constexpr int M = N - 3;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t m = sel ? sel[k] : k;
+    T b[M * (M + 1) / 2];
+    if (!symxg_dev::deflate_translations<T, N / 3>(H + m * (N * N), b)) fallback[atomicAdd(n_fallback, 1ull)] = m;
+    else if (!symxg_dev::positive_definite_by_cholesky<T, M>(b)) pending[atomicAdd(n_pending, 1ull)] = m;
+}
+
+// The deflated eigen-decomposition of the matrices k_project_pd_sort listed as pending
+// (grid-stride over the list).
+template <typename T, int N>
+__global__ void __launch_bounds__(128) k_project_pd_deflated_listed(T* __restrict__ H, const int64_t* __restrict__ list,
+                                                                    const unsigned long long* n_list, T eps,
+                                                                    int mirroring, int* not_converged)
+{
+    constexpr int M = N - 3;
+    const int64_t n = (int64_t)*n_list;
+    int nc = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        T* h = H + list[k] * (N * N);
+        T b[M * (M + 1) / 2];
+        if (symxg_dev::deflate_translations<T, N / 3>(h, b))
+            symxg_dev::project_deflated_finish<T, N / 3>(h, b, eps, mirroring != 0, &nc);
+    }
+    if (nc) *not_converged = 1;
+}
+
 // Full projection of the matrices listed by k_project_pd_deflated (grid-stride over the list).
 template <typename T, int N>
 __global__ void __launch_bounds__(128) k_project_pd_listed(T* __restrict__ H, const int64_t* __restrict__ list,
@@ -1999,11 +2038,28 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
 {
     if (count <= 0) return;
     if (N == 12 && scratch.fallback && scratch.n_fallback) {
+        const bool split = scratch.pending && scratch.n_pending;
         const cudaError_t e = cudaMemsetAsync(scratch.n_fallback, 0, sizeof(unsigned long long), s);
         if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
-        k_project_pd_deflated<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged,
-                                                                              scratch.fallback, scratch.n_fallback, sel);
-        check_launch("project_pd_deflated");
+        if (split) {
+            const cudaError_t e2 = cudaMemsetAsync(scratch.n_pending, 0, sizeof(unsigned long long), s);
+            if (e2 != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e2));
+        }
+        if (split) {
+            k_project_pd_sort<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, scratch.fallback, scratch.n_fallback,
+                                                                           sel, scratch.pending, scratch.n_pending);
+            check_launch("project_pd_sort");
+        } else {
+            k_project_pd_deflated<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged,
+                                                                                  scratch.fallback, scratch.n_fallback, sel);
+            check_launch("project_pd_deflated");
+        }
+        if (split) {
+            static const unsigned pending_grid = resident_grid(k_project_pd_deflated_listed<T, 12>, 128);
+            k_project_pd_deflated_listed<T, 12><<<pending_grid, 128, 0, s>>>(H, scratch.pending, scratch.n_pending, eps,
+                                                                           mirroring, not_converged);
+            check_launch("project_pd_deflated_listed");
+        }
         static const unsigned listed_grid = resident_grid(k_project_pd_listed<T, 12>, 128);
         k_project_pd_listed<T, 12><<<listed_grid, 128, 0, s>>>(H, scratch.fallback, scratch.n_fallback, eps, mirroring,
                                                                not_converged);

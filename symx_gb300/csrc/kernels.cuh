@@ -49,9 +49,14 @@ void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, 
 // matrices are projected in the 9-dimensional complement of the rigid translations and the
 // others with the full decomposition in a second launch; without it, every matrix takes the
 // full decomposition.
+// 12 x 12 projection lists (each sized for every matrix of one launch): matrices that are not
+// translation-invariant (full decomposition), and, when given, translation-invariant ones
+// whose deflated part is not positive definite (deflated decomposition in full warps).
 struct ProjectionScratch {
     int64_t* fallback = nullptr;
     unsigned long long* n_fallback = nullptr;
+    int64_t* pending = nullptr;
+    unsigned long long* n_pending = nullptr;
 };
 // sel: when given, project the `count` matrices H[sel[k]] instead of H[0 .. count).
 template <typename T>

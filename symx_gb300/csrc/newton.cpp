@@ -559,8 +559,8 @@ struct SolverImpl {
     DevBuf<PcgState> pcg_state;
     DevBuf<int> flags;
     // projection: indices of the 12 x 12 element Hessians that need the full decomposition
-    DevBuf<int64_t> proj_fallback;
-    DevBuf<unsigned long long> proj_n_fallback;
+    DevBuf<int64_t> proj_fallback, proj_pending;
+    DevBuf<unsigned long long> proj_n_fallback, proj_n_pending;
     // Progressive projection: per element "projected in this evaluation", per element gradient
     // block "touches an active DoF block", the selected elements of one potential, and counters
     // (inactive DoF blocks, then the selection count of each potential)
@@ -572,6 +572,8 @@ struct SolverImpl {
         symxg::ProjectionScratch ps;
         ps.fallback = proj_fallback.p;
         ps.n_fallback = proj_n_fallback.p;
+        ps.pending = proj_pending.p;
+        ps.n_pending = proj_n_pending.p;
         return ps;
     }
     // adjoint: mixed-derivative modules per (potential, data map), lambda on the device
@@ -977,6 +979,8 @@ NewtonsMethod::NewtonsMethod(spGlobalPotential G, spContext ctx)
         if (n12 > 0) {
             I.proj_fallback.alloc(n12);
             I.proj_n_fallback.alloc(1);
+            I.proj_pending.alloc(n12);
+            I.proj_n_pending.alloc(1);
         }
     }
     ck(cudaMallocHost(&I.h_scalars, sizeof(double) * 16), "pinned");

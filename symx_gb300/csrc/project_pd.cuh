@@ -393,8 +393,49 @@ SYMXG_DEVICE T helmert(const T (&c)[NB], int i, int m)
     return i < m ? c[m] : (i == m ? -T(m) * c[m] : T(0));
 }
 
+// True when the symmetric M x M matrix b (upper triangle) has a Cholesky factorization whose
+// pivots all exceed 16 M u of its largest diagonal entry (u the unit roundoff of T): it is
+// then positive definite up to rounding, with every eigenvalue above -(rounding of b).
+template <typename T>
+struct UnitRoundoff;
+template <>
+struct UnitRoundoff<float> {
+    static SYMXG_DEVICE float value() { return 5.9604645e-8f; }  // 2^-24
+};
+template <>
+struct UnitRoundoff<double> {
+    static SYMXG_DEVICE double value() { return 1.1102230246251565e-16; }  // 2^-53
+};
+template <typename T, int M>
+SYMXG_DEVICE bool positive_definite_by_cholesky(const T (&b)[M * (M + 1) / 2])
+{
+    T dmax = T(0);
+#pragma unroll
+    for (int i = 0; i < M; ++i) dmax = fmax(dmax, b[tri<M>(i, i)]);
+    const T tau = T(16 * M) * UnitRoundoff<T>::value() * dmax;
+    T u[M * (M + 1) / 2];  // U = L^T: u(k, i) = L(i, k), k <= i
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        T d = b[tri<M>(j, j)];
+#pragma unroll
+        for (int k = 0; k < j; ++k) d -= u[tri<M>(k, j)] * u[tri<M>(k, j)];
+        if (!(d > tau)) return false;
+        const T r = T(1) / sqrt(d);
+#pragma unroll
+        for (int i = j + 1; i < M; ++i) {
+            T x = b[tri<M>(j, i)];
+#pragma unroll
+            for (int k = 0; k < j; ++k) x -= u[tri<M>(k, i)] * u[tri<M>(k, j)];
+            u[tri<M>(j, i)] = x * r;
+        }
+    }
+    return true;
+}
+
+// b = Q^T H Q (upper triangle) of a translation-invariant H; returns false (b unset) when the
+// translation residual max |H t| exceeds tol * max |H|.
 template <typename T, int NB>
-SYMXG_DEVICE int project_pd_deflated(T* __restrict__ H, T eps, bool mirroring, int* not_converged)
+SYMXG_DEVICE bool deflate_translations(const T* __restrict__ H, T (&b)[(3 * NB - 3) * (3 * NB - 2) / 2])
 {
     constexpr int N = 3 * NB;
     constexpr int M = N - 3;
@@ -402,46 +443,58 @@ SYMXG_DEVICE int project_pd_deflated(T* __restrict__ H, T eps, bool mirroring, i
     c[0] = T(0);
 #pragma unroll
     for (int m = 1; m < NB; ++m) c[m] = T(1) / sqrt(T(m * (m + 1)));
-    T b[M * (M + 1) / 2];
-    {
-        T a[N * (N + 1) / 2];
-        T hmax = T(0);
+    T a[N * (N + 1) / 2];
+    T hmax = T(0);
 #pragma unroll
-        for (int i = 0; i < N; ++i)
+    for (int i = 0; i < N; ++i)
 #pragma unroll
-            for (int j = i; j < N; ++j) {
-                a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
-                hmax = fmax(hmax, fabs(a[tri<N>(i, j)]));
+        for (int j = i; j < N; ++j) {
+            a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
+            hmax = fmax(hmax, fabs(a[tri<N>(i, j)]));
+        }
+    // translation residual: (H t_e) at row (i, d), up to the factor 1/sqrt(NB)
+    T res = T(0);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            T r = T(0);
+#pragma unroll
+            for (int jn = 0; jn < NB; ++jn) r += a[tri<N>(i, 3 * jn + e)];
+            res = fmax(res, fabs(r));
+        }
+    if (!(res <= DeflationTol<T>::value() * hmax)) return false;
+    // b = Q^T H Q (upper triangle), row (m, d) of b = row 3 (m - 1) + d
+#pragma unroll
+    for (int p = 0; p < M; ++p)
+#pragma unroll
+        for (int q = p; q < M; ++q) {
+            const int m = p / 3 + 1, d = p % 3, l = q / 3 + 1, e = q % 3;
+            T s = T(0);
+#pragma unroll
+            for (int i = 0; i <= m; ++i) {
+                T t = T(0);
+#pragma unroll
+                for (int j = 0; j <= l; ++j) t += helmert<T, NB>(c, j, l) * a[tri<N>(3 * i + d, 3 * j + e)];
+                s += helmert<T, NB>(c, i, m) * t;
             }
-        // translation residual: (H t_e) at row (i, d), up to the factor 1/sqrt(NB)
-        T res = T(0);
+            b[tri<M>(p, q)] = s;
+        }
+    return true;
+}
+
+// Eigen-decomposition of b = Q^T H Q, clamping, and H = Q W Q^T + lam_t / NB (1 1^T (x) I3).
+// Returns 1 when H changed.
+template <typename T, int NB>
+SYMXG_DEVICE int project_deflated_finish(T* __restrict__ H, T (&b)[(3 * NB - 3) * (3 * NB - 2) / 2], T eps,
+                                         bool mirroring, int* not_converged)
+{
+    constexpr int N = 3 * NB;
+    constexpr int M = N - 3;
+    T c[NB];
+    c[0] = T(0);
 #pragma unroll
-        for (int i = 0; i < N; ++i)
-#pragma unroll
-            for (int e = 0; e < 3; ++e) {
-                T r = T(0);
-#pragma unroll
-                for (int jn = 0; jn < NB; ++jn) r += a[tri<N>(i, 3 * jn + e)];
-                res = fmax(res, fabs(r));
-            }
-        if (!(res <= DeflationTol<T>::value() * hmax)) return -1;
-        // b = Q^T H Q (upper triangle), row (m, d) of b = row 3 (m - 1) + d
-#pragma unroll
-        for (int p = 0; p < M; ++p)
-#pragma unroll
-            for (int q = p; q < M; ++q) {
-                const int m = p / 3 + 1, d = p % 3, l = q / 3 + 1, e = q % 3;
-                T s = T(0);
-#pragma unroll
-                for (int i = 0; i <= m; ++i) {
-                    T t = T(0);
-#pragma unroll
-                    for (int j = 0; j <= l; ++j) t += helmert<T, NB>(c, j, l) * a[tri<N>(3 * i + d, 3 * j + e)];
-                    s += helmert<T, NB>(c, i, m) * t;
-                }
-                b[tri<M>(p, q)] = s;
-            }
-    }
+    for (int m = 1; m < NB; ++m) c[m] = T(1) / sqrt(T(m * (m + 1)));
     T v[M * M];
 #pragma unroll
     for (int i = 0; i < M; ++i)
@@ -498,6 +551,20 @@ SYMXG_DEVICE int project_pd_deflated(T* __restrict__ H, T eps, bool mirroring, i
             H[bm_index<N>(j, i)] = s;
         }
     return 1;
+}
+
+// Q^T H Q positive definite (the usual case for an elastic element near its rest shape): the
+// projection keeps its eigenvalues and only lifts the three translation eigenvalues from 0 to
+// eps (the term eps / NB (1 1^T (x) I3)), a change far below the rounding of H's entries, so
+// H is left as it is and the eigen-decomposition is skipped.
+template <typename T, int NB>
+SYMXG_DEVICE int project_pd_deflated(T* __restrict__ H, T eps, bool mirroring, int* not_converged)
+{
+    constexpr int M = 3 * NB - 3;
+    T b[M * (M + 1) / 2];
+    if (!deflate_translations<T, NB>(H, b)) return -1;
+    if (positive_definite_by_cholesky<T, M>(b)) return 0;
+    return project_deflated_finish<T, NB>(H, b, eps, mirroring, not_converged);
 }
 
 }  // namespace symxg_dev
