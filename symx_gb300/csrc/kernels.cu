@@ -442,6 +442,77 @@ __device__ __forceinline__ double row_dot(const double (&w)[N], const double* ro
     return acc;
 }
 
+template <typename T>
+__device__ __forceinline__ T warp_allmax(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Warp test of one N x N element Hessian A (shared memory, row stride N + 1): true when A is
+// translation-invariant (max |A t| <= tol max |A|) and Q^T A Q (Q the Helmert basis of the
+// node space orthogonal to (1, ..., 1), (x) I3) has a Cholesky factorization with pivots above
+// 16 M u of its largest diagonal entry.  A is then positive definite in the complement of the
+// translations up to rounding, and the reference's projection would only lift the three
+// translation eigenvalues from 0 to eps, a change below the rounding of A's entries.  B (the
+// same shape) is scratch; every decision is taken by all lanes alike.
+template <typename T, int N>
+__device__ bool pairs_pd_shortcut(const T* __restrict__ A, T* __restrict__ B, int lane)
+{
+    constexpr int LD = N + 1, NB = N / 3, M = N - 3;
+    // rows of A Q (lane i < N: row i): prefix sums over the node blocks; the full sums are
+    // the translation residual of the row
+    T amax = T(0), res = T(0);
+    if (lane < N) {
+        T acc[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int m = 0; m < NB; ++m)
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const T a = A[lane * LD + 3 * m + e];
+                amax = fmax(amax, fabs(a));
+                if (m >= 1) B[lane * LD + 3 * (m - 1) + e] = (acc[e] - T(m) * a) / sqrt(T(m * (m + 1)));
+                acc[e] += a;
+            }
+        res = fmax(fabs(acc[0]), fmax(fabs(acc[1]), fabs(acc[2])));
+    }
+    amax = warp_allmax(amax);
+    res = warp_allmax(res);
+    if (!(res <= symxg_dev::DeflationTol<T>::value() * amax)) return false;
+    __syncwarp();
+    // columns of Q^T (A Q) (lane c < M: column c), written over rows 0 .. M-1 of the same column
+    if (lane < M) {
+        T acc[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int m = 0; m < NB; ++m)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const T t = B[(3 * m + d) * LD + lane];
+                if (m >= 1) B[(3 * (m - 1) + d) * LD + lane] = (acc[d] - T(m) * t) / sqrt(T(m * (m + 1)));
+                acc[d] += t;
+            }
+    }
+    __syncwarp();
+    // Cholesky (lower triangle, in place): lane i holds row i
+    const T dmax = warp_allmax(lane < M ? B[lane * LD + lane] : T(0));
+    const T tau = T(16 * M) * symxg_dev::UnitRoundoff<T>::value() * dmax;
+    for (int j = 0; j < M; ++j) {
+        const T d = B[j * LD + j];  // the same value in every lane
+        if (!(d > tau)) return false;
+        const T r = T(1) / sqrt(d);
+        const bool mine = lane > j && lane < M;
+        const T lij = mine ? B[lane * LD + j] * r : T(0);
+        __syncwarp();
+        if (mine) B[lane * LD + j] = lij;
+        __syncwarp();
+        if (mine)
+            for (int k = j + 1; k <= lane; ++k) B[lane * LD + k] -= lij * B[k * LD + j];
+        __syncwarp();
+    }
+    return true;
+}
+
 template <typename T, int N>
 __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::min_blocks)
     k_project_pd_pairs(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged,
@@ -452,6 +523,7 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
     constexpr int W = ProjPairsCfg<T>::warps;
     constexpr int LD = N + 1, NP = N / 2, NR = N - 1, NOFF = NP * (NP - 1) / 2, SLOTS = (NOFF + 31) / 32, nb = N / 3;
     __shared__ __align__(16) T sA[W][N * LD];
+    __shared__ __align__(16) T sB[W][N * LD];  // deflated copy for the positive-definiteness test
     __shared__ __align__(16) T2 sCS[W][NP];  // (c, s) of the round's rotations
     __shared__ uint2 sTab[NR][SLOTS][32];     // per round, slot and lane: 4 x 16-bit entry offsets
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -489,6 +561,8 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
             A[i * LD + j] = v;
             f += v * v;
         }
+        __syncwarp();
+        if (pairs_pd_shortcut<T, N>(A, sB[w], lane)) continue;  // H stays as it is
         T v[N];
 #pragma unroll
         for (int s = 0; s < N; ++s) v[s] = lane == slot_index<N>(s) ? T(1) : T(0);
