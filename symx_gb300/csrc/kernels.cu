@@ -1536,6 +1536,36 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                 b[0] = mB[0] * xB.x + mB[1] * xB.y + mB[2] * xB.z;
                 b[1] = mB[3] * xB.x + mB[4] * xB.y + mB[5] * xB.z;
                 b[2] = mB[6] * xB.x + mB[7] * xB.y + mB[8] * xB.z;
+            } else if (__all_sync(0xffffffffu, keA - kbA <= 32 && keB - kbB <= 32)) {
+                // rows of at most 32 blocks (Hex8: 27): two blocks of each row per lane, the four
+                // gathers issued together, values read from the stage after they arrive (the
+                // stage is released after the products)
+                if (pend_c >= 0) publish();
+                const int kA0 = kbA + lane16, kA1 = kA0 + 16, kB0 = kbB + lane16, kB1 = kB0 + 16;
+                const bool hA0 = kA0 < keA, hA1 = kA1 < keA, hB0 = kB0 < keB, hB1 = kB1 < keB;
+                const Row4<float> xA0 = hA0 ? pv(scols[kA0]) : Row4<float>{}, xA1 = hA1 ? pv(scols[kA1]) : Row4<float>{};
+                const Row4<float> xB0 = hB0 ? pv(scols[kB0]) : Row4<float>{}, xB1 = hB1 ? pv(scols[kB1]) : Row4<float>{};
+                auto prod = [&](int k, bool h, const Row4<float>& x, float (&acc)[3]) {
+                    if (!h) return;
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+                        acc[r] += svals[(3 * r) * CAP + k] * x.x + svals[(3 * r + 1) * CAP + k] * x.y +
+                                  svals[(3 * r + 2) * CAP + k] * x.z;
+                };
+                a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = 0.0f;
+                prod(kA0, hA0, xA0, a);
+                prod(kA1, hA1, xA1, a);
+                prod(kB0, hB0, xB0, b);
+                prod(kB1, hB1, xB1, b);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                if (own) {
+                    zo = __ldcg(z + o);
+                    if (!first) {
+                        po = __ldcg(p_old + o);
+                        qo = __ldcg(B.q + o);
+                    }
+                }
             } else {
                 if (pend_c >= 0) publish();
                 two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, pv, a, b);

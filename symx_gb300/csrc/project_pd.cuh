@@ -432,6 +432,41 @@ SYMXG_DEVICE bool positive_definite_by_cholesky(const T (&b)[M * (M + 1) / 2])
     return true;
 }
 
+// Upper triangle of the symmetric block-major matrix H into a, and max |entry| into hmax.  A
+// 16-byte aligned float matrix is read with 16-byte loads in storage order (N * N / 4 of
+// them instead of N (N + 1) / 2 scalar loads).
+template <typename T, int N>
+SYMXG_DEVICE void load_upper(const T* __restrict__ H, T (&a)[N * (N + 1) / 2], T& hmax)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4 && (N * N) % 4 == 0) {
+        if ((reinterpret_cast<unsigned long long>(H) & 15ull) == 0ull) {
+            const float4* H4 = reinterpret_cast<const float4*>(H);
+#pragma unroll
+            for (int q = 0; q < N * N / 4; ++q) {
+                const float4 v = __ldg(H4 + q);
+                const T vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int idx = 4 * q + t, blk = idx / 9, r = idx % 9;
+                    const int i = (blk / (N / 3)) * 3 + r / 3, j = (blk % (N / 3)) * 3 + r % 3;
+                    if (i <= j) a[tri<N>(i, j)] = vv[t];
+                    hmax = fmax(hmax, fabs(vv[t]));
+                }
+            }
+            return;
+        }
+    }
+#endif
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j) {
+            a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
+            hmax = fmax(hmax, fabs(a[tri<N>(i, j)]));
+        }
+}
+
 // b = Q^T H Q (upper triangle) of a translation-invariant H; returns false (b unset) when the
 // translation residual max |H t| exceeds tol * max |H|.
 template <typename T, int NB>
@@ -445,13 +480,7 @@ SYMXG_DEVICE bool deflate_translations(const T* __restrict__ H, T (&b)[(3 * NB -
     for (int m = 1; m < NB; ++m) c[m] = T(1) / sqrt(T(m * (m + 1)));
     T a[N * (N + 1) / 2];
     T hmax = T(0);
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = i; j < N; ++j) {
-            a[tri<N>(i, j)] = H[bm_index<N>(i, j)];
-            hmax = fmax(hmax, fabs(a[tri<N>(i, j)]));
-        }
+    load_upper<T, N>(H, a, hmax);
     // translation residual: (H t_e) at row (i, d), up to the factor 1/sqrt(NB)
     T res = T(0);
 #pragma unroll
