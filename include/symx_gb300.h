@@ -61,7 +61,7 @@ typedef struct symxg_solver symxg_solver;
 typedef struct symxg_elastic_problem {
     int32_t n_vertices;
     int32_t n_elements;
-    int32_t nodes_per_element;     /* 4 (Tet4) or 8 (Hex8) */
+    int32_t nodes_per_element;     /* 4 (Tet4), 10 (Tet10) or 8 (Hex8) */
     const int32_t* connectivity;   /* n_elements * nodes_per_element */
     const double* rest_positions;  /* n_vertices * 3 */
     const double* mu;              /* n_elements Lame mu */
@@ -173,7 +173,7 @@ int64_t symxg_launch_count(void);
 
 /* ---- stand-alone kernels on caller-owned DEVICE memory (stream: a cudaStream_t or NULL) ---- */
 
-/* Project `count` symmetric n x n matrices (n = 3k <= 24), stored block-major (3x3 block
+/* Project `count` symmetric n x n matrices (n = 3k <= 30), stored block-major (3x3 block
  * (a,b) at offset (a*k+b)*9, row-major inside), in place.  not_converged: device int set
  * to 1 if a Jacobi sweep cap was hit.  Replaces project_to_PD_inplace
  * (symx/src/solver/second_order/project_to_PD.cpp:12-81). */

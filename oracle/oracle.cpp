@@ -89,6 +89,26 @@ Rule make_rule(int nodes)
     if (nodes == 4) {
         r.w = {1.0 / 6.0};
         r.dNdxi = {{-1, -1, -1, 1, 0, 0, 0, 1, 0, 0, 0, 1}};
+    } else if (nodes == 10) {
+        // quadratic tetrahedron (fem_integrators.h:56-76), 4-point rule with the reference's
+        // rounded weights and points (fem_integrators.cpp:60-68)
+        const double w = 0.041666667, a = 0.58541020, b = 0.13819660;
+        const double pts[4][3] = {{a, b, b}, {b, a, b}, {b, b, a}, {b, b, b}};
+        for (int q = 0; q < 4; ++q) {
+            const double x0 = pts[q][0], x1 = pts[q][1], x2 = pts[q][2];
+            const double n[4] = {1.0 - x0 - x1 - x2, x0, x1, x2};
+            const double dn[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};  // d n_i / d xi_k
+            const int edge[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+            std::vector<double> d(30);
+            for (int c = 0; c < 4; ++c)
+                for (int k = 0; k < 3; ++k) d[3 * c + k] = (4.0 * n[c] - 1.0) * dn[c][k];
+            for (int m = 0; m < 6; ++m) {
+                const int i = edge[m][0], j = edge[m][1];
+                for (int k = 0; k < 3; ++k) d[3 * (4 + m) + k] = 4.0 * (dn[i][k] * n[j] + n[i] * dn[j][k]);
+            }
+            r.w.push_back(w);
+            r.dNdxi.push_back(d);
+        }
     } else {
         const double p = 1.0 / std::sqrt(3.0);
         const double s[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
@@ -405,7 +425,7 @@ double evaluate(Problem& P, double* grad, bool want_hess, double* t_eval)
     if (want_hess) P.Hel.resize((size_t)P.ne * n * n);
 #pragma omp parallel for schedule(static) num_threads(P.n_threads)
     for (int e = 0; e < P.ne; ++e) {
-        double xe[24], Xe[24];
+        double xe[30], Xe[30];
         for (int a = 0; a < nn; ++a)
             for (int d = 0; d < 3; ++d) {
                 xe[3 * a + d] = P.x[3 * P.conn[e * nn + a] + d];
@@ -697,7 +717,7 @@ int oracle_num_threads(void)
 int oracle_nh_element_batch(int nodes, int n, const double* x, const double* X, const double* mu,
                             const double* lam, double* E, double* g, double* H)
 {
-    if (nodes != 4 && nodes != 8) return 1;
+    if (nodes != 4 && nodes != 8 && nodes != 10) return 1;
     const Rule rule = make_rule(nodes);
     const int m = 3 * nodes;
 #pragma omp parallel for schedule(static)
@@ -722,7 +742,7 @@ void* oracle_create(int nv, int ne, int nodes, const int32_t* conn, const double
                     int nbc, const int32_t* bc_idx, const double* bc_target, double dt, const double* gravity,
                     double k_bc, int n_threads)
 {
-    if (nodes != 4 && nodes != 8) return nullptr;
+    if (nodes != 4 && nodes != 8 && nodes != 10) return nullptr;
     Problem* P = new Problem();
     P->nv = nv; P->ne = ne; P->nodes = nodes; P->nbc = nbc;
     P->n_threads = n_threads > 0 ? n_threads : oracle_num_threads();

@@ -113,7 +113,7 @@ std::vector<int> numbered_connectivity(const Problem& p)
 
 spGlobalPotential build_global_potential(Problem& p, std::vector<int>& numbered)
 {
-    const FEM_Element type = (p.nodes == 4) ? FEM_Element::Tet4 : FEM_Element::Hex8;
+    const FEM_Element type = p.nodes == 4 ? FEM_Element::Tet4 : p.nodes == 10 ? FEM_Element::Tet10 : FEM_Element::Hex8;
     const int stride = (int)p.nodes + 1;
     spGlobalPotential G = GlobalPotential::create();
 

@@ -69,7 +69,7 @@ template <typename T>
 static int project_impl(T* m, int32_t n, int64_t count, T eps, int32_t mirroring, int32_t* nc, void* stream)
 {
     return guarded([&] {
-        if (n <= 0 || n % 3 != 0 || n > 24) throw std::invalid_argument("n must be a multiple of 3 up to 24");
+        if (n <= 0 || n % 3 != 0 || n > 30) throw std::invalid_argument("n must be a multiple of 3 up to 30");
         if (count < 0) throw std::invalid_argument("negative count");
         if (count == 0) return SYMXG_OK;
         if (!m || !nc) throw std::invalid_argument("null device pointer");
@@ -248,8 +248,8 @@ int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, 
 {
     return guarded([&] {
         if (!p || !out) throw std::invalid_argument("null argument");
-        if (p->nodes_per_element != 4 && p->nodes_per_element != 8)
-            throw std::invalid_argument("nodes_per_element must be 4 (Tet4) or 8 (Hex8)");
+        if (p->nodes_per_element != 4 && p->nodes_per_element != 8 && p->nodes_per_element != 10)
+            throw std::invalid_argument("nodes_per_element must be 4 (Tet4), 10 (Tet10) or 8 (Hex8)");
         if (p->n_vertices <= 0 || p->n_elements < 0 || !p->connectivity || !p->rest_positions || !p->mu || !p->lambda)
             throw std::invalid_argument("missing mesh or material arrays");
         if (p->n_bc > 0 && (!p->bc_vertices || !p->bc_targets)) throw std::invalid_argument("missing boundary arrays");
@@ -289,7 +289,7 @@ int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, 
 
         using namespace symx;
         symxg_solver* s = S.get();
-        const FEM_Element type = nn == 4 ? FEM_Element::Tet4 : FEM_Element::Hex8;
+        const FEM_Element type = nn == 4 ? FEM_Element::Tet4 : nn == 10 ? FEM_Element::Tet10 : FEM_Element::Hex8;
         S->G = GlobalPotential::create();
         S->G->add_potential("neo_hookean_" + get_name(type), S->conn_numbered, nn + 1,
             [s, type, nn](MappedWorkspace<double>& mws, Element& elem) {

@@ -71,6 +71,7 @@ __device__ __forceinline__ symxg_df symxg_ldc_df(const float2* __restrict__ p, l
     return symxg_df(v.x, v.y);
 }
 __device__ __forceinline__ float symxg_ldc_f(const float2* __restrict__ p, long long i) { return __ldg(&p[i].x); }
+__device__ __forceinline__ double symxg_ldc_d(const double* __restrict__ p, long long i) { return __ldg(p + i); }
 __device__ __forceinline__ symxg_df symxg_df_fast(float a, float b)  // |a| >= |b|
 {
     const float s = __fadd_rn(a, b);
@@ -179,8 +180,10 @@ std::string emit_device_function(const Expressions& g, const std::vector<int32_t
     OpCount oc;
     std::ostringstream s;
     const bool sink = !sink_macro.empty();
-    const std::string cparam =
-        ext_load.empty() ? "const " + T + "* __restrict__ c" : "const float2* __restrict__ cq, long long cn";
+    // the cache holds doubles for double functions, (hi, lo) float pairs otherwise
+    const std::string cparam = ext_load.empty() ? "const " + T + "* __restrict__ c"
+                               : T == "double"  ? "const double* __restrict__ cq, long long cn"
+                                                : "const float2* __restrict__ cq, long long cn";
     if (sink)
         s << "__device__ __forceinline__ void " << name << "(const " << T << "* __restrict__ in, " << cparam << ", "
           << T << "* __restrict__ out, int lq, bool st)\n{\n";

@@ -33,7 +33,13 @@ std::vector<std::array<double, 4>> get_integration_rule(const FEM_Element& e)
         return {{1.0, -p, -p, -p}, {1.0, p, -p, -p}, {1.0, p, p, -p}, {1.0, -p, p, -p},
                 {1.0, -p, -p, p},  {1.0, p, -p, p},  {1.0, p, p, p},  {1.0, -p, p, p}};
     }
-    throw std::runtime_error("symx_gb300: integration rule available for Tet4 and Hex8");
+    if (e == FEM_Element::Tet10) {
+        // 4-point rule with the reference's rounded weights and points
+        // (symx/src/solver/fem_integrators.cpp:60-68), kept identical so energies match
+        const double w = 0.041666667, a = 0.58541020, b = 0.13819660;
+        return {{w, a, b, b}, {w, b, a, b}, {w, b, b, a}, {w, b, b, b}};
+    }
+    throw std::runtime_error("symx_gb300: integration rule available for Tet4, Tet10 and Hex8");
 }
 
 Vector fem_interpolation(const FEM_Element& e, const std::vector<Vector>& vh, const Vector& xi)
@@ -49,8 +55,14 @@ Vector fem_interpolation(const FEM_Element& e, const std::vector<Vector>& vh, co
         const Scalar zm = 0.5 * (1.0 - xi[2]), zp = 0.5 * (1.0 + xi[2]);
         N = {xm * ym * zm, xp * ym * zm, xp * yp * zm, xm * yp * zm,
              xm * ym * zp, xp * ym * zp, xp * yp * zp, xm * yp * zp};
+    } else if (e == FEM_Element::Tet10) {
+        if (vh.size() != 10) throw std::runtime_error("symx: Tet10 interpolation needs 10 nodes");
+        const Scalar n0 = 1.0 - xi[0] - xi[1] - xi[2], n1 = xi[0], n2 = xi[1], n3 = xi[2];
+        N = {n0 * (2.0 * n0 - 1.0), n1 * (2.0 * n1 - 1.0), n2 * (2.0 * n2 - 1.0), n3 * (2.0 * n3 - 1.0),
+             4.0 * n0 * n1,         4.0 * n1 * n2,         4.0 * n2 * n0,         4.0 * n0 * n3,
+             4.0 * n1 * n3,         4.0 * n2 * n3};
     } else {
-        throw std::runtime_error("symx_gb300: interpolation available for Tet4 and Hex8");
+        throw std::runtime_error("symx_gb300: interpolation available for Tet4, Tet10 and Hex8");
     }
     Vector x = vh[0] * N[0];
     for (size_t a = 1; a < vh.size(); ++a) x = x + vh[a] * N[a];

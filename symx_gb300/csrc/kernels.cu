@@ -271,13 +271,14 @@ __global__ void k_select_elements(int64_t n_el, int nb, const uint8_t* __restric
     sel[atomicAdd(n_sel, 1ull)] = e;
 }
 
-// Generic N (up to 24) with thread-private arrays; used for large element matrices.
+// Generic N (up to 30) with thread-private arrays; used for the element matrices the
+// specialised kernels do not cover (Tet10: 30 x 30).
 template <typename T>
 __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, int N, int64_t count, T eps,
                                                            int mirroring, int* not_converged,
                                                            const int64_t* __restrict__ sel)
 {
-    constexpr int NMAX = 24;
+    constexpr int NMAX = 30;
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
     const int64_t m = sel ? sel[k] : k;
@@ -2184,7 +2185,7 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
             break;
         }
         default:
-            if (N > 24 || N % 3 != 0) throw std::runtime_error("symx_gb300: projection supports N = 3k <= 24");
+            if (N > 30 || N % 3 != 0) throw std::runtime_error("symx_gb300: projection supports N = 3k <= 30");
             k_project_pd_generic<T><<<blocks_for(count, 64), 64, 0, s>>>(H, N, count, eps, mirroring, not_converged, sel);
     }
     check_launch("project_pd");

@@ -229,9 +229,15 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
           << "#pragma unroll\n    for (int o = 1; o < SYMXG_NQ; o <<= 1)\n"
           << "        v = v + symxg_df(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));\n"
           << "    return v;\n}\n"
+          << "__device__ __forceinline__ double symxg_qsum(double v)\n{\n"
+          << "#pragma unroll\n    for (int o = 1; o < SYMXG_NQ; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);\n"
+          << "    return v;\n}\n"
           << "#define SYMXG_Q_SUM(v) symxg_qsum(v)\n"
           << "#define SYMXG_Q_STORE(r, k) do { if (st && lq == (k) % SYMXG_NQ) out[(k)] = (r); } while (0)\n";
         s << emit_device_function(g, h_bm, "symxg_eval_h_f32_q", "float", false, nullptr, &ext, "SYMXG_Q", "symxg_ldc_f");
+        // the FP64 form of the same
+        s << emit_device_function(g, eg, "symxg_eval_eg_dl", "double", acc, nullptr, &ext, "", "symxg_ldc_d");
+        s << emit_device_function(g, h_bm, "symxg_eval_h_f64_q", "double", false, nullptr, &ext, "SYMXG_Q", "symxg_ldc_d");
     }
     s << emit_device_function(g, e_only, "symxg_eval_e", "double", acc, oe, &ext);
     if (cond >= 0) s << emit_device_function(g, {cond}, "symxg_eval_cond", "double", false, nullptr, &ext);
@@ -309,8 +315,29 @@ std::string build_source(CompiledPotential& cp, const Expressions& g, const std:
     }
     s << "}\n";
 
-    // E + g + H kernels, H in double or float
+    // E + g + H kernels, H in double or float (FP64 with several quadrature points: one lane
+    // per point, as the mixed kernel below)
+    if (qp_parallel) {
+        s << "extern \"C\" __global__ void __launch_bounds__(128) symxg_egh_f64" << sig_common
+          << ", double* __restrict__ G, double* __restrict__ H)\n{\n";
+        s << "    if (n <= 0) return;\n";
+        s << "    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;\n";
+        s << "    const int lq = (int)(t % SYMXG_NQ);\n    const bool st = t / SYMXG_NQ < n;\n";
+        s << "    const long long e = st ? t / SYMXG_NQ : n - 1;\n";
+        s << "    double in[" << NS << "];\n    symxg_gather(e, conn, maps, in);\n";
+        s << "    {\n" << set_sum("lq", main_symbol);
+        s << "        const double* __restrict__ cq = cache + (long long)lq * " << K << "LL * n + e;\n";
+        s << "        double eg[" << (NG + 1) << "];\n";
+        s << "        for (int i = 0; i < " << NG + 1 << "; ++i) eg[i] = 0.0;\n";
+        s << "        symxg_eval_eg_dl(in, cq, n, eg);\n";
+        s << "#pragma unroll\n        for (int i = 0; i < " << NG + 1 << "; ++i) eg[i] = symxg_qsum(eg[i]);\n";
+        s << "        if (st && lq == 0) E[e] = eg[0];\n";
+        s << "#pragma unroll\n        for (int i = 0; i < " << NG << "; ++i)\n"
+          << "            if (st && lq == i % SYMXG_NQ) G[e * " << NG << "LL + i] = eg[1 + i];\n";
+        s << "        symxg_eval_h_f64_q(in, cq, n, H + e * " << NH << "LL, lq, st);\n    }\n}\n";
+    }
     for (int prec = 0; prec < 2; ++prec) {
+        if (prec == 0 && qp_parallel) continue;
         const std::string TH = prec == 0 ? "double" : "float";
         const std::string kname = prec == 0 ? "symxg_egh_f64" : "symxg_egh_f32";
         s << "extern \"C\" __global__ void __launch_bounds__(128) " << kname << sig_common
@@ -508,7 +535,7 @@ CompiledPotential prepare_potential(const Potential& pot, const GlobalPotential&
     }
     cp.nb = (int)cp.dof_set.size();
     if (cp.nb == 0) throw std::runtime_error("symx: potential '" + pot.name + "' depends on no DoF");
-    if (cp.nb > 8) throw std::runtime_error("symx_gb300: at most 8 DoF blocks per element (24x24 Hessians)");
+    if (cp.nb > 10) throw std::runtime_error("symx_gb300: at most 10 DoF blocks per element (30x30 Hessians)");
     cp.conn_stride = mws.conn.stride;
     DiffCache cache;
     Vector grad = gradient(pot.expression, wrt, cache);
@@ -671,7 +698,7 @@ struct SolverImpl {
                 double* G = g_el.p + cp.g_off * 3;
                 void* H = mode == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
                 void* args[] = {&n, &conn, &maps, &cache, &E, &G, &H};
-                const unsigned grid_eh = mode == 1 ? (unsigned)((n * cp.qp_lanes + 127) / 128) : grid;
+                const unsigned grid_eh = (unsigned)((n * cp.qp_lanes + 127) / 128);  // both E+g+H kernels
                 cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_df32", dim3(grid_eh), dim3(128), 0, stream,
                                   args);
             }

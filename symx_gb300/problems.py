@@ -86,6 +86,25 @@ def cuboid_tet4(nx: int, ny: int, nz: int, size):
     return X, tets.reshape(-1, 4).astype(np.int32)
 
 
+# Tet10 node order after the 4 corners: the midpoints of edges (0,1), (1,2), (2,0), (0,3),
+# (1,3), (2,3), matching the quadratic shape functions (symx/src/solver/fem_integrators.h:56-76).
+_TET10_EDGES = ((0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3))
+
+
+def cuboid_tet10(nx: int, ny: int, nz: int, size):
+    """Structured Tet10 box: the Tet4 split with a node at every edge midpoint
+    (vertices (nv,3) f64, tets (6*cells,10) i32; corner vertices first)."""
+    X, tets = cuboid_tet4(nx, ny, nz, size)
+    nv = X.shape[0]
+    pairs = np.stack([np.sort(tets[:, [a, b]], axis=1) for a, b in _TET10_EDGES], axis=1)  # (ne, 6, 2)
+    keys = pairs[..., 0].astype(np.int64) * nv + pairs[..., 1]
+    uniq, inv = np.unique(keys.ravel(), return_inverse=True)
+    ua, ub = uniq // nv, uniq % nv
+    mids = 0.5 * (X[ua] + X[ub])
+    conn = np.concatenate([tets, (nv + inv.reshape(-1, 6)).astype(np.int32)], axis=1)
+    return np.concatenate([X, mids], axis=0), conn.astype(np.int32)
+
+
 def cuboid_hex8(nx: int, ny: int, nz: int, size):
     """Structured Hex8 box on [0, size]: (vertices (nv,3) f64, hexes (cells,8) i32)."""
     X = _grid_vertices(nx, ny, nz, size)
@@ -106,9 +125,10 @@ _HEX8_SIGNS = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
 
 
 def element_volumes(X, conn):
-    """Rest volume of each element (Tet4: |det|/6; Hex8: 2x2x2 Gauss sum of det J)."""
-    if conn.shape[1] == 4:
-        P = X[conn]
+    """Rest volume of each element (Tet4 and Tet10 with straight edges: |det|/6 of the
+    corners; Hex8: 2x2x2 Gauss sum of det J)."""
+    if conn.shape[1] in (4, 10):
+        P = X[conn[:, :4]]
         D = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=2)
         return np.abs(np.linalg.det(D)) / 6.0
     P = X[conn]  # (ne, 8, 3)
@@ -156,6 +176,8 @@ CONFIGS = {
     # unprojected Hessian is indefinite, so the adaptive projection modes retry and project.
     "tet4_5c": dict(kind="tet4", cells=(5, 4, 4), h=0.01, perturb=0.0, seed=13, init_compress_y=0.5,
                     init_perturb=0.1),
+    # Quadratic tetrahedra (30 x 30 element Hessians, 4 quadrature points).
+    "tet10_2": dict(kind="tet10", cells=(3, 2, 2), h=0.01, perturb=0.05, seed=14),
     "tet4_32": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.0, seed=3),
     "tet4_40": dict(kind="tet4", cells=(40, 40, 40), h=0.01, perturb=0.0, seed=4),
 }
@@ -175,6 +197,8 @@ def step_problem(name_or_cfg, *, youngs=1e5, poisson=0.3, density=1000.0, dt=1.0
     size = (nx * h, ny * h, nz * h)
     if cfg["kind"] == "tet4":
         X, conn = cuboid_tet4(nx, ny, nz, size)
+    elif cfg["kind"] == "tet10":
+        X, conn = cuboid_tet10(nx, ny, nz, size)
     else:
         X, conn = cuboid_hex8(nx, ny, nz, size)
     nv, ne = X.shape[0], conn.shape[0]

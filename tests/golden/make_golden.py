@@ -212,6 +212,11 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             print(make_modes(tmp))
         return
+    if len(sys.argv) == 3 and sys.argv[1] == "case":  # one problem's eval and solve fixtures
+        with tempfile.TemporaryDirectory() as tmp:
+            out, sol = make_case(tmp, sys.argv[2], keep_triplets=sys.argv[2] != "tet10_2")
+            print({k: v for k, v in sol.items() if not k.startswith(("x_", "log_"))})
+        return
     with tempfile.TemporaryDirectory() as tmp:
         rows, out = make_elem(tmp)
         make_project(tmp, out)
@@ -220,6 +225,7 @@ def main():
         make_case(tmp, "tet4_6p")
         make_case(tmp, "hex8_3")
         make_case(tmp, "tet4_10", keep_triplets=False)
+        make_case(tmp, "tet10_2", keep_triplets=False)
         make_modes(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -12,7 +12,7 @@ from oracle import oracle as O
 from symx_gb300 import problems
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CASES = ["tet4_3", "tet4_6p", "hex8_3", "tet4_10"]
+CASES = ["tet4_3", "tet4_6p", "hex8_3", "tet4_10", "tet10_2"]
 
 
 # ------------------------------------------------------------------ oracle pinning

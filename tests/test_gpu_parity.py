@@ -10,7 +10,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["tet4_3", "tet4_6p", "hex8_3", "tet4_10"]
+CASES = ["tet4_3", "tet4_6p", "hex8_3", "tet4_10", "tet10_2"]
 
 
 @pytest.fixture(scope="module")
@@ -40,7 +40,7 @@ def test_energy_gradient_match_reference(sg, golden, case):
     assert abs(s.evaluate_energy() - ev["E_only"]) <= 1e-12 * abs(ev["E_only"])
 
 
-@pytest.mark.parametrize("case", ["tet4_3", "hex8_3", "tet4_6p"])
+@pytest.mark.parametrize("case", ["tet4_3", "hex8_3", "tet4_6p", "tet10_2"])
 def test_element_outputs_match_oracle(sg, golden, case):
     from oracle import oracle as O
 
@@ -62,7 +62,7 @@ def test_element_outputs_match_oracle(sg, golden, case):
     idx = ev["hess_sample_idx"]
     ref = ev["hess_sample_projected"]
     assert np.max(np.abs(Hp[idx] - ref)) <= 1e-9 * np.max(np.abs(ref))
-    assert nodes in (4, 8)
+    assert nodes in (4, 8, 10)
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -171,7 +171,7 @@ def test_unknown_projection_mode_rejected(sg):
         s.set_settings(project_to_pd=4)
 
 
-@pytest.mark.parametrize("case", ["tet4_6p", "hex8_3"])
+@pytest.mark.parametrize("case", ["tet4_6p", "hex8_3", "tet10_2"])
 def test_mixed_element_hessians_within_float_tolerance(sg, case):
     """FP32 element Hessians of the mixed path against the FP64 path (Hex8: summed over the
     eight quadrature points by the lanes that evaluate them)."""
