@@ -63,6 +63,24 @@ struct symxg_solver {
     // rollout: (x0, v0) before every checkpoint_every-th step of the last forward rollout
     std::vector<std::vector<Vec3>> ckpt_x0, ckpt_v0;
     int rollout_steps = 0, checkpoint_every = 0;
+    // The bound host arrays are page-locked once their size is final (they are only written
+    // in place afterwards), so every upload and download copies at full host-device link
+    // speed.  A refused registration is skipped (the copies then go through pageable memory).
+    std::vector<void*> pinned;
+    template <typename V>
+    void pin(V& v)
+    {
+        if (v.empty()) return;
+        if (cudaHostRegister(v.data(), sizeof(v[0]) * v.size(), cudaHostRegisterDefault) == cudaSuccess)
+            pinned.push_back(v.data());
+        else
+            cudaGetLastError();
+    }
+    ~symxg_solver()
+    {
+        newton.reset();
+        for (void* p : pinned) cudaHostUnregister(p);
+    }
 };
 
 template <typename T>
@@ -338,6 +356,14 @@ int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, 
         auto ctx = Context::create();
         if (cache_dir) ctx->compilation_directory = cache_dir;
         S->newton = std::make_unique<NewtonsMethod>(S->G, ctx);
+        S->pin(S->x);
+        S->pin(S->x0);
+        S->pin(S->v0);
+        S->pin(S->X);
+        S->pin(S->bc_target);
+        S->pin(S->mu);
+        S->pin(S->lam);
+        S->pin(S->mass);
         *out = S.release();
         return SYMXG_OK;
     });
