@@ -679,28 +679,35 @@ struct SolverImpl {
         cp.cache_df = df;
     }
 
-    // mode: 0 E+g+H in FP64, 1 mixed (E+g double-float, H FP32), 2 E only FP64, 3 E only double-float
+    // mode: 0 E+g+H in FP64, 1 mixed (E+g double-float, H FP32), 2 E only FP64, 3 E only double-float.
+    // In the mixed modes, potentials of one DoF block per element (inertia or gravity, penalty
+    // boundary conditions) keep E and g in FP64: their coefficients are large (a 1e8 penalty
+    // times the rounding of x in double-float, about 1e-15 m, is a gradient error near 1e-7,
+    // above the solver's tolerances), and one-vertex elements cost little in FP64.
     void launch_eval(int mode)
     {
         for (auto& cp : pots) {
             if (cp.n_elements == 0) continue;
-            ensure_cache(cp, mode == 1 || mode == 3);
+            const bool fp64_eg = cp.nb == 1;
+            const int m = (fp64_eg && mode == 3) ? 2 : mode;  // energy only: FP64
+            const bool eg64_h32 = fp64_eg && m == 1;           // FP64 E+g, FP32 H
+            ensure_cache(cp, (m == 1 || m == 3) && !fp64_eg);
             long long n = cp.n_elements;
             const int32_t* conn = cp.conn.p;
             const double* const* maps = cp.map_ptrs.p;
             const double* cache = cp.cache.p;
             double* E = E_el.p + cp.e_off;
             const unsigned grid = (unsigned)((n + 127) / 128);
-            if (mode >= 2) {
+            if (m >= 2) {
                 void* args[] = {&n, &conn, &maps, &cache, &E};
-                cp.module->launch(mode == 2 ? "symxg_e" : "symxg_e_df", dim3(grid), dim3(128), 0, stream, args);
+                cp.module->launch(m == 2 ? "symxg_e" : "symxg_e_df", dim3(grid), dim3(128), 0, stream, args);
             } else {
                 double* G = g_el.p + cp.g_off * 3;
-                void* H = mode == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
+                void* H = m == 0 ? (void*)(H64.p + cp.h_off * 9) : (void*)(H32.p + cp.h_off * 9);
                 void* args[] = {&n, &conn, &maps, &cache, &E, &G, &H};
                 const unsigned grid_eh = (unsigned)((n * cp.qp_lanes + 127) / 128);  // both E+g+H kernels
-                cp.module->launch(mode == 0 ? "symxg_egh_f64" : "symxg_egh_df32", dim3(grid_eh), dim3(128), 0, stream,
-                                  args);
+                const char* kname = m == 0 ? "symxg_egh_f64" : eg64_h32 ? "symxg_egh_f32" : "symxg_egh_df32";
+                cp.module->launch(kname, dim3(eg64_h32 ? grid : grid_eh), dim3(128), 0, stream, args);
             }
         }
     }
