@@ -20,6 +20,7 @@
 //   symx_ref_harness project <in.bin> <out.bin>            project_to_PD_inplace on n x n matrices
 //   symx_ref_harness eval    <problem.bin> <outdir> <thr>  E, grad, element Hessians, BCSR triplets
 //   symx_ref_harness solve   <problem.bin> <outdir> <thr> [max_newton] [cg_rel_tol] [projection mode]
+//   symx_ref_harness mesh    d|f <type> <nx> <ny> <nz> <sx> <sy> <sz> <out.bin>   generate_cuboid_mesh
 #include <symx>
 #include <Eigen/Sparse>
 
@@ -354,8 +355,32 @@ int mode_solve(const std::string& pfile, const std::string& outdir, int n_thread
 
 }  // namespace
 
+// generate_cuboid_mesh (mesh_generation.cpp:306-327) written as int64 {n_vertices, n_elements,
+// stride}, the vertices (FLOAT) and the connectivity (int32).
+template <typename FLOAT>
+int write_mesh(int type, const std::array<int32_t, 3>& n, const Eigen::Matrix<FLOAT, 3, 1>& size, const char* path)
+{
+    const FEMMesh<FLOAT> m = generate_cuboid_mesh<FLOAT>(static_cast<FEM_Element>(type), size, n);
+    std::ofstream f(path, std::ios::binary);
+    const int64_t hdr[3] = {(int64_t)m.vertices.size(), (int64_t)m.n_elements, (int64_t)m.connectivity_stride};
+    f.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+    for (const auto& v : m.vertices) f.write(reinterpret_cast<const char*>(v.data()), 3 * sizeof(FLOAT));
+    f.write(reinterpret_cast<const char*>(m.connectivity.data()), sizeof(int) * m.connectivity.size());
+    return f ? 0 : 1;
+}
+
+int mode_mesh(char** a)
+{
+    const int type = std::atoi(a[1]);
+    const std::array<int32_t, 3> n = {std::atoi(a[2]), std::atoi(a[3]), std::atoi(a[4])};
+    if (std::string(a[0]) == "f")
+        return write_mesh<float>(type, n, Eigen::Vector3f((float)std::atof(a[5]), (float)std::atof(a[6]), (float)std::atof(a[7])), a[8]);
+    return write_mesh<double>(type, n, Eigen::Vector3d(std::atof(a[5]), std::atof(a[6]), std::atof(a[7])), a[8]);
+}
+
 int main(int argc, char** argv)
 {
+    if (argc >= 11 && std::string(argv[1]) == "mesh") return mode_mesh(argv + 2);
     if (argc < 4) {
         std::cerr << "usage: symx_ref_harness elem|project|eval|solve <in> <out> [threads] [max_newton] [cg_rel_tol]\n";
         return 1;

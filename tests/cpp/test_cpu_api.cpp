@@ -187,6 +187,31 @@ static int nvrtc(const char* cache_dir)
     return 0;
 }
 
+// Writes generate_cuboid_mesh's output: int64 {n_vertices, n_elements, stride}, the vertices
+// (FLOAT), the connectivity (int32).  prec is "d" or "f".
+template <typename FLOAT>
+int write_mesh(int type, const std::array<int32_t, 3>& n, const std::array<FLOAT, 3>& size, const char* path)
+{
+    const symx::FEMMesh<FLOAT> m = symx::generate_cuboid_mesh(static_cast<symx::FEM_Element>(type), size, n);
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return 1;
+    const int64_t hdr[3] = {(int64_t)m.vertices.size(), (int64_t)m.n_elements, (int64_t)m.connectivity_stride};
+    std::fwrite(hdr, sizeof(hdr), 1, f);
+    for (const auto& v : m.vertices) std::fwrite(v.data(), sizeof(FLOAT), 3, f);
+    std::fwrite(m.connectivity.data(), sizeof(int), m.connectivity.size(), f);
+    std::fclose(f);
+    return 0;
+}
+
+int mesh(char** a)
+{
+    const int type = std::atoi(a[1]);
+    const std::array<int32_t, 3> n = {std::atoi(a[2]), std::atoi(a[3]), std::atoi(a[4])};
+    if (std::string(a[0]) == "f")
+        return write_mesh<float>(type, n, {(float)std::atof(a[5]), (float)std::atof(a[6]), (float)std::atof(a[7])}, a[8]);
+    return write_mesh<double>(type, n, {std::atof(a[5]), std::atof(a[6]), std::atof(a[7])}, a[8]);
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 2) return 2;
@@ -195,6 +220,7 @@ int main(int argc, char** argv)
         if (mode == "selftest") return selftest();
         if (mode == "nh_elem" && argc >= 4) return nh_elem(argv[2], argv[3]);
         if (mode == "nvrtc") return nvrtc(argc >= 3 ? argv[2] : "");
+        if (mode == "mesh" && argc >= 11) return mesh(argv + 2);  // prec type nx ny nz sx sy sz out
     } catch (const std::exception& e) {
         std::printf("exception: %s\n", e.what());
         return 3;

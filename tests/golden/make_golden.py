@@ -16,6 +16,7 @@ Fixtures:
   <case>_eval.npz      E, gradient, element Hessians, BCSR triplets at the initial state
   <case>_solve.npz     final positions and iteration counts of NewtonsMethod::solve
   tet4_5c_modes.npz    NewtonsMethod::solve in each ProjectionToPD mode (indefinite start)
+  meshes.npz           generate_cuboid_mesh (mesh_generation.cpp:306-327) for each element type
 """
 from __future__ import annotations
 
@@ -205,9 +206,45 @@ def make_modes(tmp, case="tet4_5c"):
     return out
 
 
+# (precision, element type as FEM_Element's index, cells per axis, box size)
+MESH_CASES = [
+    ("d", 0, (3, 2, 4), (0.3, 0.2, 0.4)),
+    ("d", 0, (7, 5, 6), (1.0, 0.5, 0.75)),
+    ("f", 0, (4, 4, 3), (0.04, 0.04, 0.03)),
+    ("d", 1, (2, 3, 2), (1.0, 1.5, 1.0)),
+    ("d", 2, (5, 3, 4), (1.28, 1.28, 0.32)),
+    ("f", 2, (3, 3, 3), (0.3, 0.3, 0.3)),
+    ("d", 3, (2, 2, 3), (2.0, 1.0, 1.0)),
+]
+
+
+def read_mesh(path, prec):
+    hdr = np.fromfile(path, dtype=np.int64, count=3)
+    nv, ne, stride = (int(v) for v in hdr)
+    ft = np.float32 if prec == "f" else np.float64
+    verts = np.fromfile(path, dtype=ft, count=nv * 3, offset=24).reshape(nv, 3)
+    conn = np.fromfile(path, dtype=np.int32, offset=24 + nv * 3 * verts.itemsize).reshape(ne, stride)
+    return verts, conn
+
+
+def make_meshes(tmp):
+    out = {}
+    for i, (prec, etype, n, size) in enumerate(MESH_CASES):
+        path = os.path.join(tmp, f"mesh{i}.bin")
+        run("mesh", prec, etype, *n, *(repr(float(s)) for s in size), path)
+        out[f"vertices_{i}"], out[f"conn_{i}"] = read_mesh(path, prec)
+    out["cases"] = np.array(json.dumps(MESH_CASES))
+    np.savez_compressed(os.path.join(HERE, "meshes.npz"), **out)
+    return out
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -f oracle/Makefile.ref -j8")
+    if sys.argv[1:] == ["meshes"]:  # only the mesh-generator fixture
+        with tempfile.TemporaryDirectory() as tmp:
+            make_meshes(tmp)
+        return
     if sys.argv[1:] == ["modes"]:  # only the projection-mode fixture
         with tempfile.TemporaryDirectory() as tmp:
             print(make_modes(tmp))
@@ -227,6 +264,7 @@ def main():
         make_case(tmp, "tet4_10", keep_triplets=False)
         make_case(tmp, "tet10_2", keep_triplets=False)
         make_modes(tmp)
+        make_meshes(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 

@@ -265,3 +265,26 @@ def test_host_build_of_projection_matches_reference(golden, tmp_path):
         err = np.abs(out[mode] - ref) / scale
         sel = nh if mode in (1, 3) else slice(None)
         assert np.max(err[sel]) <= tol, mode
+
+
+def test_cpp_mesh_generators_match_reference(cpp_test, golden, tmp_path):
+    """generate_cuboid_{Tet4,Tet10,Hex8,Hex27}_mesh: vertices and connectivity, node for node
+    and element for element, equal to the reference's (RCM node order, reversed element walk)."""
+    import json
+
+    d = golden("meshes")
+    for i, (prec, etype, n, size) in enumerate(json.loads(str(d["cases"]))):
+        out = tmp_path / f"mesh{i}.bin"
+        subprocess.run([cpp_test, "mesh", prec, str(etype), *map(str, n), *(repr(float(s)) for s in size), str(out)],
+                       check=True)
+        nv, ne, stride = (int(v) for v in np.fromfile(out, dtype=np.int64, count=3))
+        ft = np.float32 if prec == "f" else np.float64
+        verts = np.fromfile(out, dtype=ft, count=nv * 3, offset=24).reshape(nv, 3)
+        conn = np.fromfile(out, dtype=np.int32, offset=24 + verts.nbytes).reshape(ne, stride)
+        np.testing.assert_array_equal(conn, d[f"conn_{i}"], err_msg=f"case {i}")
+        # Coordinates: one rounding of min + i * spacing apart at most.  The reference's release
+        # build fuses that multiply-add in some components and not in others (Eigen packets
+        # under -mfma); this library always fuses it.
+        ulp = np.finfo(ft).eps * max(size)
+        np.testing.assert_allclose(verts, d[f"vertices_{i}"], rtol=0, atol=ulp, err_msg=f"case {i}")
+        assert sorted(set(conn.ravel())) == list(range(nv)) or stride in (10, 27)
