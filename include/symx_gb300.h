@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SYMXG_ABI_VERSION 3
+#define SYMXG_ABI_VERSION 4
 
 /* status codes */
 #define SYMXG_OK 0
@@ -167,6 +167,16 @@ int symxg_assembled_hessian(symxg_solver* solver, int32_t project, int32_t* n_bl
 int symxg_element_outputs(symxg_solver* solver, int32_t potential, int32_t project, double* E, double* g, double* H);
 /* Number of scalar operations in the generated code of a potential: E+g, H, E-only. */
 int symxg_op_counts(symxg_solver* solver, int32_t potential, int64_t counts[3]);
+
+/* Structured box mesh as the reference's generate_cuboid_mesh builds it
+ * (symx/src/solver/mesh_generation.cpp:306-327, mesh_ordering.cpp:231-252): a box of `size`
+ * centred at the origin with `cells` per axis, element_type 0 Tet4 (6 per cell), 1 Tet10,
+ * 2 Hex8, 3 Hex27, nodes renumbered by reverse Cuthill-McKee, elements in the reference's
+ * order.  Host only.  With vertices or connectivity NULL: writes the sizes.  Otherwise
+ * *n_vertices and *n_elements hold the buffers' capacities (vertices: 3 doubles each,
+ * connectivity: *stride int32 each) and are set to the sizes written. */
+int symxg_generate_cuboid_mesh(int32_t element_type, const double size[3], const int32_t cells[3], int64_t* n_vertices,
+                               int64_t* n_elements, int32_t* stride, double* vertices, int32_t* connectivity);
 
 /* Number of CUDA kernels this library has launched since it was loaded (all handles). */
 int64_t symxg_launch_count(void);

@@ -28,6 +28,7 @@ EXPORTS = [
     "symxg_assembled_hessian", "symxg_element_outputs", "symxg_op_counts", "symxg_project_pd_f32",
     "symxg_project_pd_f64", "symxg_bcsr_spmv_f32", "symxg_bcsr_spmv_f64", "symxg_launch_count",
     "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64", "symxg_bcsr_pcg_f32_noalloc", "symxg_adjoint",
+    "symxg_generate_cuboid_mesh",
     "symxg_rollout_forward", "symxg_rollout_backward",
 ]
 
@@ -146,6 +147,7 @@ def load(path: str | None = None):
         "symxg_assembled_hessian": ([P, I32, C.POINTER(I32), C.POINTER(I64), P, P, P], C.c_int),
         "symxg_element_outputs": ([P, I32, I32, P, P, P], C.c_int),
         "symxg_op_counts": ([P, I32, P], C.c_int),
+        "symxg_generate_cuboid_mesh": ([I32, P, P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I32), P, P], C.c_int),
         "symxg_project_pd_f32": ([P, I32, I64, C.c_float, I32, P, P], C.c_int),
         "symxg_project_pd_f64": ([P, I32, I64, D, I32, P, P], C.c_int),
         "symxg_bcsr_spmv_f32": ([I32, P, P, P, I64, P, P, P], C.c_int),
@@ -169,3 +171,26 @@ def check(rc: int):
     if rc != 0:
         msg = load().symxg_last_error().decode(errors="replace")
         raise SymxgError(f"symx_gb300 call failed (status {rc}): {msg}")
+
+
+# FEM_Element order of the reference (symx/src/solver/fem_integrators.h:9).
+ELEMENT_TYPES = {"tet4": 0, "tet10": 1, "hex8": 2, "hex27": 3}
+
+
+def generate_cuboid_mesh(kind: str, size, cells):
+    """The reference's generate_cuboid_mesh (mesh_generation.cpp:306-327): box of `size`
+    centred at the origin, reverse Cuthill-McKee node numbering.  Returns (vertices (nv, 3)
+    float64, connectivity (ne, stride) int32)."""
+    import numpy as np
+
+    L = load()
+    t = ELEMENT_TYPES[kind]
+    sz = (C.c_double * 3)(*map(float, size))
+    nc = (C.c_int32 * 3)(*map(int, cells))
+    nv, ne, st = C.c_int64(), C.c_int64(), C.c_int32()
+    check(L.symxg_generate_cuboid_mesh(t, sz, nc, C.byref(nv), C.byref(ne), C.byref(st), None, None))
+    X = np.empty((nv.value, 3), dtype=np.float64)
+    conn = np.empty((ne.value, st.value), dtype=np.int32)
+    check(L.symxg_generate_cuboid_mesh(t, sz, nc, C.byref(nv), C.byref(ne), C.byref(st), X.ctypes.data,
+                                       conn.ctypes.data))
+    return X, conn

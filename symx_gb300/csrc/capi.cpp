@@ -19,6 +19,7 @@
 #include "fem.h"
 #include "global_potential.h"
 #include "kernels.cuh"
+#include "mesh.h"
 #include "newton.h"
 
 namespace {
@@ -512,6 +513,28 @@ int symxg_element_outputs(symxg_solver* s, int32_t potential, int32_t project, d
         if (potential < 0 || potential >= s->G->get_n_potentials()) throw std::invalid_argument("no such potential");
         s->newton->upload();
         s->newton->element_outputs(potential, project != 0, E, g, H);
+        return SYMXG_OK;
+    });
+}
+
+int symxg_generate_cuboid_mesh(int32_t type, const double size[3], const int32_t cells[3], int64_t* n_vertices,
+                               int64_t* n_elements, int32_t* stride, double* vertices, int32_t* connectivity)
+{
+    return guarded([&] {
+        if (!size || !cells || !n_vertices || !n_elements || !stride) throw std::invalid_argument("null argument");
+        if (type < 0 || type > 3) throw std::invalid_argument("element_type must be 0 (Tet4), 1 (Tet10), 2 (Hex8) or 3 (Hex27)");
+        const symx::FEMMesh<double> m = symx::generate_cuboid_mesh<double>(
+            static_cast<symx::FEM_Element>(type), Vec3{size[0], size[1], size[2]}, {cells[0], cells[1], cells[2]});
+        const int64_t nv = (int64_t)m.vertices.size(), ne = m.n_elements;
+        if (vertices && connectivity) {
+            if (*n_vertices < nv || *n_elements < ne) throw std::invalid_argument("mesh buffers too small");
+            for (int64_t i = 0; i < nv; ++i)
+                for (int k = 0; k < 3; ++k) vertices[3 * i + k] = m.vertices[i][k];
+            std::copy(m.connectivity.begin(), m.connectivity.end(), connectivity);
+        }
+        *n_vertices = nv;
+        *n_elements = ne;
+        *stride = m.connectivity_stride;
         return SYMXG_OK;
     });
 }

@@ -14,7 +14,9 @@ Two deliberate differences, both pure relabelings/translations that leave the
 physics unchanged: the reference's reverse Cuthill-McKee renumbering
 (``mesh_generation.cpp:89``) is not applied (the lexicographic numbering of a
 structured grid is already banded), and the box is translated from
-``[-L/2, L/2]`` to ``[0, L]`` so that the clamped face is ``x = 0``.
+``[-L/2, L/2]`` to ``[0, L]`` so that the clamped face is ``x = 0``.  Configs with
+``numbering="rcm"`` use the reference's numbering instead, built by the library's
+``symxg_generate_cuboid_mesh``.
 
 Random numbers come from a splitmix64 stream with a Box-Muller transform,
 written out here so that the same seed gives the same inputs on every numpy
@@ -178,6 +180,10 @@ CONFIGS = {
                     init_perturb=0.1),
     # Quadratic tetrahedra (30 x 30 element Hessians, 4 quadrature points).
     "tet10_2": dict(kind="tet10", cells=(3, 2, 2), h=0.01, perturb=0.05, seed=14),
+    # The 64^3 step on the reference's own mesh: generate_cuboid_Tet4_mesh with its reverse
+    # Cuthill-McKee node numbering and element order (same statistics, other per-node draws).
+    "tet4_64_rcm": dict(kind="tet4", cells=(64, 64, 64), h=0.01, perturb=0.05, seed=1, numbering="rcm"),
+    "tet4_6p_rcm": dict(kind="tet4", cells=(6, 5, 4), h=0.01, perturb=0.05, seed=11, numbering="rcm"),
     "tet4_32": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.0, seed=3),
     "tet4_40": dict(kind="tet4", cells=(40, 40, 40), h=0.01, perturb=0.0, seed=4),
 }
@@ -195,7 +201,13 @@ def step_problem(name_or_cfg, *, youngs=1e5, poisson=0.3, density=1000.0, dt=1.0
     nx, ny, nz = cfg["cells"]
     h = cfg["h"]
     size = (nx * h, ny * h, nz * h)
-    if cfg["kind"] == "tet4":
+    if cfg.get("numbering") == "rcm":  # the reference's own mesh and numbering, moved to [0, L]
+        from .capi import generate_cuboid_mesh
+
+        X, conn = generate_cuboid_mesh(cfg["kind"], size, (nx, ny, nz))
+        X = X + 0.5 * np.asarray(size)
+        X[np.abs(X) < 1e-12 * max(size)] = 0.0  # exact zeros on the clamped face
+    elif cfg["kind"] == "tet4":
         X, conn = cuboid_tet4(nx, ny, nz, size)
     elif cfg["kind"] == "tet10":
         X, conn = cuboid_tet10(nx, ny, nz, size)

@@ -151,7 +151,7 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(capi.EXPORTS) == declared
     for name in declared:
         assert hasattr(lib, name), name
-    assert lib.symxg_abi_version() == 3
+    assert lib.symxg_abi_version() == 4
 
 
 def test_invalid_arguments_are_reported(lib):
@@ -288,3 +288,31 @@ def test_cpp_mesh_generators_match_reference(cpp_test, golden, tmp_path):
         ulp = np.finfo(ft).eps * max(size)
         np.testing.assert_allclose(verts, d[f"vertices_{i}"], rtol=0, atol=ulp, err_msg=f"case {i}")
         assert sorted(set(conn.ravel())) == list(range(nv)) or stride in (10, 27)
+
+
+def test_c_abi_mesh_generator_matches_reference(golden):
+    """symxg_generate_cuboid_mesh gives the reference's connectivity, and the configs built on it
+    clamp the whole x = 0 face."""
+    import json
+
+    from symx_gb300 import capi
+
+    d = golden("meshes")
+    cases = json.loads(str(d["cases"]))
+    for i, (prec, etype, n, size) in enumerate(cases):
+        if prec != "d":
+            continue
+        kind = [k for k, v in capi.ELEMENT_TYPES.items() if v == etype][0]
+        X, conn = capi.generate_cuboid_mesh(kind, size, n)
+        np.testing.assert_array_equal(conn, d[f"conn_{i}"], err_msg=f"case {i}")
+        np.testing.assert_allclose(X, d[f"vertices_{i}"], rtol=0, atol=np.finfo(float).eps * max(size))
+    with pytest.raises(capi.SymxgError, match="element_type"):
+        capi.check(
+            capi.load().symxg_generate_cuboid_mesh(7, (capi.C.c_double * 3)(1, 1, 1), (capi.C.c_int32 * 3)(1, 1, 1),
+                                                   capi.C.byref(capi.C.c_int64()), capi.C.byref(capi.C.c_int64()),
+                                                   capi.C.byref(capi.C.c_int32()), None, None))
+    p = problems.step_problem("tet4_6p_rcm")
+    nx, ny, nz = problems.CONFIGS["tet4_6p_rcm"]["cells"]
+    assert p["conn"].shape == (6 * nx * ny * nz, 4)
+    assert p["bc_idx"].size == (ny + 1) * (nz + 1)
+    assert np.min(p["X"]) == 0.0

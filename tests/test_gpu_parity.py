@@ -311,3 +311,21 @@ def test_fp32_tet4_hessians_take_the_deflated_projection(sg):
     res = np.abs(H.reshape(-1, 12, 4, 3).sum(axis=2)).max(axis=(1, 2))
     hmax = np.abs(H).max(axis=(1, 2))
     assert np.mean(res <= 1e-5 * hmax) >= 0.99
+
+
+def test_newton_fp64_on_reference_numbered_mesh_matches_oracle(sg):
+    """The step on generate_cuboid_Tet4_mesh's own numbering (reverse Cuthill-McKee nodes,
+    reordered elements): FP64 GPU solve against the oracle on the same arrays, same Newton and
+    CG iteration counts and positions within 1e-8 of |x - x0|."""
+    from oracle import oracle as O
+
+    p, s = make(sg, "tet4_6p_rcm")
+    st = s.solve()
+    P = O.Problem(p, 1)
+    P.set_x(p["x_init"])
+    so = P.solve(O.default_settings(cg_rel_tolerance=1e-3))
+    assert st["solver_return"] == 0 and so["solver_return"] == 0
+    assert st["newton_iterations"] == so["newton_iterations"]
+    assert st["cg_iterations"] == so["cg_iterations"]
+    x, xo = s.get_positions(), P.get_x()
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo - p["x0"]) < 1e-8
