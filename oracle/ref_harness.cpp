@@ -21,6 +21,7 @@
 //   symx_ref_harness eval    <problem.bin> <outdir> <thr>  E, grad, element Hessians, BCSR triplets
 //   symx_ref_harness solve   <problem.bin> <outdir> <thr> [max_newton] [cg_rel_tol] [projection mode]
 //   symx_ref_harness mesh    d|f <type> <nx> <ny> <nz> <sx> <sy> <sz> <out.bin>   generate_cuboid_mesh
+//   symx_ref_harness rcm     <in.bin> <out.bin> <reorder_elements 0|1>           reorder_connectivity_RCM
 #include <symx>
 #include <Eigen/Sparse>
 
@@ -378,9 +379,26 @@ int mode_mesh(char** a)
     return write_mesh<double>(type, n, Eigen::Vector3d(std::atof(a[5]), std::atof(a[6]), std::atof(a[7])), a[8]);
 }
 
+// reorder_connectivity_RCM (mesh_ordering.cpp:231-252) on an arbitrary connectivity.
+// in: int64 {stride, n_elements, num_nodes}, int32 conn; out: int32 old_to_new, int32 conn.
+int mode_rcm(const char* in, const char* out, bool reorder_elements)
+{
+    std::ifstream f(in, std::ios::binary);
+    int64_t hdr[3];
+    f.read(reinterpret_cast<char*>(hdr), sizeof(hdr));
+    std::vector<int> conn;
+    read_into(f, conn, (size_t)(hdr[0] * hdr[1]));
+    const ReorderResult r = reorder_connectivity_RCM(conn.data(), (int)hdr[0], (int)hdr[1], (int)hdr[2], reorder_elements);
+    std::ofstream o(out, std::ios::binary);
+    o.write(reinterpret_cast<const char*>(r.old_to_new.data()), sizeof(int) * r.old_to_new.size());
+    o.write(reinterpret_cast<const char*>(conn.data()), sizeof(int) * conn.size());
+    return o ? 0 : 1;
+}
+
 int main(int argc, char** argv)
 {
     if (argc >= 11 && std::string(argv[1]) == "mesh") return mode_mesh(argv + 2);
+    if (argc >= 5 && std::string(argv[1]) == "rcm") return mode_rcm(argv[2], argv[3], std::atoi(argv[4]) != 0);
     if (argc < 4) {
         std::cerr << "usage: symx_ref_harness elem|project|eval|solve <in> <out> [threads] [max_newton] [cg_rel_tol]\n";
         return 1;

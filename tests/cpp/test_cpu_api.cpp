@@ -212,6 +212,27 @@ int mesh(char** a)
     return write_mesh<double>(type, n, {std::atof(a[5]), std::atof(a[6]), std::atof(a[7])}, a[8]);
 }
 
+// reorder_connectivity_RCM on a connectivity file: in int64 {stride, n_elements, num_nodes},
+// int32 conn; out int32 old_to_new, int32 conn.
+int rcm(const char* in, const char* out, bool reorder_elements)
+{
+    std::FILE* f = std::fopen(in, "rb");
+    if (!f) return 1;
+    int64_t hdr[3];
+    if (std::fread(hdr, sizeof(hdr), 1, f) != 1) return 1;
+    std::vector<int> conn((size_t)(hdr[0] * hdr[1]));
+    if (std::fread(conn.data(), sizeof(int), conn.size(), f) != conn.size()) return 1;
+    std::fclose(f);
+    const symx::ReorderResult r =
+        symx::reorder_connectivity_RCM(conn.data(), (int)hdr[0], (int)hdr[1], (int)hdr[2], reorder_elements);
+    f = std::fopen(out, "wb");
+    if (!f) return 1;
+    std::fwrite(r.old_to_new.data(), sizeof(int), r.old_to_new.size(), f);
+    std::fwrite(conn.data(), sizeof(int), conn.size(), f);
+    std::fclose(f);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 2) return 2;
@@ -221,6 +242,7 @@ int main(int argc, char** argv)
         if (mode == "nh_elem" && argc >= 4) return nh_elem(argv[2], argv[3]);
         if (mode == "nvrtc") return nvrtc(argc >= 3 ? argv[2] : "");
         if (mode == "mesh" && argc >= 11) return mesh(argv + 2);  // prec type nx ny nz sx sy sz out
+        if (mode == "rcm" && argc >= 5) return rcm(argv[2], argv[3], std::atoi(argv[4]) != 0);
     } catch (const std::exception& e) {
         std::printf("exception: %s\n", e.what());
         return 3;

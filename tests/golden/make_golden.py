@@ -17,6 +17,8 @@ Fixtures:
   <case>_solve.npz     final positions and iteration counts of NewtonsMethod::solve
   tet4_5c_modes.npz    NewtonsMethod::solve in each ProjectionToPD mode (indefinite start)
   meshes.npz           generate_cuboid_mesh (mesh_generation.cpp:306-327) for each element type
+  rcm.npz              reorder_connectivity_RCM (mesh_ordering.cpp:231-252) on relabelled,
+                        disconnected connectivities with isolated nodes
 """
 from __future__ import annotations
 
@@ -238,12 +240,53 @@ def make_meshes(tmp):
     return out
 
 
+def rcm_inputs():
+    """Seeded connectivities for reorder_connectivity_RCM: (stride, num_nodes, conn, reorder_elements)."""
+    rng = np.random.default_rng(21)
+    cases = []
+    # two disjoint Tet4 boxes and three isolated nodes, nodes and elements shuffled
+    _, a = problems.cuboid_tet4(3, 2, 2, (1.0, 1.0, 1.0))
+    _, b = problems.cuboid_tet4(2, 2, 1, (1.0, 1.0, 1.0))
+    na = int(a.max()) + 1
+    conn = np.concatenate([a, b + na])
+    nn = int(conn.max()) + 1 + 3
+    perm = rng.permutation(nn).astype(np.int32)
+    cases.append((4, nn, perm[conn][rng.permutation(conn.shape[0])], 1))
+    # a relabelled Hex8 box, elements kept in place
+    _, h = problems.cuboid_hex8(3, 3, 2, (1.0, 1.0, 1.0))
+    nn = int(h.max()) + 1
+    cases.append((8, nn, rng.permutation(nn).astype(np.int32)[h], 0))
+    # a relabelled Tet10 box
+    _, t = problems.cuboid_tet10(2, 1, 2, (1.0, 1.0, 1.0))
+    nn = int(t.max()) + 1
+    cases.append((10, nn, rng.permutation(nn).astype(np.int32)[t][rng.permutation(t.shape[0])], 1))
+    return cases
+
+
+def make_rcm(tmp):
+    out = {}
+    for i, (stride, nn, conn, reorder) in enumerate(rcm_inputs()):
+        fin, fout = os.path.join(tmp, f"rcm{i}.in"), os.path.join(tmp, f"rcm{i}.out")
+        with open(fin, "wb") as f:
+            np.array([stride, conn.shape[0], nn], dtype=np.int64).tofile(f)
+            np.ascontiguousarray(conn, dtype=np.int32).tofile(f)
+        run("rcm", fin, fout, reorder)
+        res = np.fromfile(fout, dtype=np.int32)
+        out[f"in_{i}"] = conn.astype(np.int32)
+        out[f"meta_{i}"] = np.array([stride, nn, reorder], dtype=np.int64)
+        out[f"old_to_new_{i}"] = res[:nn]
+        out[f"conn_{i}"] = res[nn:].reshape(conn.shape)
+    np.savez_compressed(os.path.join(HERE, "rcm.npz"), **out)
+    return out
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -f oracle/Makefile.ref -j8")
-    if sys.argv[1:] == ["meshes"]:  # only the mesh-generator fixture
+    if sys.argv[1:] == ["meshes"]:  # only the mesh-generator and ordering fixtures
         with tempfile.TemporaryDirectory() as tmp:
             make_meshes(tmp)
+            make_rcm(tmp)
         return
     if sys.argv[1:] == ["modes"]:  # only the projection-mode fixture
         with tempfile.TemporaryDirectory() as tmp:
@@ -265,6 +308,7 @@ def main():
         make_case(tmp, "tet10_2", keep_triplets=False)
         make_modes(tmp)
         make_meshes(tmp)
+        make_rcm(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 

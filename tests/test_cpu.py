@@ -316,3 +316,24 @@ def test_c_abi_mesh_generator_matches_reference(golden):
     assert p["conn"].shape == (6 * nx * ny * nz, 4)
     assert p["bc_idx"].size == (ny + 1) * (nz + 1)
     assert np.min(p["X"]) == 0.0
+
+
+def test_cpp_rcm_reorder_matches_reference(cpp_test, golden, tmp_path):
+    """reorder_connectivity_RCM on shuffled labels, two components and isolated nodes (one
+    pseudo-peripheral root per component), with and without the element walk: the node
+    permutation and the reordered connectivity equal the reference's."""
+    d = golden("rcm")
+    i = 0
+    while f"meta_{i}" in d:
+        stride, nn, reorder = (int(v) for v in d[f"meta_{i}"])
+        conn = d[f"in_{i}"]
+        fin, fout = tmp_path / f"rcm{i}.in", tmp_path / f"rcm{i}.out"
+        with open(fin, "wb") as f:
+            np.array([stride, conn.shape[0], nn], dtype=np.int64).tofile(f)
+            conn.astype(np.int32).tofile(f)
+        subprocess.run([cpp_test, "rcm", str(fin), str(fout), str(reorder)], check=True)
+        res = np.fromfile(fout, dtype=np.int32)
+        np.testing.assert_array_equal(res[:nn], d[f"old_to_new_{i}"], err_msg=f"case {i}")
+        np.testing.assert_array_equal(res[nn:].reshape(conn.shape), d[f"conn_{i}"], err_msg=f"case {i}")
+        i += 1
+    assert i == 3
