@@ -22,6 +22,7 @@
 //   symx_ref_harness solve   <problem.bin> <outdir> <thr> [max_newton] [cg_rel_tol] [projection mode]
 //   symx_ref_harness mesh    d|f <type> <nx> <ny> <nz> <sx> <sy> <sz> <out.bin>   generate_cuboid_mesh
 //   symx_ref_harness rcm     <in.bin> <out.bin> <reorder_elements 0|1>           reorder_connectivity_RCM
+//   symx_ref_harness elem27  <in.bin> <out.bin>            NH Hex27 [E, g(81)] over get_integration_rule(Hex27)
 #include <symx>
 #include <Eigen/Sparse>
 
@@ -379,6 +380,49 @@ int mode_mesh(char** a)
     return write_mesh<double>(type, n, Eigen::Vector3d(std::atof(a[5]), std::atof(a[6]), std::atof(a[7])), a[8]);
 }
 
+// Neo-Hookean Hex27 element: E and dE/dx summed over get_integration_rule(Hex27)
+// (fem_integrators.cpp:83-113) with fem_jacobian's triquadratic shape functions
+// (fem_integrators.h:101-147).  in: int64 n, then n x 164 f64 rows [x (81), X (81), mu, lambda];
+// out: n x 82 [E, g(81)].
+int mode_elem27(const std::string& in, const std::string& out)
+{
+    std::ifstream f(in, std::ios::binary);
+    int64_t n = 0;
+    f.read(reinterpret_cast<char*>(&n), sizeof(n));
+    std::vector<double> rows;
+    read_into(f, rows, (size_t)n * 164);
+    Workspace ws;
+    std::vector<Vector> x = ws.make_vectors(3, 27), X = ws.make_vectors(3, 27);
+    Vector xi = ws.make_vectors(3, 1)[0];
+    Scalar mu = ws.make_scalar(), lam = ws.make_scalar();
+    Matrix Jx = fem_jacobian(FEM_Element::Hex27, x, xi);
+    Matrix JX = fem_jacobian(FEM_Element::Hex27, X, xi);
+    Matrix F = Jx * JX.inv();
+    Scalar logdetF = log(F.det());
+    Scalar psi = 0.5 * mu * ((F.transpose() * F).trace() - 3.0) - mu * logdetF + 0.5 * lam * logdetF.powN(2);
+    Compiled<double> c(value_gradient(psi * JX.det(), collect_scalars(x)), "ref_harness_nh_hex27_vg",
+                       symx::get_codegen_dir());
+    const std::vector<std::array<double, 4>> rule = get_integration_rule(FEM_Element::Hex27);
+    std::vector<double> result((size_t)n * 82, 0.0);
+    for (int64_t e = 0; e < n; ++e) {
+        const double* r = rows.data() + 164 * e;
+        for (int v = 0; v < 27; ++v)
+            for (int d = 0; d < 3; ++d) {
+                c.set(x[v][d], r[3 * v + d]);
+                c.set(X[v][d], r[81 + 3 * v + d]);
+            }
+        c.set(mu, r[162]);
+        c.set(lam, r[163]);
+        for (const auto& q : rule) {
+            for (int d = 0; d < 3; ++d) c.set(xi[d], q[1 + d]);
+            View<double> o = c.run();
+            for (int i = 0; i < 82; ++i) result[82 * e + i] += q[0] * o[i];
+        }
+    }
+    write_raw(out, result.data(), result.size());
+    return 0;
+}
+
 // reorder_connectivity_RCM (mesh_ordering.cpp:231-252) on an arbitrary connectivity.
 // in: int64 {stride, n_elements, num_nodes}, int32 conn; out: int32 old_to_new, int32 conn.
 int mode_rcm(const char* in, const char* out, bool reorder_elements)
@@ -407,6 +451,7 @@ int main(int argc, char** argv)
     const std::string mode = argv[1];
     const int n_threads = argc > 4 ? std::atoi(argv[4]) : 1;
     if (mode == "elem") return mode_elem(argv[2], argv[3]);
+    if (mode == "elem27") return mode_elem27(argv[2], argv[3]);
     if (mode == "project") return mode_project(argv[2], argv[3]);
     if (mode == "eval") return mode_eval(argv[2], argv[3], n_threads);
     if (mode == "solve") {

@@ -39,7 +39,22 @@ std::vector<std::array<double, 4>> get_integration_rule(const FEM_Element& e)
         const double w = 0.041666667, a = 0.58541020, b = 0.13819660;
         return {{w, a, b, b}, {w, b, a, b}, {w, b, b, a}, {w, b, b, b}};
     }
-    throw std::runtime_error("symx_gb300: integration rule available for Tet4, Tet10 and Hex8");
+    if (e == FEM_Element::Hex27) {
+        // 3x3x3 Gauss-Legendre, products of the 1-D weights 5/9 and 8/9 at -p, 0, p with
+        // p = sqrt(3/5): corners, edge, face and centre points in the reference's order and
+        // with its rounded values (symx/src/solver/fem_integrators.cpp:83-113)
+        const double p = 0.7745966692;
+        const double wc = 0.1714677641, we = 0.2743484225, wf = 0.4389574760, w0 = 0.7023319616;
+        return {{wc, -p, -p, -p}, {wc, p, -p, -p}, {wc, -p, p, -p}, {wc, p, p, -p},
+                {wc, -p, -p, p},  {wc, p, -p, p},  {wc, -p, p, p},  {wc, p, p, p},
+                {we, 0.0, -p, -p}, {we, -p, 0.0, -p}, {we, p, 0.0, -p}, {we, 0.0, p, -p},
+                {we, -p, -p, 0.0}, {we, p, -p, 0.0}, {we, -p, p, 0.0}, {we, p, p, 0.0},
+                {we, 0.0, -p, p},  {we, -p, 0.0, p},  {we, p, 0.0, p},  {we, 0.0, p, p},
+                {wf, 0.0, 0.0, -p}, {wf, 0.0, -p, 0.0}, {wf, -p, 0.0, 0.0},
+                {wf, p, 0.0, 0.0},  {wf, 0.0, p, 0.0},  {wf, 0.0, 0.0, p},
+                {w0, 0.0, 0.0, 0.0}};
+    }
+    throw std::runtime_error("symx_gb300: unknown element type");
 }
 
 Vector fem_interpolation(const FEM_Element& e, const std::vector<Vector>& vh, const Vector& xi)
@@ -61,8 +76,25 @@ Vector fem_interpolation(const FEM_Element& e, const std::vector<Vector>& vh, co
         N = {n0 * (2.0 * n0 - 1.0), n1 * (2.0 * n1 - 1.0), n2 * (2.0 * n2 - 1.0), n3 * (2.0 * n3 - 1.0),
              4.0 * n0 * n1,         4.0 * n1 * n2,         4.0 * n2 * n0,         4.0 * n0 * n3,
              4.0 * n1 * n3,         4.0 * n2 * n3};
+    } else if (e == FEM_Element::Hex27) {
+        // triquadratic Lagrange: per axis L-(t) = t(t-1)/2, L+(t) = t(t+1)/2, L0(t) = 1-t^2,
+        // nodes ordered corners, mid-edges (z = -1 ring, z = +1 ring, vertical), faces
+        // (x-, x+, y+, y-, z-, z+), centre, as the reference's Hex27 mesh and shape functions
+        if (vh.size() != 27) throw std::runtime_error("symx: Hex27 interpolation needs 27 nodes");
+        std::array<std::array<Scalar, 3>, 3> L{};  // L[axis][0: -1, 1: 0, 2: +1]
+        for (int k = 0; k < 3; ++k) {
+            const Scalar& t = xi[k];
+            L[k][0] = 0.5 * t * (t - 1.0);
+            L[k][1] = 1.0 - t * t;
+            L[k][2] = 0.5 * t * (t + 1.0);
+        }
+        static const int at[27][3] = {{0, 0, 0}, {2, 0, 0}, {2, 2, 0}, {0, 2, 0}, {0, 0, 2}, {2, 0, 2}, {2, 2, 2},
+                                      {0, 2, 2}, {1, 0, 0}, {2, 1, 0}, {1, 2, 0}, {0, 1, 0}, {1, 0, 2}, {2, 1, 2},
+                                      {1, 2, 2}, {0, 1, 2}, {0, 0, 1}, {2, 0, 1}, {2, 2, 1}, {0, 2, 1}, {0, 1, 1},
+                                      {2, 1, 1}, {1, 2, 1}, {1, 0, 1}, {1, 1, 0}, {1, 1, 2}, {1, 1, 1}};
+        for (const auto& a : at) N.push_back(L[0][a[0]] * L[1][a[1]] * L[2][a[2]]);
     } else {
-        throw std::runtime_error("symx_gb300: interpolation available for Tet4, Tet10 and Hex8");
+        throw std::runtime_error("symx_gb300: unknown element type");
     }
     Vector x = vh[0] * N[0];
     for (size_t a = 1; a < vh.size(); ++a) x = x + vh[a] * N[a];

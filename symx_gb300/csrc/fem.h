@@ -1,6 +1,7 @@
 // FEM helpers for potential definitions (reference: symx/src/solver/fem_integrators.{h,cpp}).
-// Shape functions and quadrature rules for Tet4 (1 point, weight 1/6) and Hex8
-// (2x2x2 Gauss, weight 1, +-1/sqrt(3)); fem_integrator registers the rule as a
+// Shape functions and quadrature rules for Tet4 (1 point, weight 1/6), Tet10 (4 points),
+// Hex8 (2x2x2 Gauss, weight 1, +-1/sqrt(3)) and Hex27 (3x3x3 Gauss, triquadratic
+// Lagrange); fem_integrator registers the rule as a
 // summation, so the element kernel runs the summand once per quadrature point.
 #pragma once
 

@@ -105,6 +105,45 @@ static int nh_elem(const char* in, const char* out)
     return 0;
 }
 
+// Neo-Hookean Hex27 element, E and dE/dx summed over get_integration_rule(Hex27), evaluated on
+// the host.  in: int64 n, n x 164 rows [x (81), X (81), mu, lambda]; out: n x 82 [E, g(81)].
+static int nh_elem27(const char* in, const char* out)
+{
+    std::ifstream f(in, std::ios::binary);
+    int64_t n = 0;
+    f.read(reinterpret_cast<char*>(&n), sizeof(n));
+    std::vector<double> rows(164 * n);
+    f.read(reinterpret_cast<char*>(rows.data()), sizeof(double) * rows.size());
+    Workspace ws;
+    std::vector<Vector> x = ws.make_vectors(3, 27), X = ws.make_vectors(3, 27);
+    Vector xi = ws.make_vectors(3, 1)[0];
+    Scalar mu = ws.make_scalar(), lam = ws.make_scalar();
+    Matrix Jx = fem_jacobian(FEM_Element::Hex27, x, xi), JX = fem_jacobian(FEM_Element::Hex27, X, xi);
+    Matrix F = Jx * JX.inv();
+    Scalar logJ = log(F.det());
+    Scalar psi = 0.5 * mu * ((F.transpose() * F).trace() - 3.0) - mu * logJ + 0.5 * lam * logJ.powN(2);
+    std::vector<Scalar> vg = value_gradient(psi * JX.det(), collect_scalars(x));
+    const auto rule = get_integration_rule(FEM_Element::Hex27);
+    std::vector<double> res(82 * n, 0.0);
+    for (int64_t e = 0; e < n; ++e) {
+        const double* r = &rows[164 * e];
+        for (int v = 0; v < 27; ++v)
+            for (int d = 0; d < 3; ++d) {
+                x[v][d].set_value(r[3 * v + d]);
+                X[v][d].set_value(r[81 + 3 * v + d]);
+            }
+        mu.set_value(r[162]);
+        lam.set_value(r[163]);
+        for (const auto& q : rule) {
+            for (int d = 0; d < 3; ++d) xi[d].set_value(q[1 + d]);
+            for (int k = 0; k < 82; ++k) res[82 * e + k] += q[0] * vg[k].eval();
+        }
+    }
+    std::ofstream o(out, std::ios::binary);
+    o.write(reinterpret_cast<const char*>(res.data()), sizeof(double) * res.size());
+    return 0;
+}
+
 static int nvrtc(const char* cache_dir)
 {
     (void)cache_dir;
@@ -240,6 +279,7 @@ int main(int argc, char** argv)
     try {
         if (mode == "selftest") return selftest();
         if (mode == "nh_elem" && argc >= 4) return nh_elem(argv[2], argv[3]);
+        if (mode == "nh_elem27" && argc >= 4) return nh_elem27(argv[2], argv[3]);
         if (mode == "nvrtc") return nvrtc(argc >= 3 ? argv[2] : "");
         if (mode == "mesh" && argc >= 11) return mesh(argv + 2);  // prec type nx ny nz sx sy sz out
         if (mode == "rcm" && argc >= 5) return rcm(argv[2], argv[3], std::atoi(argv[4]) != 0);

@@ -17,6 +17,7 @@ Fixtures:
   <case>_solve.npz     final positions and iteration counts of NewtonsMethod::solve
   tet4_5c_modes.npz    NewtonsMethod::solve in each ProjectionToPD mode (indefinite start)
   meshes.npz           generate_cuboid_mesh (mesh_generation.cpp:306-327) for each element type
+  elem_nh_hex27.npz    NH Hex27 [E, g(81)] over the reference's Hex27 rule and shape functions
   rcm.npz              reorder_connectivity_RCM (mesh_ordering.cpp:231-252) on relabelled,
                         disconnected connectivities with isolated nodes
 """
@@ -240,6 +241,34 @@ def make_meshes(tmp):
     return out
 
 
+# Hex27 node positions in half cells (the reference's node order, mesh_generation.cpp:253-295)
+HEX27_AT = [(0, 0, 0), (2, 0, 0), (2, 2, 0), (0, 2, 0), (0, 0, 2), (2, 0, 2), (2, 2, 2), (0, 2, 2),
+            (1, 0, 0), (2, 1, 0), (1, 2, 0), (0, 1, 0), (1, 0, 2), (2, 1, 2), (1, 2, 2), (0, 1, 2),
+            (0, 0, 1), (2, 0, 1), (2, 2, 1), (0, 2, 1), (0, 1, 1), (2, 1, 1), (1, 2, 1), (1, 0, 1),
+            (1, 1, 0), (1, 1, 2), (1, 1, 1)]
+
+
+def make_elem27(tmp, n=6):
+    rng = np.random.default_rng(27)
+    base = 0.005 * np.array(HEX27_AT, dtype=np.float64)  # 1 cm cube
+    rows = []
+    for _ in range(n):
+        X = base + 2e-4 * (rng.random(base.shape) - 0.5)
+        A = np.eye(3) + 0.15 * (rng.random((3, 3)) - 0.5)
+        x = X @ A.T + 3e-4 * (rng.random(base.shape) - 0.5)
+        mu, lam = problems.lame(1e5 * np.exp(0.3 * rng.standard_normal()), 0.3)
+        rows.append(np.concatenate([x.ravel(), X.ravel(), [mu, lam]]))
+    rows = np.array(rows)
+    fin, fout = os.path.join(tmp, "e27.in"), os.path.join(tmp, "e27.out")
+    with open(fin, "wb") as f:
+        np.array([n], dtype=np.int64).tofile(f)
+        rows.tofile(f)
+    run("elem27", fin, fout)
+    out = np.fromfile(fout).reshape(n, 82)
+    np.savez_compressed(os.path.join(HERE, "elem_nh_hex27.npz"), inputs=rows, outputs=out)
+    return out
+
+
 def rcm_inputs():
     """Seeded connectivities for reorder_connectivity_RCM: (stride, num_nodes, conn, reorder_elements)."""
     rng = np.random.default_rng(21)
@@ -287,6 +316,7 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             make_meshes(tmp)
             make_rcm(tmp)
+            print(make_elem27(tmp)[:, :3])
         return
     if sys.argv[1:] == ["modes"]:  # only the projection-mode fixture
         with tempfile.TemporaryDirectory() as tmp:
@@ -309,6 +339,7 @@ def main():
         make_modes(tmp)
         make_meshes(tmp)
         make_rcm(tmp)
+        make_elem27(tmp)
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 

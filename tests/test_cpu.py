@@ -337,3 +337,18 @@ def test_cpp_rcm_reorder_matches_reference(cpp_test, golden, tmp_path):
         np.testing.assert_array_equal(res[nn:].reshape(conn.shape), d[f"conn_{i}"], err_msg=f"case {i}")
         i += 1
     assert i == 3
+
+
+def test_cpp_hex27_element_matches_reference(cpp_test, golden, tmp_path):
+    """Hex27: the triquadratic shape functions, node order and 27-point rule give the reference's
+    Neo-Hookean element energy and gradient (six distorted elements)."""
+    d = golden("elem_nh_hex27")
+    rows, ref = d["inputs"], d["outputs"]
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        np.array([rows.shape[0]], dtype=np.int64).tofile(f)
+        rows.tofile(f)
+    subprocess.run([cpp_test, "nh_elem27", str(fin), str(fout)], check=True)
+    out = np.fromfile(fout).reshape(-1, 82)
+    assert np.max(np.abs(out[:, 0] - ref[:, 0])) <= 1e-12 * np.max(np.abs(ref[:, 0]))
+    assert np.max(np.abs(out[:, 1:] - ref[:, 1:])) <= 1e-12 * np.max(np.abs(ref[:, 1:]))
