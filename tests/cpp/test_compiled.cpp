@@ -415,6 +415,54 @@ static void nogpu(const std::string& dir)
     REQUIRE(!f.is_valid() && !get_check_mode_ON() && is_load_compiled_enabled());
 }
 
+// Neo-Hookean Hex27 element through Compiled<double> on the GPU: E and dE/dx per quadrature
+// point, summed over get_integration_rule(Hex27), against the reference's sums (n x 82).
+static void nh_hex27(const std::string& dir, const char* in_path, const char* ref_path)
+{
+    std::ifstream fi(in_path, std::ios::binary), fr(ref_path, std::ios::binary);
+    int64_t n = 0;
+    fi.read(reinterpret_cast<char*>(&n), sizeof(n));
+    std::vector<double> rows(164 * n), ref(82 * n);
+    fi.read(reinterpret_cast<char*>(rows.data()), sizeof(double) * rows.size());
+    fr.read(reinterpret_cast<char*>(ref.data()), sizeof(double) * ref.size());
+    REQUIRE(fi.good() && fr.good() && n > 0);
+    Workspace ws;
+    std::vector<Vector> x = ws.make_vectors(3, 27), X = ws.make_vectors(3, 27);
+    Vector xi = ws.make_vectors(3, 1)[0];
+    Scalar mu = ws.make_scalar(), lam = ws.make_scalar();
+    Matrix Jx = fem_jacobian(FEM_Element::Hex27, x, xi), JX = fem_jacobian(FEM_Element::Hex27, X, xi);
+    Matrix F = Jx * JX.inv();
+    Scalar logJ = log(F.det());
+    Scalar psi = 0.5 * mu * ((F.transpose() * F).trace() - 3.0) - mu * logJ + 0.5 * lam * logJ.powN(2);
+    Compiled<double> c(value_gradient(psi * JX.det(), collect_scalars(x)), "nh_hex27_vg", dir);
+    const auto rule = get_integration_rule(FEM_Element::Hex27);
+    double scale_e = 0.0, scale_g = 0.0, err_e = 0.0, err_g = 0.0;
+    for (int64_t e = 0; e < n; ++e) {
+        const double* r = &rows[164 * e];
+        for (int v = 0; v < 27; ++v)
+            for (int d = 0; d < 3; ++d) {
+                c.set(x[v][d], r[3 * v + d]);
+                c.set(X[v][d], r[81 + 3 * v + d]);
+            }
+        c.set(mu, r[162]);
+        c.set(lam, r[163]);
+        std::vector<double> sum(82, 0.0);
+        for (const auto& q : rule) {
+            for (int d = 0; d < 3; ++d) c.set(xi[d], q[1 + d]);
+            const View<double> o = c.run();
+            for (int k = 0; k < 82; ++k) sum[k] += q[0] * o[k];
+        }
+        scale_e = std::max(scale_e, std::abs(ref[82 * e]));
+        err_e = std::max(err_e, std::abs(sum[0] - ref[82 * e]));
+        for (int k = 1; k < 82; ++k) {
+            scale_g = std::max(scale_g, std::abs(ref[82 * e + k]));
+            err_g = std::max(err_g, std::abs(sum[k] - ref[82 * e + k]));
+        }
+    }
+    std::printf("hex27: max |dE| %.3e of %.3e, max |dg| %.3e of %.3e\n", err_e, scale_e, err_g, scale_g);
+    REQUIRE(err_e <= 1e-12 * scale_e && err_g <= 1e-12 * scale_g);
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 3) {
@@ -434,6 +482,8 @@ int main(int argc, char** argv)
             check_mode(dir);
             batches(dir);
             nh_tet4(dir, argv[3], argv[4]);
+        } else if (mode == "hex27" && argc == 5) {
+            nh_hex27(dir, argv[3], argv[4]);
         } else {
             std::printf("bad arguments\n");
             return 2;

@@ -27,3 +27,22 @@ def test_cpp_compiled_on_gpu(compiled_test, golden, tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "compiled PASS" in r.stdout
+
+
+def test_cpp_compiled_hex27_element_on_gpu(compiled_test, golden, tmp_path):
+    """A Hex27 Neo-Hookean element (81 DoFs, 27 quadrature points) through Compiled<double> on the
+    GPU gives the reference's energy and gradient within 1e-12."""
+    d = golden("elem_nh_hex27")
+    rows, ref = d["inputs"], d["outputs"]
+    fin, fref = tmp_path / "in.bin", tmp_path / "ref.bin"
+    with open(fin, "wb") as f:
+        np.array([rows.shape[0]], dtype=np.int64).tofile(f)
+        np.ascontiguousarray(rows, dtype=np.float64).tofile(f)
+    np.ascontiguousarray(ref, dtype=np.float64).tofile(fref)
+    folder = tmp_path / "codegen"
+    folder.mkdir()
+    r = subprocess.run([compiled_test, "hex27", str(folder), str(fin), str(fref)], capture_output=True, text=True,
+                       timeout=600)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "compiled PASS" in r.stdout
