@@ -106,7 +106,7 @@ def measured_peaks():
 
 def workload_name(name, p):
     cfg = __import__("symx_gb300.problems", fromlist=["CONFIGS"]).CONFIGS.get(name, {})
-    kind = "Tet4" if p["conn"].shape[1] == 4 else "Hex8 (2x2x2 Gauss points)"
+    kind = {4: "Tet4", 10: "Tet10 (4 quadrature points)"}.get(p["conn"].shape[1], "Hex8 (2x2x2 Gauss points)")
     cells = "x".join(str(c) for c in cfg.get("cells", ())) or "custom"
     return (f"Neo-Hookean {kind} implicit-Euler step, {cells} cells ({p['X'].shape[0]:,} vertices, "
             f"{p['conn'].shape[0]:,} elements)")
@@ -115,6 +115,8 @@ def workload_name(name, p):
 def projection_kernel(p):
     if p["conn"].shape[1] == 4:
         return "k_project_pd_deflated<float,12> + k_project_pd_listed<float,12> (fallback list)"
+    if p["conn"].shape[1] == 10:
+        return "k_project_pd_generic<float> (30 x 30, one thread per matrix, cyclic Jacobi)"
     return "k_project_pd_pairs<float,24> (one warp per matrix, pair-block parallel Jacobi)"
 
 
@@ -326,7 +328,7 @@ def cpu_baseline(p, args):
     what = "the complete" if n <= 0 else f"the first {its} Newton iterations of the"
     return {"value": round(st["t_total"] * 1e3 / its, 3), "unit": UNIT + " per Newton step", "cores": threads,
             "kind": "port",
-            "sample": f"{what} tet4_64 solve (oracle port, OpenMP): {its} Newton / {st['cg_iterations']} CG "
+            "sample": f"{what} {args.config} solve (oracle port, OpenMP): {its} Newton / {st['cg_iterations']} CG "
                       f"iterations in {st['t_total']:.1f} s",
             "stage_seconds": {k: round(st[k], 3) for k in ("t_eval", "t_project", "t_assembly", "t_linear_solve",
                                                             "t_line_search")}}

@@ -180,6 +180,9 @@ CONFIGS = {
                     init_perturb=0.1),
     # Quadratic tetrahedra (30 x 30 element Hessians, 4 quadrature points).
     "tet10_2": dict(kind="tet10", cells=(3, 2, 2), h=0.01, perturb=0.05, seed=14),
+    # Quadratic tetrahedra at scale: 32^3 cells, 274,625 nodes (the 64^3 Tet4 node count),
+    # 196,608 elements with 30 x 30 Hessians.
+    "tet10_32": dict(kind="tet10", cells=(32, 32, 32), h=0.02, perturb=0.05, seed=15),
     # The 64^3 step on the reference's own mesh: generate_cuboid_Tet4_mesh with its reverse
     # Cuthill-McKee node numbering and element order (same statistics, other per-node draws).
     "tet4_64_rcm": dict(kind="tet4", cells=(64, 64, 64), h=0.01, perturb=0.05, seed=1, numbering="rcm"),
