@@ -104,20 +104,35 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+ELEMENT_KINDS = {4: "Tet4", 10: "Tet10 (4 quadrature points)", 8: "Hex8 (2x2x2 Gauss points)"}
+
+
+def element_kind(p):
+    nodes = p["conn"].shape[1]
+    if nodes not in ELEMENT_KINDS:
+        raise ValueError(f"no bench description for elements with {nodes} nodes")
+    return nodes
+
+
 def workload_name(name, p):
     cfg = __import__("symx_gb300.problems", fromlist=["CONFIGS"]).CONFIGS.get(name, {})
-    kind = {4: "Tet4", 10: "Tet10 (4 quadrature points)"}.get(p["conn"].shape[1], "Hex8 (2x2x2 Gauss points)")
+    kind = ELEMENT_KINDS[element_kind(p)]
     cells = "x".join(str(c) for c in cfg.get("cells", ())) or "custom"
     return (f"Neo-Hookean {kind} implicit-Euler step, {cells} cells ({p['X'].shape[0]:,} vertices, "
             f"{p['conn'].shape[0]:,} elements)")
 
 
 def projection_kernel(p):
-    if p["conn"].shape[1] == 4:
-        return "k_project_pd_deflated<float,12> + k_project_pd_listed<float,12> (fallback list)"
-    if p["conn"].shape[1] == 10:
-        return "k_project_pd_generic<float> (30 x 30, one thread per matrix, cyclic Jacobi)"
-    return "k_project_pd_pairs<float,24> (one warp per matrix, pair-block parallel Jacobi)"
+    return {4: "k_project_pd_sort<float,12> + k_project_pd_deflated_listed<float,12> + k_project_pd_listed<float,12>",
+            10: "k_project_pd_generic<float> (30 x 30, one thread per matrix, cyclic Jacobi)",
+            8: "k_project_pd_pairs<float,24> (one warp per matrix, pair-block parallel Jacobi)"}[element_kind(p)]
+
+
+def working_set(p):
+    """Device bytes of the element Hessians (f32) and the BCSR values the timed solve streams."""
+    m = 3 * p["conn"].shape[1]
+    h_bytes = p["conn"].shape[0] * m * m * 4
+    return f"working set > L2 (element Hessians {h_bytes / 1e9:.2f} GB f32, plus the BCSR matrix)"
 
 
 def spmv_roofline(solver, torch, sg, n_rep=30):
@@ -275,7 +290,7 @@ def run_ours(args):
         "config": {"workload": workload_name(args.config, p),
                    "name": args.config, "precision": "mixed", "newton_iterations": newton_its,
                    "cg_iterations": st["cg_iterations"], "final_residual": st["final_residual"],
-                   "l2": "working set > L2 (element Hessians 0.9 GB, BCSR 0.16 GB)",
+                   "l2": working_set(p),
                    "parallelism": "replicas only" if world > 1 else "single GPU"},
         "stage_seconds": {k: round(st[k], 6) for k in st if k.startswith("t_")},
         "fp64": {"ms_per_step": round(statistics.mean(fp64_ms), 3),
@@ -303,7 +318,27 @@ def run_ours(args):
         "clocks": clocks.summary(),
     }
     if args.cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(p, args)
+        out["cpu_baseline"], x_oracle, oracle_stats = cpu_baseline(p, args)
+        if x_oracle is not None:
+            out["oracle_parity"] = oracle_parity(p, x_oracle, oracle_stats,
+                                                 {"mixed": (x_mixed, st), "fp64": (x_fp64, fp64_st)})
+    return out
+
+
+def oracle_parity(p, x_oracle, oracle_stats, runs):
+    """Final positions of the GPU solves against the oracle's complete FP64 solve of the same
+    inputs: relative to |x_oracle| and to the step's displacement |x_oracle - x0|."""
+    disp = float(np.linalg.norm(x_oracle - p["x0"]))
+    nrm = float(np.linalg.norm(x_oracle))
+    out = {"oracle": "FP64 CPU restatement of the reference's solve (complete solve, same inputs)",
+           "oracle_newton_iterations": int(oracle_stats["newton_iterations"]),
+           "oracle_cg_iterations": int(oracle_stats["cg_iterations"]),
+           "oracle_final_residual": float(oracle_stats["final_residual"])}
+    for name, (x, st) in runs.items():
+        d = float(np.linalg.norm(x - x_oracle))
+        out[name] = {"rel_err": d / nrm, "rel_err_displacement": d / disp,
+                     "max_abs_err_m": float(np.max(np.abs(x - x_oracle))),
+                     "newton_iterations": int(st["newton_iterations"]), "cg_iterations": int(st["cg_iterations"])}
     return out
 
 
@@ -326,12 +361,13 @@ def cpu_baseline(p, args):
     st = P.solve(oracle_settings(O, n))
     its = max(1, st["newton_iterations"])
     what = "the complete" if n <= 0 else f"the first {its} Newton iterations of the"
+    x = P.get_x() if n <= 0 and st["solver_return"] == 0 else None
     return {"value": round(st["t_total"] * 1e3 / its, 3), "unit": UNIT + " per Newton step", "cores": threads,
             "kind": "port",
             "sample": f"{what} {args.config} solve (oracle port, OpenMP): {its} Newton / {st['cg_iterations']} CG "
                       f"iterations in {st['t_total']:.1f} s",
             "stage_seconds": {k: round(st[k], 3) for k in ("t_eval", "t_project", "t_assembly", "t_linear_solve",
-                                                            "t_line_search")}}
+                                                            "t_line_search")}}, x, st
 
 
 def run_profile(args):

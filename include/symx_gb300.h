@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SYMXG_ABI_VERSION 4
+#define SYMXG_ABI_VERSION 5
 
 /* status codes */
 #define SYMXG_OK 0
@@ -181,6 +181,17 @@ int symxg_generate_cuboid_mesh(int32_t element_type, const double size[3], const
 /* Number of CUDA kernels this library has launched since it was loaded (all handles). */
 int64_t symxg_launch_count(void);
 
+/* Bound on the waits inside the staged PCG kernels (no counterpart in the reference, whose
+ * CPU solver never waits on another processor).  Every wait of those kernels on a
+ * shared-memory stage or on the other blocks of the launch polls at most this many times;
+ * when one gives up, the kernel stops its work, waits (with the default bound) for its own
+ * copies in flight, flags the solve and returns, and the call fails with SYMXG_ERR_RUNTIME
+ * ("a bounded wait in the PCG kernels gave up").  The context stays usable.  Process-wide,
+ * read at each launch; polls < 0 restores the default (2^22).  A small value (0: give up
+ * without polling) makes the waits run out on purpose, to test a caller's error path. */
+void symxg_set_wait_poll_limit(int64_t polls);
+int64_t symxg_wait_poll_limit(void);
+
 /* ---- stand-alone kernels on caller-owned DEVICE memory (stream: a cudaStream_t or NULL) ---- */
 
 /* Project `count` symmetric n x n matrices (n = 3k <= 30), stored block-major (3x3 block
@@ -194,6 +205,8 @@ int symxg_project_pd_f64(double* matrices, int32_t n, int64_t count, double eps,
 /* y = A x for a 3x3-block CSR matrix: row_ptr (n_blocks+1), cols (nnzb) and values stored
  * component-major, i.e. component m (row-major inside the 3x3 block) of block k at
  * vals[m * vals_stride + k], vals_stride >= nnzb (the layout the solver's PCG uses).
+ * The SpMV runs asynchronously and cannot read row_ptr[n_blocks] back, so vals_stride >= nnzb
+ * is the caller's to ensure (the PCG calls below check it).
  * Replaces BlockedSparseMatrix::spmxv_from_ptr (BlockedSparseMatrix.h:986-1138). */
 int symxg_bcsr_spmv_f32(int32_t n_blocks, const int32_t* row_ptr, const int32_t* cols, const float* vals,
                         int64_t vals_stride, const float* x, float* y, void* stream);
@@ -213,7 +226,8 @@ typedef struct symxg_pcg_info {
 /* Solve A x = b with block-Jacobi PCG on the device: A as for symxg_bcsr_spmv_*, b and x
  * (3 * n_blocks) device arrays, x starting at zero.  Stops when sqrt(r.r/b.b) < abs_tol, when
  * it falls below rel_tol times its initial value, on p.Ap <= 0, or after max_iterations.
- * Every row must hold its diagonal block.  Allocates its workspace (about 150 bytes per block
+ * Every row must hold its diagonal block; vals_stride below row_ptr[n_blocks] fails with
+ * SYMXG_ERR_INVALID_ARGUMENT before any kernel runs.  Allocates its workspace (about 150 bytes per block
  * row in f32, 300 in f64) on each call and returns with `stream` synchronized.  Replaces
  * BlockedSparseMatrix::prepare_preconditioning (BlockedSparseMatrix.h:1147) followed by
  * bsm::solve_pcg (solve_pcg.h:83-232), as NewtonsMethod.cpp:427-446 calls them. */

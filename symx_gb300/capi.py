@@ -29,7 +29,7 @@ EXPORTS = [
     "symxg_project_pd_f64", "symxg_bcsr_spmv_f32", "symxg_bcsr_spmv_f64", "symxg_launch_count",
     "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64", "symxg_bcsr_pcg_f32_noalloc", "symxg_adjoint",
     "symxg_generate_cuboid_mesh",
-    "symxg_rollout_forward", "symxg_rollout_backward",
+    "symxg_rollout_forward", "symxg_rollout_backward", "symxg_set_wait_poll_limit", "symxg_wait_poll_limit",
 ]
 
 
@@ -132,6 +132,8 @@ def load(path: str | None = None):
         "symxg_last_error": ([], C.c_char_p),
         "symxg_abi_version": ([], C.c_int),
         "symxg_launch_count": ([], C.c_int64),
+        "symxg_set_wait_poll_limit": ([C.c_int64], None),
+        "symxg_wait_poll_limit": ([], C.c_int64),
         "symxg_default_settings": ([C.POINTER(NewtonSettings)], None),
         "symxg_elastic_create": ([C.POINTER(ElasticProblem), C.c_char_p, C.POINTER(P)], C.c_int),
         "symxg_destroy": ([P], C.c_int),

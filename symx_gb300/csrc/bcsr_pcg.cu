@@ -116,6 +116,16 @@ BcsrPcgResult run_bcsr_pcg(int n_blocks, const int32_t* row_ptr, const int32_t* 
     B.tickets = reinterpret_cast<unsigned*>(w + L.tickets);
     B.state = &hdr->st;
 
+    // The values array holds nine components of vals_stride entries each: a stride below the
+    // number of blocks, row_ptr[n_blocks], would alias the components or read past the array.
+    // Checked before the first kernel reads a value.
+    int32_t nnzb = 0;
+    ck(cudaMemcpyAsync(&nnzb, row_ptr + n_blocks, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "read row_ptr[n_blocks]");
+    ck(cudaStreamSynchronize(s), "synchronize");
+    if (nnzb < 0 || vals_stride < (int64_t)nnzb)
+        throw std::invalid_argument("bcsr_pcg: vals_stride " + std::to_string(vals_stride) +
+                                    " is smaller than the number of blocks row_ptr[n_blocks] = " + std::to_string(nnzb));
+
     // The completion tickets and the missing-diagonal counter must start at zero.
     Header h{};
     h.st.abs_tol = abs_tol;

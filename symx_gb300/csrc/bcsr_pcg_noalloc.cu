@@ -15,8 +15,15 @@
 //    that overlap on one device (two host threads, or two streams) race on it and give wrong
 //    results: run them one after the other.  Each call returns with its stream synchronized.
 //  * Set-up: the first call on a device, with that device current, looks up the array's
-//    device address (cudaGetSymbolAddress) and caches it.  If that first call is the set-up
-//    step of a program that later captures streams, it must come before any stream capture.
+//    device address (cudaGetSymbolAddress) and caches it together with the device's current
+//    context.  A call that finds another context current (after cudaDeviceReset, or a new
+//    primary context) looks the address up again, so a cached address never outlives the
+//    context it belongs to.  If that first call is the set-up step of a program that later
+//    captures streams, it must come before any stream capture.
+//  * Device assumption: the reduction partials have room for kNoAllocPartials = 2,048
+//    per-block sums.  The widest PCG launch is one block of 256 threads per resident slot,
+//    i.e. SMs x resident blocks per SM (GB300: 152 x 8 = 1,216).  A device with room for more
+//    resident blocks than 2,048 is refused by run_bcsr_pcg before any launch.
 //  * What must be zero when the kernels start: the eight completion tickets of the
 //    reductions and the missing-diagonal counter.  Every call clears them on its stream
 //    (cudaMemsetAsync / cudaMemcpyAsync into the array) before its first kernel.  Everything
@@ -47,9 +54,33 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_address[kMaxDevices] = {};
+struct ScratchAddress {
+    void* context = nullptr;  // the context the address was looked up in
+    void* address = nullptr;
+};
+ScratchAddress g_scratch_address[kMaxDevices];
 
-// Device address of the scratch array on the current device (looked up once per device).
+// The current context, or null before the runtime has made one current (driver entry point
+// cuCtxGetCurrent, resolved at run time like the rest of this library's driver calls, so the
+// library still loads without a driver).
+void* current_context()
+{
+    using CtxGetCurrent = int (*)(void**);
+    static CtxGetCurrent fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(p);
+    }();
+    void* ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Device address of the scratch array in the current device's current context (looked up
+// once per device, and again whenever that device's context has changed).
 void* scratch_on_current_device()
 {
     int dev = -1;
@@ -57,15 +88,21 @@ void* scratch_on_current_device()
     if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("bcsr_pcg_noalloc: device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            throw std::runtime_error(std::string("bcsr_pcg_noalloc: cudaGetSymbolAddress of the scratch array: ") +
-                                     cudaGetErrorString(e));
-        g_scratch_address[dev] = p;
-    }
-    return g_scratch_address[dev];
+    ScratchAddress& a = g_scratch_address[dev];
+    void* ctx = current_context();
+    if (ctx && a.address && a.context == ctx) return a.address;
+    // first call in this context: the lookup also makes the runtime's context current if no
+    // context was yet
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        throw std::runtime_error(std::string("bcsr_pcg_noalloc: cudaGetSymbolAddress of the scratch array: ") +
+                                 cudaGetErrorString(e));
+    ctx = current_context();
+    if (!ctx) throw std::runtime_error("bcsr_pcg_noalloc: no current CUDA context");
+    a.context = ctx;
+    a.address = p;
+    return p;
 }
 
 }  // namespace

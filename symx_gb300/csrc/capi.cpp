@@ -235,6 +235,8 @@ extern "C" {
 const char* symxg_last_error(void) { return g_last_error.c_str(); }
 int symxg_abi_version(void) { return SYMXG_ABI_VERSION; }
 int64_t symxg_launch_count(void) { return symxg::launch_count(); }
+void symxg_set_wait_poll_limit(int64_t polls) { symxg::set_wait_poll_limit((long long)polls); }
+int64_t symxg_wait_poll_limit(void) { return (int64_t)symxg::wait_poll_limit(); }
 
 void symxg_default_settings(symxg_newton_settings* s)
 {

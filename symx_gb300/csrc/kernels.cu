@@ -19,6 +19,7 @@
 #include <atomic>
 #include <mutex>
 #include <type_traits>
+#include <map>
 #include <unordered_map>
 #include <stdexcept>
 #include <string>
@@ -1059,7 +1060,9 @@ constexpr int kStagedConsumerWarps = 15;
 constexpr int kStagedThreads = 32 * (kStagedConsumerWarps + 1);  // warp 0: producer
 constexpr int kStagedRows = 4 * kStagedConsumerWarps;
 constexpr int kStagedMaxStages = 8;
-constexpr long long kMaxBarrierPolls = 1ll << 22;
+// Bound of the drain waits (copies in flight before a block exits); the data waits use
+// B.staged.max_polls (wait_poll_limit()).
+constexpr long long kMaxBarrierPolls = kDefaultWaitPolls;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
@@ -1084,10 +1087,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
         : "memory");
     return ok != 0;
 }
-// Wait for the phase of parity `parity` to complete; false after kMaxBarrierPolls polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+// Wait for the phase of parity `parity` to complete; false after max_polls polls (none
+// when max_polls is 0).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long max_polls = kMaxBarrierPolls)
 {
-    for (long long i = 0; i < kMaxBarrierPolls; ++i)
+    for (long long i = 0; i < max_polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -1200,7 +1204,7 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
                 const int j = (int)(g % (unsigned)n_stages);
                 const int kb = next_kb, ke = next_ke;
                 if (g + 1 < last) range(g + 1, next_kb, next_ke);
-                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1)) {
+                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1, B.staged.max_polls)) {
                     *abort_flag = 1;
                     break;
                 }
@@ -1229,7 +1233,8 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
         for (int j = 0; j < n_stages; ++j) {
             const unsigned g = seq + j, s = g % NS;
             // one decision per warp: the product below shuffles over the full warp
-            const bool stop = __any_sync(0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1));
+            const bool stop = __any_sync(
+                0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1, B.staged.max_polls));
             if (stop) {
                 *abort_flag = 1;
                 break;
@@ -1388,7 +1393,7 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                     }
                 }
                 const unsigned g = issued, s = g % NS, use = g / NS;
-                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1)) {
+                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1, B.staged.max_polls)) {
                     *abort_flag = 1;
                     break;
                 }
@@ -1478,7 +1483,8 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
         for (;;) {
             const unsigned g = seq, s = g % NS;
             // one decision per warp: the product below shuffles over the full warp
-            const bool stop = __any_sync(0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1));
+            const bool stop = __any_sync(
+                0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1, B.staged.max_polls));
             if (stop) {
                 *abort_flag = 1;
                 break;
@@ -1797,7 +1803,7 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v)
 {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* ok_flag)
+__device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* ok_flag, long long max_polls)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1806,7 +1812,7 @@ __device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* 
         red_release_add(&bar[0], 1u);
         bool ok = true;
         for (long long polls = 0; ld_acquire(&bar[0]) < target; ++polls) {
-            if (polls > kMaxBarrierPolls) {
+            if (polls > max_polls) {
                 ok = false;
                 break;
             }
@@ -1860,7 +1866,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         const bool first = iteration == 0;
         staged_spmv_pass_dyn(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : (float)beta, seq, issued, P,
                              abort_flag, part_pq);
-        if (!grid_barrier(bar, generation, &barrier_ok) || *abort_flag) {
+        if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls) || *abort_flag) {
             failed = true;
             break;
         }
@@ -1906,7 +1912,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
             part_rr[blockIdx.x] = make_float2(brr.hi, brr.lo);
             part_rz[blockIdx.x] = make_float2(brz.hi, brz.lo);
         }
-        if (!grid_barrier(bar, generation, &barrier_ok)) {
+        if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls)) {
             failed = true;
             break;
         }
@@ -2099,22 +2105,26 @@ template <typename K>
 unsigned resident_grid(K kernel, int threads)
 {
     static std::mutex m;
-    static std::unordered_map<const void*, unsigned> cache;
-    std::lock_guard<std::mutex> lock(m);
-    auto it = cache.find((const void*)kernel);
-    if (it != cache.end()) return it->second;
+    static std::map<std::pair<const void*, int>, unsigned> cache;  // per (kernel, device)
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(m);
+    const auto key = std::make_pair((const void*)kernel, dev);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
     const unsigned g = (unsigned)std::max(1, sms * std::max(1, per_sm));
-    cache[(const void*)kernel] = g;
+    cache[key] = g;
     return g;
 }
 
 }  // namespace
 
 int64_t launch_count() { return g_launches.load(); }
+std::atomic<long long> g_wait_polls{kDefaultWaitPolls};
+void set_wait_poll_limit(long long polls) { g_wait_polls.store(polls < 0 ? kDefaultWaitPolls : polls); }
+long long wait_poll_limit() { return g_wait_polls.load(); }
 void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void launch_sum(const double* x, int64_t n, double* partials, unsigned* ticket, double* out, cudaStream_t s)
@@ -2160,12 +2170,12 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
             check_launch("project_pd_deflated");
         }
         if (split) {
-            static const unsigned pending_grid = resident_grid(k_project_pd_deflated_listed<T, 12>, 128);
+            const unsigned pending_grid = resident_grid(k_project_pd_deflated_listed<T, 12>, 128);
             k_project_pd_deflated_listed<T, 12><<<pending_grid, 128, 0, s>>>(H, scratch.pending, scratch.n_pending, eps,
                                                                            mirroring, not_converged);
             check_launch("project_pd_deflated_listed");
         }
-        static const unsigned listed_grid = resident_grid(k_project_pd_listed<T, 12>, 128);
+        const unsigned listed_grid = resident_grid(k_project_pd_listed<T, 12>, 128);
         k_project_pd_listed<T, 12><<<listed_grid, 128, 0, s>>>(H, scratch.fallback, scratch.n_fallback, eps, mirroring,
                                                                not_converged);
         check_launch("project_pd_listed");
@@ -2178,7 +2188,7 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
         case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
         case 24: {
             constexpr int threads = ProjPairsCfg<T>::warps * 32;
-            static const unsigned grid = resident_grid(k_project_pd_pairs<T, 24>, threads);
+            const unsigned grid = resident_grid(k_project_pd_pairs<T, 24>, threads);
             const unsigned need = blocks_for(count, ProjPairsCfg<T>::warps);
             k_project_pd_pairs<T, 24><<<need < grid ? need : grid, threads, 0, s>>>(H, count, eps, mirroring,
                                                                                    not_converged, sel);
@@ -2266,7 +2276,9 @@ void launch_pcg_spmv(const PcgBuffers<T>& B, int iteration, cudaStream_t s)
         if (B.staged.stages > 0 && B.vals_stride != kTiledBcsr) {
             float* p_old = (iteration & 1) ? B.p : B.p2;
             float* p_new = (iteration & 1) ? B.p2 : B.p;
-            k_pcg_spmv_staged<<<B.staged.grid, kStagedThreads, B.staged.smem_bytes, s>>>(B, p_old, p_new,
+            PcgBuffers<float> arg = B;
+            arg.staged.max_polls = wait_poll_limit();
+            k_pcg_spmv_staged<<<B.staged.grid, kStagedThreads, B.staged.smem_bytes, s>>>(arg, p_old, p_new,
                                                                                         iteration == 0 ? 1 : 0);
             check_launch("pcg_spmv_staged");
             return;
@@ -2282,6 +2294,7 @@ void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s)
     const cudaError_t e = cudaMemsetAsync(B.tickets + 6, 0, 5 * sizeof(unsigned), s);
     if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
     PcgBuffers<float> arg = B;
+    arg.staged.max_polls = wait_poll_limit();
     void* args[] = {&arg};
     const cudaError_t l = cudaLaunchCooperativeKernel((const void*)k_pcg_solve_staged, dim3(B.staged.grid),
                                                       dim3(kStagedThreads), args, B.staged.smem_bytes, s);

@@ -11,6 +11,16 @@ namespace symxg {
 int64_t launch_count();
 void count_launch(int64_t n = 1);
 
+// Polls after which a bounded wait of the staged PCG kernels (a shared-memory stage's
+// mbarrier, the persistent kernel's grid barrier) gives up and flags the solve
+// (PcgState::wait_failed).  Process-wide, read at each launch; the default is
+// kDefaultWaitPolls.  A small value makes the waits run out on purpose, which is how the
+// error path is tested.  The drain of a block's bulk copies in flight before it exits always
+// uses the default, so a block never exits with a copy still writing its shared memory.
+constexpr long long kDefaultWaitPolls = 1ll << 22;
+void set_wait_poll_limit(long long polls);  // < 0: the default
+long long wait_poll_limit();
+
 // Device-resident state of one PCG solve (read by the host between chunks of iterations).
 struct PcgState {
     double bb;        // b.b
@@ -125,6 +135,7 @@ struct PcgBuffers {
         int grid = 0;
         size_t smem_bytes = 0;
         int persistent = 0;      // 1: the whole PCG loop can run as one cooperative launch
+        long long max_polls = kDefaultWaitPolls;  // set from wait_poll_limit() at each launch
         const int32_t* row_ptr_ext = nullptr;  // row_ptr, then nnzb repeated to grid * rows_per_block + stage_rows + 8
         const int32_t* cols_ext = nullptr;     // cols, padded with zeros to a multiple of 4 plus 4
     } staged;

@@ -188,6 +188,8 @@ CONFIGS = {
     "tet4_64_rcm": dict(kind="tet4", cells=(64, 64, 64), h=0.01, perturb=0.05, seed=1, numbering="rcm"),
     "tet4_6p_rcm": dict(kind="tet4", cells=(6, 5, 4), h=0.01, perturb=0.05, seed=11, numbering="rcm"),
     "tet4_32": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.0, seed=3),
+    # the metric's configuration at 32^3 cells: at-scale parity against the oracle's solve
+    "tet4_32p": dict(kind="tet4", cells=(32, 32, 32), h=0.01, perturb=0.05, seed=7),
     "tet4_40": dict(kind="tet4", cells=(40, 40, 40), h=0.01, perturb=0.0, seed=4),
 }
 

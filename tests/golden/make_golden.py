@@ -38,7 +38,10 @@ sys.path.insert(0, ROOT)
 from symx_gb300 import problems  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "symx_ref_harness")
-REF_DOC = "/root/reference/docs/source/compilation.md"
+sys.path.insert(0, ROOT)
+from __graft_entry__ import reference_dir  # noqa: E402  ($SYMX_REFERENCE_DIR or oracle/Makefile.ref's REF)
+
+REF_DOC = os.path.join(reference_dir(), "docs", "source", "compilation.md")
 
 
 def run(*args):

@@ -151,7 +151,7 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(capi.EXPORTS) == declared
     for name in declared:
         assert hasattr(lib, name), name
-    assert lib.symxg_abi_version() == 4
+    assert lib.symxg_abi_version() == 5
 
 
 def test_invalid_arguments_are_reported(lib):

@@ -93,6 +93,21 @@ def test_pcg_edge_cases(sg):
     rp2[1:] -= 1
     with pytest.raises(SymxgError, match="diagonal"):
         gpu_solve(sg, rp2, cols[keep], vals[keep], b, "float64")
+    # a values stride below the block count is refused before any kernel reads a value
+    import ctypes as C
+
+    from symx_gb300 import capi
+
+    L = sg.load()
+    d_rp, d_cols = torch.tensor(rp, device="cuda"), torch.tensor(cols, device="cuda")
+    d_vals = sg.component_major(torch.tensor(vals, dtype=torch.float64, device="cuda"))
+    d_b = torch.tensor(b, device="cuda")
+    d_x = torch.zeros_like(d_b)
+    pinfo = capi.PcgInfo()
+    rc = L.symxg_bcsr_pcg_f64(rp.size - 1, C.c_void_p(d_rp.data_ptr()), C.c_void_p(d_cols.data_ptr()),
+                              C.c_void_p(d_vals.data_ptr()), cols.size - 1, C.c_void_p(d_b.data_ptr()),
+                              C.c_void_p(d_x.data_ptr()), 1e-10, 1e-6, 100, C.byref(pinfo), None)
+    assert rc == 1 and "vals_stride" in L.symxg_last_error().decode()
     # empty system
     t = torch.zeros(0, dtype=torch.float32, device="cuda")
     info = sg.bcsr_pcg(torch.zeros(1, dtype=torch.int32, device="cuda"), torch.zeros(0, dtype=torch.int32, device="cuda"),
