@@ -179,8 +179,9 @@ def run_ours(args):
     # time_kernels: CUDA events around every PCG SpMV / projection launch (roofline, live)
     solver.set_settings(cg_rel_tolerance=1e-3, precision="mixed", time_kernels=1)
 
-    def device_solve(precision):
-        solver.set_settings(precision=precision)
+    def device_solve(precision, **kw):
+        solver.set_settings(precision=precision, **{"projection_fp64_refinement": 0, "cg_residual_replacement": 0,
+                                                    **kw})
         solver.set_state(p["x_init"], p["x0"], p["v0"])
         solver.upload()
         torch.cuda.synchronize()
@@ -219,6 +220,32 @@ def run_ours(args):
         fp64_st = s64
     solver.download()
     x_fp64 = solver.get_positions()
+
+    # the split that keeps the projection's arithmetic and the PCG's residual in FP64: FP32
+    # Jacobi refined by one FP64 step (12 x 12 element Hessians), FP64 residual replacement
+    # every 50 PCG iterations; and the FP64 form with the same refined projection
+    variants = {"mixed_fp64_projection_and_residual": ("mixed", dict(projection_fp64_refinement=1,
+                                                                     cg_residual_replacement=50)),
+                "fp64_refined_projection": ("fp64", dict(projection_fp64_refinement=1))}
+    variant_out, variant_x = {}, {}
+    for name, (prec, kw) in variants.items():
+        if args.no_variants:
+            break
+        vms, vst = [], None
+        for i in range(max(1, args.fp64_steps) + 1):
+            t, vst = device_solve(prec, **kw)
+            if i > 0:
+                vms.append(t)
+        assert vst["solver_return"] == 0 and vst["final_residual"] < 1e-6, vst
+        solver.download()
+        variant_x[name] = (solver.get_positions(), vst)
+        variant_out[name] = {
+            "precision": prec, **kw, "ms_per_step": round(statistics.mean(vms), 3),
+            "ms_per_newton_step": round(statistics.mean(vms) / vst["newton_iterations"], 4),
+            "newton_iterations": vst["newton_iterations"], "cg_iterations": vst["cg_iterations"],
+            "cg_residual_replacements": vst["cg_residual_replacements"], "final_residual": vst["final_residual"],
+            "stage_seconds": {k: round(vst[k], 6) for k in vst if k.startswith("t_")},
+            "vs_fp64_step_speedup": round(statistics.mean(fp64_ms) / statistics.mean(vms), 3)}
 
     # end to end through the C ABI with host arrays
     solver.set_settings(precision="mixed")
@@ -298,6 +325,7 @@ def run_ours(args):
                  "newton_iterations": fp64_st["newton_iterations"], "cg_iterations": fp64_st["cg_iterations"],
                  "stage_seconds": {k: round(fp64_st[k], 6) for k in fp64_st if k.startswith("t_")}},
         "mixed_vs_fp64_step_speedup": round(statistics.mean(fp64_ms) / ms_step, 3),
+        "variants": variant_out,
         "mixed_vs_fp64_position_rel_err": rel_vs_fp64,
         "e2e": {"value": round(statistics.mean(e2e_ms) / e2e_st["newton_iterations"], 4),
                 "unit": UNIT + " per Newton step", "ms_per_step": round(statistics.mean(e2e_ms), 3),
@@ -321,7 +349,7 @@ def run_ours(args):
         out["cpu_baseline"], x_oracle, oracle_stats = cpu_baseline(p, args)
         if x_oracle is not None:
             out["oracle_parity"] = oracle_parity(p, x_oracle, oracle_stats,
-                                                 {"mixed": (x_mixed, st), "fp64": (x_fp64, fp64_st)})
+                                                 {"mixed": (x_mixed, st), "fp64": (x_fp64, fp64_st), **variant_x})
     return out
 
 
@@ -610,6 +638,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-newton-iterations", type=int, default=0, help="0: the complete solve")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-variants", action="store_true", help="skip the FP64-projection / residual-replacement runs")
     ap.add_argument("--profile-solve", choices=["mixed", "fp64"], default=None)
     ap.add_argument("--measure", choices=["adjoint", "rollout"], default=None,
                     help="instead of the bench line: the adjoint (quasistatic) or rollout measurement")

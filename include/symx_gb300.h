@@ -100,6 +100,10 @@ typedef struct symxg_newton_settings {
     int32_t project_on_demand_countdown; /* ProjectOnDemand: iterations projected after a failure (4) */
     double ppn_tightening_factor;    /* Progressive: threshold factor after a failed direction (0.5) */
     double ppn_release_factor;       /* Progressive: threshold factor after a successful one (2.0) */
+    int32_t projection_fp64_refinement; /* 1: 12x12 projections FP64-accurate (FP32 Jacobi + one FP64
+                                           refinement step, FP64 clamping correction), either precision */
+    int32_t cg_residual_replacement; /* Mixed: every k PCG iterations replace the residual by b - A x
+                                        accumulated in FP64 (0: never) */
 } symxg_newton_settings;
 
 typedef struct symxg_solve_stats {
@@ -126,6 +130,8 @@ typedef struct symxg_solve_stats {
     int32_t cg_iterations_per_newton[16]; /* PCG iterations of the first 16 linear solves (0 after) */
     int64_t n_hessians;              /* element Hessians of the Newton iterations that found a direction */
     int64_t n_projected_hessians;    /* ... and how many of them were projected */
+    int32_t cg_residual_replacements; /* residual replacements made by the FP32 PCG */
+    int32_t pad;
 } symxg_solve_stats;
 
 /* message of the last failing call on this thread ("" if none) */

@@ -55,7 +55,8 @@ class NewtonSettings(C.Structure):
         ("cg_abs_tolerance", C.c_double), ("cg_rel_tolerance", C.c_double),
         ("bailout_residual", C.c_double), ("precision", C.c_int32), ("time_kernels", C.c_int32),
         ("project_on_demand_countdown", C.c_int32), ("ppn_tightening_factor", C.c_double),
-        ("ppn_release_factor", C.c_double),
+        ("ppn_release_factor", C.c_double), ("projection_fp64_refinement", C.c_int32),
+        ("cg_residual_replacement", C.c_int32),
     ]
 
 
@@ -72,6 +73,7 @@ class SolveStats(C.Structure):
         ("pcg_solve_iterations", C.c_int64), ("pcg_solve_seconds", C.c_double),
         ("cg_iterations_per_newton", C.c_int32 * 16),
         ("n_hessians", C.c_int64), ("n_projected_hessians", C.c_int64),
+        ("cg_residual_replacements", C.c_int32), ("pad", C.c_int32),
     ]
 
     def as_dict(self):

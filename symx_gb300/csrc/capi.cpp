@@ -167,6 +167,7 @@ static void fill_stats(const symx::SolveStats& st, symx::SolverReturn r, symxg_s
     o->d2h_bytes = st.d2h_bytes;
     o->n_hessians = (int64_t)st.n_hessians;
     o->n_projected_hessians = (int64_t)st.n_projected_hessians;
+    o->cg_residual_replacements = st.cg_residual_replacements;
     for (const auto& kv : st.kernels) {
         if (kv.first.rfind("pcg_spmv", 0) == 0) {
             o->spmv_launches += kv.second.first;
@@ -263,6 +264,8 @@ void symxg_default_settings(symxg_newton_settings* s)
     s->project_on_demand_countdown = d.project_on_demand_countdown;
     s->ppn_tightening_factor = d.ppn_tightening_factor;
     s->ppn_release_factor = d.ppn_release_factor;
+    s->projection_fp64_refinement = d.projection_fp64_refinement ? 1 : 0;
+    s->cg_residual_replacement = d.cg_residual_replacement;
 }
 
 int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, symxg_solver** out)
@@ -411,6 +414,9 @@ int symxg_set_settings(symxg_solver* s, const symxg_newton_settings* c)
         t.bailout_residual = c->bailout_residual;
         t.precision = c->precision == SYMXG_PRECISION_MIXED ? symx::Precision::Mixed : symx::Precision::FP64;
         t.time_kernels = c->time_kernels != 0;
+        if (c->cg_residual_replacement < 0) throw std::invalid_argument("negative cg_residual_replacement");
+        t.projection_fp64_refinement = c->projection_fp64_refinement != 0;
+        t.cg_residual_replacement = c->cg_residual_replacement;
         return SYMXG_OK;
     });
 }

@@ -238,6 +238,23 @@ __global__ void __launch_bounds__(128) k_project_pd_listed(T* __restrict__ H, co
     if (nc) *not_converged = 1;
 }
 
+// FP64-accurate projection (symxg_dev::project_pd_refined: FP32 Jacobi, one FP64 refinement
+// step, clamping applied as an FP64 correction) of the matrices k_project_pd_sort listed,
+// grid-stride over the list.  Deflate: the `pending` list (translation-invariant matrices),
+// otherwise the `fallback` list (full decomposition).  One thread per matrix; the kernel is
+// bound by the FP64 pipe, so a small block keeps the per-thread arrays in L1.
+template <typename S, int N, bool Deflate>
+__global__ void __launch_bounds__(64) k_project_pd_refined_listed(S* __restrict__ H, const int64_t* __restrict__ list,
+                                                                  const unsigned long long* n_list, double eps,
+                                                                  int mirroring, int* not_converged)
+{
+    const int64_t n = (int64_t)*n_list;
+    int nc = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        symxg_dev::project_pd_refined<S, N / 3, Deflate>(H + list[k] * (N * N), eps, mirroring != 0, &nc);
+    if (nc) *not_converged = 1;
+}
+
 // Progressive projection (NewtonsMethod.cpp:305-329): flag the element gradient blocks of
 // every DoF block whose gradient max-abs is at least thr (gflag zeroed before); counts the
 // other blocks in *n_inactive.
@@ -1857,8 +1874,10 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
     float2* part_rz = part_rr + G;
     const int row_begin = (int)((int64_t)blockIdx.x * B.n_blocks / G);
     const int row_end = (int)((int64_t)(blockIdx.x + 1) * B.n_blocks / G);
-    double rz = st0.rz, alpha = 0.0, beta = 0.0, pAp = 0.0, rr = 0.0, error = st0.error;
-    int iteration = st0.iteration, converged = 0, indefinite = 0;
+    // a launch after a residual replacement continues the recurrence: beta from the state
+    double rz = st0.rz, alpha = 0.0, beta = st0.iteration > 0 ? st0.beta : 0.0, pAp = 0.0, rr = 0.0,
+           error = st0.error;
+    int iteration = st0.iteration, converged = 0, indefinite = 0, paused = 0;
     bool failed = false;
     for (int li = 0;; ++li) {
         float* p_old = (iteration & 1) ? B.p : B.p2;
@@ -1925,6 +1944,10 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
             break;
         }
         if (iteration >= st0.max_iterations) break;
+        if (st0.replace_every > 0 && iteration % st0.replace_every == 0) {
+            paused = 1;  // rz stays that of the last iterate: the replacement forms beta
+            break;
+        }
         beta = rz_new / rz;
         rz = rz_new;
     }
@@ -1935,13 +1958,73 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         st->iteration = iteration;
         st->converged = converged;
         st->indefinite = indefinite;
-        st->done = 1;
+        st->done = paused ? 0 : 1;
         st->pAp = pAp;
         st->alpha = alpha;
         st->beta = beta;
         st->rz = rz;
         st->rr = rr;
         st->error = error;
+    }
+}
+
+// Residual replacement (see launch_pcg_replace_residual): one half-warp per block row,
+// lane-strided over the row's blocks, products and sums in FP64.
+__global__ void __launch_bounds__(256) k_pcg_replace_residual(PcgBuffers<float> B, const double* __restrict__ grad)
+{
+    if (B.state->done) return;
+    __shared__ double sh[32];
+    const int lane16 = threadIdx.x & 15, half = (threadIdx.x >> 4) & 1;
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps_total = (gridDim.x * blockDim.x) >> 5;
+    const int64_t st = B.vals_stride;
+    double rr = 0.0, rz = 0.0;
+    // two rows per warp and pass; the loop bound is warp-uniform, so the full-mask shuffles
+    // below are converged (a half-warp past the last row adds zeros)
+    for (int base = 2 * warp_global; base < B.n_blocks; base += 2 * warps_total) {
+        const int row = base + half;
+        const bool valid = row < B.n_blocks;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        const int kb = valid ? B.row_ptr[row] : 0, ke = valid ? B.row_ptr[row + 1] : 0;
+        for (int k = kb + lane16; k < ke; k += 16) {
+            const Row4<float> x = ld4(B.x + 4 * B.cols[k]);
+            const float* __restrict__ m = B.vals + k;
+            const double x0 = x.x, x1 = x.y, x2 = x.z;
+            a0 = fma((double)m[0], x0, fma((double)m[st], x1, fma((double)m[2 * st], x2, a0)));
+            a1 = fma((double)m[3 * st], x0, fma((double)m[4 * st], x1, fma((double)m[5 * st], x2, a1)));
+            a2 = fma((double)m[6 * st], x0, fma((double)m[7 * st], x1, fma((double)m[8 * st], x2, a2)));
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o, 16);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o, 16);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o, 16);
+        }
+        if (valid && lane16 == 0) {
+            const Row4<float> r{(float)(-grad[3 * row] - a0), (float)(-grad[3 * row + 1] - a1),
+                                (float)(-grad[3 * row + 2] - a2), 0.0f};
+            const Row4<float> z = apply_block_jacobi(B.Dinv, row, r);
+            st4(B.r + 4 * row, r);
+            st4(B.z + 4 * row, z);
+            rr = fma((double)r.x, (double)r.x, fma((double)r.y, (double)r.y, fma((double)r.z, (double)r.z, rr)));
+            rz = fma((double)r.x, (double)z.x, fma((double)r.y, (double)z.y, fma((double)r.z, (double)z.z, rz)));
+        }
+    }
+    const double bv[2] = {block_reduce<false>(rr, sh), block_reduce<false>(rz, sh)};
+    double res[2];
+    if (publish_and_combine<2>(bv, B.partials, B.tickets + 1, res) && threadIdx.x == 0) {
+        PcgState* s = B.state;
+        s->replacements += 1;
+        s->rr = res[0];
+        s->error = sqrt(res[0] / s->bb);
+        if (s->error < s->abs_tol || s->error / s->error0 < s->rel_tol) {
+            s->converged = 1;
+            s->done = 1;
+        } else if (s->iteration >= s->max_iterations) {
+            s->done = 1;
+        } else {
+            s->beta = res[1] / s->rz;
+            s->rz = res[1];
+        }
     }
 }
 
@@ -2202,6 +2285,30 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
 }
 
 template <typename T>
+void launch_project_pd_refined12(T* H, int64_t count, double eps, bool mirroring, int* not_converged, cudaStream_t s,
+                                 ProjectionScratch scratch, const int64_t* sel)
+{
+    if (count <= 0) return;
+    if (!scratch.fallback || !scratch.n_fallback || !scratch.pending || !scratch.n_pending)
+        throw std::runtime_error("symx_gb300: the refined projection needs the sorting pass's lists");
+    for (unsigned long long* c : {scratch.n_fallback, scratch.n_pending}) {
+        const cudaError_t e = cudaMemsetAsync(c, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(e));
+    }
+    k_project_pd_sort<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, scratch.fallback, scratch.n_fallback, sel,
+                                                                   scratch.pending, scratch.n_pending);
+    check_launch("project_pd_sort");
+    const unsigned pending_grid = resident_grid(k_project_pd_refined_listed<T, 12, true>, 64);
+    k_project_pd_refined_listed<T, 12, true><<<pending_grid, 64, 0, s>>>(H, scratch.pending, scratch.n_pending, eps,
+                                                                         mirroring, not_converged);
+    check_launch("project_pd_refined_listed");
+    const unsigned fallback_grid = resident_grid(k_project_pd_refined_listed<T, 12, false>, 64);
+    k_project_pd_refined_listed<T, 12, false><<<fallback_grid, 64, 0, s>>>(H, scratch.fallback, scratch.n_fallback, eps,
+                                                                           mirroring, not_converged);
+    check_launch("project_pd_refined_fallback");
+}
+
+template <typename T>
 void launch_assemble_blocks(int64_t nnzb, const int64_t* slot_ptr, const int32_t* contrib, const T* blocks, T* vals,
                             int64_t vstride, cudaStream_t s)
 {
@@ -2301,6 +2408,12 @@ void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s)
     if (l != cudaSuccess)
         throw std::runtime_error(std::string("symx_gb300: cooperative launch of the PCG failed: ") + cudaGetErrorString(l));
     check_launch("pcg_solve_staged");
+}
+
+void launch_pcg_replace_residual(const PcgBuffers<float>& B, const double* grad, cudaStream_t s)
+{
+    k_pcg_replace_residual<<<kReduceBlocks, 256, 0, s>>>(B, grad);
+    check_launch("pcg_replace_residual");
 }
 
 StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged& st)
@@ -2461,6 +2574,8 @@ void launch_convert_to_double(int64_t n, const T* x, double* y, cudaStream_t s)
 
 #define SYMXG_INSTANTIATE(T)                                                                                          \
     template void launch_dot_mixed<T>(const T*, const double*, int64_t, double*, unsigned*, double*, cudaStream_t);  \
+    template void launch_project_pd_refined12<T>(T*, int64_t, double, bool, int*, cudaStream_t, ProjectionScratch,    \
+                                                 const int64_t*);                                                     \
     template void launch_project_pd<T>(T*, int, int64_t, T, bool, int*, cudaStream_t, ProjectionScratch,               \
                                        const int64_t*);                                                                 \
     template void launch_assemble_blocks<T>(int64_t, const int64_t*, const int32_t*, const T*, T*, int64_t, cudaStream_t); \

@@ -36,6 +36,11 @@ struct PcgState {
     int converged;
     int indefinite;
     int wait_failed;  // 1 if a bounded wait inside a kernel gave up (the solve is invalid)
+    // One-launch FP32 PCG: every replace_every iterations (0: never) the launch returns
+    // unfinished and k_pcg_replace_residual replaces the recursive residual by b - A x
+    // accumulated in FP64; `replacements` counts them.
+    int replace_every;
+    int replacements;
 };
 
 // Deterministic reductions: each launch uses a fixed grid, every block sums a fixed
@@ -72,6 +77,14 @@ struct ProjectionScratch {
 template <typename T>
 void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s,
                        ProjectionScratch scratch = ProjectionScratch{}, const int64_t* sel = nullptr);
+
+// 12 x 12 projection whose arithmetic is FP64-accurate for float or double storage: the
+// sorting pass, then for the listed matrices an FP32 cyclic Jacobi refined by one FP64
+// Ogita-Aishima step, the clamping applied as an FP64 correction and rounded once into H
+// (symxg_dev::project_pd_refined).  Needs the sorting pass's lists in `scratch`.
+template <typename T>
+void launch_project_pd_refined12(T* H, int64_t count, double eps, bool mirroring, int* not_converged, cudaStream_t s,
+                                 ProjectionScratch scratch, const int64_t* sel = nullptr);
 
 // Progressive projection: flag (gflag[gblock] = 1) the element gradient blocks of the DoF
 // blocks with max |grad| >= thr, counting the other blocks in *n_inactive; then list the
@@ -141,6 +154,13 @@ struct PcgBuffers {
     } staged;
 };
 constexpr int kPcgMaxPartials = 1 << 16;
+
+// Residual replacement of the one-launch FP32 PCG when it returned unfinished (no-op once the
+// solve is done): r = b - A x with b = -grad, the products and sums in FP64 and r rounded once
+// to float, z = M^-1 r, then r.r and r.z in FP64, the convergence test on the true residual,
+// beta = r.z / r.z_old.  The next launch of the one-launch PCG continues from there.
+void launch_pcg_replace_residual(const PcgBuffers<float>& B, const double* grad, cudaStream_t s);
+
 
 // Set x = 0, r = b (b = -grad converted to T), z = M^-1 r, bb, rz, error0.
 template <typename T>

@@ -1148,6 +1148,20 @@ double NewtonsMethod::evaluate(double* grad_host)
 }
 
 namespace {
+// Project `count` element Hessians of potential cp (all of them, or those listed in sel):
+// the 12 x 12 ones with FP64-accurate arithmetic when the settings ask for it.
+template <typename T>
+void project_potential(SolverImpl& I, const CompiledPotential& cp, const NewtonSettings& s, int64_t count,
+                       cudaStream_t stream, const int64_t* sel = nullptr)
+{
+    if (s.projection_fp64_refinement && cp.nb == 4)
+        symxg::launch_project_pd_refined12<T>(I.Hbuf<T>() + cp.h_off * 9, count, s.projection_eps,
+                                              s.project_to_pd_use_mirroring, I.flags.p, stream, I.proj_scratch(), sel);
+    else
+        symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, count, (T)s.projection_eps,
+                                    s.project_to_pd_use_mirroring, I.flags.p, stream, I.proj_scratch(), sel);
+}
+
 template <typename T>
 void assemble_t(SolverImpl& I, bool project, const NewtonSettings& s, int mode)
 {
@@ -1155,9 +1169,7 @@ void assemble_t(SolverImpl& I, bool project, const NewtonSettings& s, int mode)
     I.launch_eval(mode);
     if (project) {
         ck(cudaMemsetAsync(I.flags.p, 0, sizeof(int), I.stream), "memset");
-        for (auto& cp : I.pots)
-            symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements, (T)s.projection_eps,
-                                        s.project_to_pd_use_mirroring, I.flags.p, I.stream, I.proj_scratch());
+        for (auto& cp : I.pots) project_potential<T>(I, cp, s, cp.n_elements, I.stream);
     }
     symxg::launch_assemble_blocks<T>(I.nnzb, I.slot_ptr.p, I.contrib.p, I.Hbuf<T>(), I.vals<T>(), I.vstride, I.stream);
 }
@@ -1252,10 +1264,7 @@ uint64_t ppn_project(SolverImpl& I, const NewtonSettings& S, cudaStream_t s, dou
     for (size_t k = 0; k < np; ++k) {
         const auto& cp = I.pots[k];
         const int64_t n = (int64_t)counts[1 + k];
-        if (n > 0)
-            symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, n, (T)S.projection_eps,
-                                        S.project_to_pd_use_mirroring, I.flags.p, s, I.proj_scratch(),
-                                        I.ppn_sel.p + cp.e_off);
+        if (n > 0) project_potential<T>(I, cp, S, n, s, I.ppn_sel.p + cp.e_off);
         total += (uint64_t)n;
     }
     return total;
@@ -1348,9 +1357,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
                             cudaEventCreate(&b);
                             cudaEventRecord(a, s);
                         }
-                        symxg::launch_project_pd<T>(I.Hbuf<T>() + cp.h_off * 9, 3 * cp.nb, cp.n_elements,
-                                                    (T)S.projection_eps, S.project_to_pd_use_mirroring, I.flags.p, s,
-                                                    I.proj_scratch());
+                        project_potential<T>(I, cp, S, cp.n_elements, s);
                         if (timed) {
                             cudaEventRecord(b, s);
                             pending_kernel_events.push_back(
@@ -1378,6 +1385,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             init.abs_tol = std::max(forcing, S.cg_abs_tolerance);
             init.rel_tol = S.cg_rel_tolerance;
             init.max_iterations = S.cg_max_iterations;
+            init.replace_every = std::is_same<T, float>::value ? S.cg_residual_replacement : 0;
             ck(cudaMemcpyAsync(I.pcg_state.p, &init, sizeof(PcgState), cudaMemcpyHostToDevice, s), "pcg state");
             symxg::launch_pcg_init<T>(B, I.grad.p, s);
             int launched = 0, chunk = 8;
@@ -1385,25 +1393,43 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
             bool persistent = false;
             if constexpr (std::is_same<T, float>::value) persistent = B.staged.persistent != 0;
             if (persistent) {  // every iteration in one cooperative launch
-                cudaEvent_t a = nullptr, b = nullptr;
-                if (S.time_kernels) {
-                    cudaEventCreate(&a);
-                    cudaEventCreate(&b);
-                    cudaEventRecord(a, s);
+                // With residual replacement the launch returns every replace_every iterations;
+                // k_pcg_replace_residual forms the true residual and the next launch continues.
+                // Each round is a launch pair that does nothing once the solve is done.
+                const int every = init.replace_every;
+                const int rounds = every > 0 ? 4 : 1;
+                for (int round = 0;; round += rounds) {
+                    cudaEvent_t a = nullptr, b = nullptr;
+                    if (S.time_kernels) {
+                        cudaEventCreate(&a);
+                        cudaEventCreate(&b);
+                        cudaEventRecord(a, s);
+                    }
+                    for (int k = 0; k < rounds; ++k) {
+                        if constexpr (std::is_same<T, float>::value) {
+                            symxg::launch_pcg_solve_persistent(B, s);
+                            if (every > 0) symxg::launch_pcg_replace_residual(B, I.grad.p, s);
+                        }
+                    }
+                    if (S.time_kernels) cudaEventRecord(b, s);
+                    const int it_before = I.h_state->iteration;
+                    ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s),
+                       "pcg state");
+                    ck(cudaStreamSynchronize(s), "synchronize");
+                    if (S.time_kernels) {
+                        float ms = 0.f;
+                        cudaEventElapsedTime(&ms, a, b);
+                        auto& kt = st.kernels["pcg_solve_f32"];
+                        kt.first += I.h_state->iteration - (round == 0 ? 0 : it_before);
+                        kt.second += ms * 1e-3;
+                        cudaEventDestroy(a);
+                        cudaEventDestroy(b);
+                    }
+                    if (I.h_state->done || I.h_state->wait_failed || every <= 0 ||
+                        I.h_state->iteration >= S.cg_max_iterations)
+                        break;
                 }
-                if constexpr (std::is_same<T, float>::value) symxg::launch_pcg_solve_persistent(B, s);
-                if (S.time_kernels) cudaEventRecord(b, s);
-                ck(cudaMemcpyAsync(I.h_state, I.pcg_state.p, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "pcg state");
-                ck(cudaStreamSynchronize(s), "synchronize");
-                if (S.time_kernels) {
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, a, b);
-                    auto& kt = st.kernels["pcg_solve_f32"];
-                    kt.first += I.h_state->iteration;
-                    kt.second += ms * 1e-3;
-                    cudaEventDestroy(a);
-                    cudaEventDestroy(b);
-                }
+                st.cg_residual_replacements += I.h_state->replacements;
             }
             while (!persistent) {
                 for (int k = 0; k < chunk; ++k) {

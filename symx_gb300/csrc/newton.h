@@ -68,6 +68,16 @@ struct NewtonSettings {
     Precision precision = Precision::FP64;
     // Record CUDA events around every PCG SpMV and PD-projection launch (SolveStats::kernels).
     bool time_kernels = false;
+    // 12 x 12 element projections (Tet4) with FP64-accurate arithmetic in either precision: an
+    // FP32 Jacobi refined by one FP64 Ogita-Aishima step, the clamping applied as an FP64
+    // correction (the reference's projection is FP64 Eigen, project_to_PD.cpp:12-32).  Mixed
+    // precision keeps the FP32 element Hessians and BCSR matrix; only the projection's
+    // arithmetic changes.  Other element sizes are projected as without it.
+    bool projection_fp64_refinement = false;
+    // One-launch FP32 PCG (Mixed): every this many iterations the recursive residual is
+    // replaced by the true residual b - A x accumulated in FP64 and the convergence test
+    // is made on it (0: never; the FP64 PCG never replaces).
+    int cg_residual_replacement = 0;
 };
 
 struct Context {
@@ -99,6 +109,8 @@ struct SolveStats {
     std::map<std::string, std::pair<int64_t, double>> kernels;
     // PCG iterations of each Newton iteration's linear solve, in order.
     std::vector<int> cg_iterations_per_newton;
+    // residual replacements made by the FP32 PCG (cg_residual_replacement)
+    int cg_residual_replacements = 0;
 };
 
 struct SolverImpl;

@@ -596,4 +596,192 @@ SYMXG_DEVICE int project_pd_deflated(T* __restrict__ H, T eps, bool mirroring, i
     return project_deflated_finish<T, NB>(H, b, eps, mirroring, not_converged);
 }
 
+// ---- FP64-accurate projection from an FP32 eigen-decomposition
+//
+// The cyclic Jacobi above converges in FP32 for a small fraction of its FP64 cost (GB300's
+// FP64 rate is 1/64 of FP32).  Its eigenvectors X (orthonormal and exact to ~1e-6) are then
+// refined in FP64 with one step of Ogita and Aishima's iterative refinement for the symmetric
+// eigenvalue problem (T. Ogita, K. Aishima, "Iterative refinement for symmetric eigenvalue
+// decomposition", Japan J. Indust. Appl. Math. 35 (2018) 1007-1035, Algorithm 1):
+//   R = I - X^T X,  S = X^T A X,  lam_i = s_ii / (1 - r_ii),
+//   delta = 2 (|S - diag(lam)| + |A| |R|)            (Frobenius norms bound the 2-norms),
+//   E_ij = (s_ij + lam_j r_ij) / (lam_j - lam_i) when |lam_i - lam_j| > delta, else r_ij / 2,
+//   X' = X + X E,
+// which squares the eigenvector error (one step takes FP32 vectors to ~1e-12 relative).  The
+// clamping is then applied as a correction to A itself, A + sum_k (lam'_k - lam_k) x'_k x'_k^T
+// over the clamped eigenvalues only, so the eigenpairs that do not change do not enter the
+// result at all and the correction carries the (small) clamped eigenvalues' accuracy.
+//
+// A is the upper triangle in FP64, X the FP32 eigenvectors (column k = eigenvector k).  dW
+// (upper triangle) receives the correction; returns true when some eigenvalue was clamped.
+template <int M>
+SYMXG_DEVICE bool refine_clamp_correction(const double (&A)[M * (M + 1) / 2], const float (&X)[M * M], double eps,
+                                          bool mirroring, double (&dW)[M * (M + 1) / 2])
+{
+    constexpr int MT = M * (M + 1) / 2;
+    double S[MT], R[MT];
+#pragma unroll 1
+    for (int j = 0; j < M; ++j) {
+        double y[M];  // A x_j
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            double t = 0.0;
+#pragma unroll
+            for (int k = 0; k < M; ++k) t = fma(A[tri<M>(i, k)], (double)X[k * M + j], t);
+            y[i] = t;
+        }
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            if (i > j) continue;
+            double s = 0.0, r = 0.0;
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+                const double xi = (double)X[k * M + i];
+                s = fma(xi, y[k], s);
+                r = fma(xi, (double)X[k * M + j], r);
+            }
+            S[tri<M>(i, j)] = s;
+            R[tri<M>(i, j)] = (i == j ? 1.0 : 0.0) - r;
+        }
+    }
+    double lam[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) lam[i] = S[tri<M>(i, i)] / (1.0 - R[tri<M>(i, i)]);
+    double nsd = 0.0, na = 0.0, nr = 0.0;
+#pragma unroll
+    for (int i = 0; i < M; ++i)
+#pragma unroll
+        for (int j = i; j < M; ++j) {
+            const double w = i == j ? 1.0 : 2.0;
+            const double sd = i == j ? S[tri<M>(i, i)] - lam[i] : S[tri<M>(i, j)];
+            nsd = fma(w * sd, sd, nsd);
+            na = fma(w * A[tri<M>(i, j)], A[tri<M>(i, j)], na);
+            nr = fma(w * R[tri<M>(i, j)], R[tri<M>(i, j)], nr);
+        }
+    const double delta = 2.0 * (sqrt(nsd) + sqrt(na) * sqrt(nr));
+#pragma unroll
+    for (int k = 0; k < MT; ++k) dW[k] = 0.0;
+    bool changed = false;
+#pragma unroll 1
+    for (int k = 0; k < M; ++k) {
+        const double l = lam[k];
+        if (!(l < eps)) continue;
+        changed = true;
+        const double c = (mirroring ? -l : eps) - l;
+        double x[M];  // x'_k = x_k + X E[:, k]
+#pragma unroll
+        for (int r = 0; r < M; ++r) x[r] = (double)X[r * M + k];
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            const double rik = R[tri<M>(i, k)];
+            double e;
+            if (i == k) e = 0.5 * rik;
+            else if (fabs(lam[i] - l) > delta) e = (S[tri<M>(i, k)] + l * rik) / (l - lam[i]);
+            else e = 0.5 * rik;
+#pragma unroll
+            for (int r = 0; r < M; ++r) x[r] = fma((double)X[r * M + i], e, x[r]);
+        }
+#pragma unroll
+        for (int p = 0; p < M; ++p)
+#pragma unroll
+            for (int q = p; q < M; ++q) dW[tri<M>(p, q)] = fma(c * x[p], x[q], dW[tri<M>(p, q)]);
+    }
+    return changed;
+}
+
+// Projection of one stored matrix H (S = float or double storage) with the FP32 Jacobi and
+// the FP64 refinement above.  Deflate: H is translation-invariant (an elastic element's
+// Hessian, as k_project_pd_sort found it): the decomposition is of b = Q^T H Q (Q the
+// Helmert basis of the translations' complement, (3 NB - 3) x (3 NB - 3)), and the result is
+// H + Q dW Q^T + lam_t / NB (1 1^T (x) I3) with the translation eigenvalues 0 -> eps (0 when
+// mirroring), as project_deflated_finish has it.  Otherwise the full N x N matrix is
+// decomposed and H + dW is stored.  Every sum is formed in FP64 and rounded once into S.
+// Returns 1 when H changed; sets *not_converged when the FP32 Jacobi hit its sweep cap.
+template <typename S, int NB, bool Deflate>
+SYMXG_DEVICE int project_pd_refined(S* __restrict__ H, double eps, bool mirroring, int* not_converged)
+{
+    constexpr int N = 3 * NB;
+    constexpr int M = Deflate ? N - 3 : N;
+    constexpr int MT = M * (M + 1) / 2;
+    double c[NB];
+    c[0] = 0.0;
+#pragma unroll
+    for (int m = 1; m < NB; ++m) c[m] = 1.0 / sqrt((double)(m * (m + 1)));
+    double b[MT];
+    if constexpr (Deflate) {
+        // b = Q^T H Q, row (m, d) of b = row 3 (m - 1) + d; H read entry by entry (L1 hits)
+#pragma unroll
+        for (int p = 0; p < M; ++p)
+#pragma unroll
+            for (int q = p; q < M; ++q) {
+                const int m = p / 3 + 1, d = p % 3, l = q / 3 + 1, e = q % 3;
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i <= m; ++i) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int j = 0; j <= l; ++j)
+                        t = fma(helmert<double, NB>(c, j, l), (double)H[bm_index<N>(3 * i + d, 3 * j + e)], t);
+                    s = fma(helmert<double, NB>(c, i, m), t, s);
+                }
+                b[tri<M>(p, q)] = s;
+            }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int j = i; j < N; ++j) b[tri<M>(i, j)] = (double)H[bm_index<N>(i, j)];
+    }
+    float a32[MT], v[M * M];
+#pragma unroll
+    for (int k = 0; k < MT; ++k) a32[k] = (float)b[k];
+#pragma unroll
+    for (int i = 0; i < M; ++i)
+#pragma unroll
+        for (int j = 0; j < M; ++j) v[i * M + j] = (i == j) ? 1.0f : 0.0f;
+    if (!jacobi_eigen<float, M>(a32, v) && not_converged) *not_converged = 1;
+    double dW[MT];
+    bool changed = refine_clamp_correction<M>(b, v, eps, mirroring, dW);
+    double lam_t = 0.0;
+    if (Deflate && 0.0 < eps) {
+        changed = true;
+        lam_t = mirroring ? 0.0 : eps;
+    }
+    if (!changed) return 0;
+    if constexpr (Deflate) {
+        const double diag_t = lam_t / (double)NB;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int j = i; j < N; ++j) {
+                const int in = i / 3, d = i % 3, jn = j / 3, e = j % 3;
+                double s = (d == e) ? diag_t : 0.0;
+#pragma unroll
+                for (int m = 1; m < NB; ++m) {
+                    if (m < in) continue;  // B[in][m] = 0 for in > m
+                    double t = 0.0;
+#pragma unroll
+                    for (int l = 1; l < NB; ++l) {
+                        if (l < jn) continue;
+                        t = fma(helmert<double, NB>(c, jn, l), dW[tri<M>(3 * (m - 1) + d, 3 * (l - 1) + e)], t);
+                    }
+                    s = fma(helmert<double, NB>(c, in, m), t, s);
+                }
+                const S out = (S)((double)H[bm_index<N>(i, j)] + s);
+                H[bm_index<N>(i, j)] = out;
+                H[bm_index<N>(j, i)] = out;
+            }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int j = i; j < N; ++j) {
+                const S out = (S)((double)H[bm_index<N>(i, j)] + dW[tri<M>(i, j)]);
+                H[bm_index<N>(i, j)] = out;
+                H[bm_index<N>(j, i)] = out;
+            }
+    }
+    return 1;
+}
+
 }  // namespace symxg_dev
