@@ -124,7 +124,7 @@ def workload_name(name, p):
 
 def projection_kernel(p):
     return {4: "k_project_pd_sort<float,12> + k_project_pd_deflated_listed<float,12> + k_project_pd_listed<float,12>",
-            10: "k_project_pd_generic<float> (30 x 30, one thread per matrix, cyclic Jacobi)",
+            10: "k_project_pd_pairs<float,30> (one warp per matrix, pair-block parallel Jacobi)",
             8: "k_project_pd_pairs<float,24> (one warp per matrix, pair-block parallel Jacobi)"}[element_kind(p)]
 
 

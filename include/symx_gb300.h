@@ -104,6 +104,9 @@ typedef struct symxg_newton_settings {
                                            refinement step, FP64 clamping correction), either precision */
     int32_t cg_residual_replacement; /* Mixed: every k PCG iterations replace the residual by b - A x
                                         accumulated in FP64 (0: never) */
+    int32_t cg_fp64_partial_sums;    /* Mixed: dot-product partials of the PCG summed in FP64 (1, default)
+                                        or float-float (0) */
+    int32_t pad;
 } symxg_newton_settings;
 
 typedef struct symxg_solve_stats {
@@ -203,7 +206,11 @@ int64_t symxg_wait_poll_limit(void);
 /* Project `count` symmetric n x n matrices (n = 3k <= 30), stored block-major (3x3 block
  * (a,b) at offset (a*k+b)*9, row-major inside), in place.  not_converged: device int set
  * to 1 if a Jacobi sweep cap was hit.  Replaces project_to_PD_inplace
- * (symx/src/solver/second_order/project_to_PD.cpp:12-81). */
+ * (symx/src/solver/second_order/project_to_PD.cpp:12-81).  n = 3..12 run one matrix per
+ * thread in registers, n = 18, 24, 30 one matrix per warp in shared memory.  n = 15, 21, 27
+ * run one matrix per thread with the matrix and its eigenvectors in local memory: the first
+ * such call makes the driver reserve local memory for every thread the device can hold
+ * (several GB in f64), which the context keeps until it is destroyed. */
 int symxg_project_pd_f32(float* matrices, int32_t n, int64_t count, float eps, int32_t mirroring,
                          int32_t* not_converged, void* stream);
 int symxg_project_pd_f64(double* matrices, int32_t n, int64_t count, double eps, int32_t mirroring,

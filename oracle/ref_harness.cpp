@@ -23,6 +23,10 @@
 //   symx_ref_harness mesh    d|f <type> <nx> <ny> <nz> <sx> <sy> <sz> <out.bin>   generate_cuboid_mesh
 //   symx_ref_harness rcm     <in.bin> <out.bin> <reorder_elements 0|1>           reorder_connectivity_RCM
 //   symx_ref_harness elem27  <in.bin> <out.bin>            NH Hex27 [E, g(81)] over get_integration_rule(Hex27)
+//   symx_ref_harness mixed   <in.bin> <out.bin>            NH Tet4 [dg/dmu (12), dg/dlambda (12)] via gradient()
+//   symx_ref_harness contact <problem.bin> <scene.bin> <outdir> <thr>
+//                     the step problem plus a conditional ground contact and a second DoF set
+//                     (handles): E and gradient at the initial state, NewtonsMethod::solve
 #include <symx>
 #include <Eigen/Sparse>
 
@@ -355,6 +359,143 @@ int mode_solve(const std::string& pfile, const std::string& outdir, int n_thread
     return ret == SolverReturn::Successful ? 0 : 3;
 }
 
+// Mixed second derivatives of the NH Tet4 element energy, d(dE/dx)/dmu and d(dE/dx)/dlambda,
+// through the reference's own symbolic differentiation (gradient(), symx/src/symbol/diff.h:32-35)
+// and Compiled<double>.  in: as mode_elem; out: n x 24.
+int mode_mixed(const std::string& in, const std::string& out)
+{
+    std::ifstream f(in, std::ios::binary);
+    int64_t n = 0;
+    f.read(reinterpret_cast<char*>(&n), sizeof(n));
+    std::vector<double> rows;
+    read_into(f, rows, (size_t)n * 26);
+    Workspace ws;
+    std::vector<Vector> x = ws.make_vectors(3, 4);
+    std::vector<Vector> X = ws.make_vectors(3, 4);
+    Scalar mu = ws.make_scalar();
+    Scalar lam = ws.make_scalar();
+    auto jac = [&](const std::vector<Vector>& v) {
+        Matrix J = ws.get_identity_matrix(3);
+        J.set_col(0, v[1] - v[0]);
+        J.set_col(1, v[2] - v[0]);
+        J.set_col(2, v[3] - v[0]);
+        return J;
+    };
+    Matrix F = jac(x) * jac(X).inv();
+    Scalar logdetF = log(F.det());
+    Scalar psi = 0.5 * mu * ((F.transpose() * F).trace() - 3.0) - mu * logdetF + 0.5 * lam * logdetF.powN(2);
+    Scalar E = psi * jac(X).det() * (1.0 / 6.0);
+    Vector g = gradient(E, collect_scalars(x));
+    std::vector<Scalar> outs;
+    for (int i = 0; i < 12; ++i) outs.push_back(gradient(g[i], std::vector<Scalar>{mu})[0]);
+    for (int i = 0; i < 12; ++i) outs.push_back(gradient(g[i], std::vector<Scalar>{lam})[0]);
+    Compiled<double> c(outs, "ref_harness_nh_tet4_mixed", symx::get_codegen_dir());
+    std::vector<double> result((size_t)n * 24);
+    for (int64_t e = 0; e < n; ++e) {
+        const double* r = rows.data() + 26 * e;
+        for (int v = 0; v < 4; ++v)
+            for (int d = 0; d < 3; ++d) {
+                c.set(x[v][d], r[3 * v + d]);
+                c.set(X[v][d], r[12 + 3 * v + d]);
+            }
+        c.set(mu, r[24]);
+        c.set(lam, r[25]);
+        View<double> o = c.run();
+        for (int i = 0; i < 24; ++i) result[24 * e + i] = o[i];
+    }
+    write_raw(out, result.data(), result.size());
+    return 0;
+}
+
+// The step problem of mode_solve plus
+//   * a cubic ground-contact penalty k p^3 / 3 on every vertex, p = ground_y - y, active only
+//     where p > 0 (the conditional-potential idiom of examples/dynamic_elasticity_with_contact.cpp:126-139);
+//   * a second DoF set, "handles" h_j, each tied to mesh vertex v_j by a spring
+//     k_s / 2 |x_v - h_j|^2 and pulled to a target t_j by k_p / 2 |h_j - t_j|^2.
+// scene.bin: f64 ground_y, k_contact, k_spring, k_pull; int64 n_handles; int32 vertex[n];
+// f64 handle[n*3], target[n*3].  Writes E.bin and grad.bin (x DoFs, then handle DoFs) at the
+// initial state, x_final.bin, h_final.bin and stats.json of NewtonsMethod::solve.
+int mode_contact(const std::string& pfile, const std::string& sfile, const std::string& outdir, int n_threads)
+{
+    Problem p = load_problem(pfile);
+    std::ifstream f(sfile, std::ios::binary);
+    double sc[4];
+    f.read(reinterpret_cast<char*>(sc), sizeof(sc));
+    int64_t nh = 0;
+    f.read(reinterpret_cast<char*>(&nh), sizeof(nh));
+    std::vector<int32_t> hv;
+    std::vector<double> tmp;
+    read_into(f, hv, (size_t)nh);
+    read_into(f, tmp, (size_t)nh * 3);
+    std::vector<Eigen::Vector3d> handles = to_vec3(tmp);
+    read_into(f, tmp, (size_t)nh * 3);
+    std::vector<Eigen::Vector3d> targets = to_vec3(tmp);
+    double ground_y = sc[0], k_contact = sc[1], k_spring = sc[2], k_pull = sc[3];
+    LabelledConnectivity<2> hconn{{"handle", "vertex"}};
+    for (int64_t j = 0; j < nh; ++j) hconn.numbered_push_back({hv[j]});
+
+    std::vector<int> numbered = numbered_connectivity(p);
+    spGlobalPotential G = build_global_potential(p, numbered);
+    G->add_potential("ground_contact", p.all_vertices,
+        [&](MappedWorkspace<double>& mws, Element& elem)
+        {
+            Vector x = mws.make_vector(p.x, elem[0]);
+            Scalar k = mws.make_scalar(k_contact);
+            Scalar yg = mws.make_scalar(ground_y);
+            Scalar pen = yg - x[1];
+            Scalar P = k * pen.powN(3) / 3.0;
+            Scalar cond = pen > 0.0;
+            return std::make_pair(P, cond);
+        });
+    G->add_potential("handle_spring", hconn,
+        [&](MappedWorkspace<double>& mws, Element& conn)
+        {
+            Vector x = mws.make_vector(p.x, conn["vertex"]);
+            Vector h = mws.make_vector(handles, conn["handle"]);
+            Scalar k = mws.make_scalar(k_spring);
+            return 0.5 * k * (x - h).squared_norm();
+        });
+    G->add_potential("handle_pull", hconn,
+        [&](MappedWorkspace<double>& mws, Element& conn)
+        {
+            Vector h = mws.make_vector(handles, conn["handle"]);
+            Vector t = mws.make_vector(targets, conn["handle"]);
+            Scalar k = mws.make_scalar(k_pull);
+            return 0.5 * k * (h - t).squared_norm();
+        });
+    G->add_dof(handles);
+    spContext ctx = make_context(n_threads, outdir);
+    {
+        SecondOrderCompiledGlobal compiled(G, ctx);
+        const int ndofs = G->get_total_n_dofs();
+        double E = 0.0;
+        Eigen::VectorXd grad(ndofs);
+        compiled.evaluate_P__dP_du__local_d2P_du2(E, grad);
+        write_raw(outdir + "/E.bin", &E, 1);
+        write_raw(outdir + "/grad.bin", grad.data(), (size_t)ndofs);
+    }
+    NewtonsMethod newton(G, ctx);
+    newton.settings.projection_mode = ProjectionToPD::ProjectedNewton;
+    newton.settings.projection_eps = 1e-10;
+    newton.settings.project_to_pd_use_mirroring = false;
+    newton.settings.linear_solver = LinearSolver::BDPCG;
+    newton.settings.cg_rel_tolerance = 1e-3;
+    newton.settings.line_search_armijo_beta = 1e-4;
+    newton.settings.residual_tolerance_abs = 1e-6;
+    SolverReturn ret = newton.solve();
+    std::vector<double> xf(3 * p.nv), hf(3 * nh);
+    for (int64_t i = 0; i < p.nv; ++i) for (int d = 0; d < 3; ++d) xf[3 * i + d] = p.x[i][d];
+    for (int64_t i = 0; i < nh; ++i) for (int d = 0; d < 3; ++d) hf[3 * i + d] = handles[i][d];
+    write_raw(outdir + "/x_final.bin", xf.data(), xf.size());
+    write_raw(outdir + "/h_final.bin", hf.data(), hf.size());
+    std::ofstream js(outdir + "/stats.json");
+    js << "{\n  \"return\": " << (int)ret
+       << ",\n  \"newton_iterations\": " << newton.get_last_solve_stats().newton_iterations
+       << ",\n  \"cg_iterations\": " << newton.get_last_solve_stats().cg_iterations
+       << ",\n  \"ls_bt_iterations\": " << newton.get_last_solve_stats().ls_bt_iterations << "\n}\n";
+    return ret == SolverReturn::Successful ? 0 : 3;
+}
+
 }  // namespace
 
 // generate_cuboid_mesh (mesh_generation.cpp:306-327) written as int64 {n_vertices, n_elements,
@@ -452,6 +593,9 @@ int main(int argc, char** argv)
     const int n_threads = argc > 4 ? std::atoi(argv[4]) : 1;
     if (mode == "elem") return mode_elem(argv[2], argv[3]);
     if (mode == "elem27") return mode_elem27(argv[2], argv[3]);
+    if (mode == "mixed") return mode_mixed(argv[2], argv[3]);
+    if (mode == "contact" && argc >= 5)
+        return mode_contact(argv[2], argv[3], argv[4], argc > 5 ? std::atoi(argv[5]) : 1);
     if (mode == "project") return mode_project(argv[2], argv[3]);
     if (mode == "eval") return mode_eval(argv[2], argv[3], n_threads);
     if (mode == "solve") {

@@ -379,10 +379,21 @@ __global__ void __launch_bounds__(64) k_project_pd_generic(T* __restrict__ H, in
 //     are back in their initial order, slot_index() below.
 // Only the upper triangle of A in shared memory is kept up to date.  No two lanes touch the
 // same entry within a round.
-template <typename T>
+template <typename T, int N>
 struct ProjPairsCfg {
     static constexpr int warps = sizeof(T) == 4 ? 8 : 4;
-    static constexpr int min_blocks = 4;  // float: 64 registers, 32 warps per SM
+    // 24 x 24 float: 64 registers, 32 warps per SM; 30 x 30 (Tet10) holds 30 eigenvector
+    // entries per lane and ~90 KB of shared memory per block: two blocks per SM
+    static constexpr int min_blocks = N <= 24 ? 4 : 2;
+    static constexpr int LD = N + 1;  // row stride of A and B (odd: conflict-free columns)
+    static constexpr int VS = (N + 3) / 4 * 4;  // row stride of V in the reconstruction (16-byte rows)
+    static constexpr int NP = N / 2, NR = N - 1, NOFF = NP * (NP - 1) / 2, SLOTS = (NOFF + 31) / 32;
+    static constexpr int mat_elems = N * LD > N * VS ? N * LD : N * VS;
+    // dynamic shared memory: A and B per warp, (c, s) per warp, the offset table
+    static constexpr size_t off_B = (size_t)warps * mat_elems * sizeof(T);
+    static constexpr size_t off_CS = off_B + (size_t)warps * mat_elems * sizeof(T);
+    static constexpr size_t off_tab = (off_CS + (size_t)warps * NP * 2 * sizeof(T) + 15) / 16 * 16;
+    static constexpr size_t smem_bytes = off_tab + (size_t)NR * SLOTS * 32 * sizeof(uint2);
 };
 
 // Pair k of round r as (a, b): position N - 1 is fixed, the others rotate.
@@ -433,7 +444,8 @@ struct Pair2<double> {
     using type = double2;
 };
 
-// sum_k w[k] * row[k] with 16-byte shared-memory loads (row 16-byte aligned)
+// sum_{k < N} w[k] * row[k] with 16-byte shared-memory loads (row 16-byte aligned, padded
+// to a multiple of 4 floats / 2 doubles)
 template <int N>
 __device__ __forceinline__ float row_dot(const float (&w)[N], const float* row)
 {
@@ -442,9 +454,9 @@ __device__ __forceinline__ float row_dot(const float (&w)[N], const float* row)
     for (int k = 0; k < N; k += 4) {
         const float4 r = *reinterpret_cast<const float4*>(row + k);
         acc = fmaf(w[k], r.x, acc);
-        acc = fmaf(w[k + 1], r.y, acc);
-        acc = fmaf(w[k + 2], r.z, acc);
-        acc = fmaf(w[k + 3], r.w, acc);
+        if (k + 1 < N) acc = fmaf(w[k + 1 < N ? k + 1 : k], r.y, acc);
+        if (k + 2 < N) acc = fmaf(w[k + 2 < N ? k + 2 : k], r.z, acc);
+        if (k + 3 < N) acc = fmaf(w[k + 3 < N ? k + 3 : k], r.w, acc);
     }
     return acc;
 }
@@ -456,7 +468,7 @@ __device__ __forceinline__ double row_dot(const double (&w)[N], const double* ro
     for (int k = 0; k < N; k += 2) {
         const double2 r = *reinterpret_cast<const double2*>(row + k);
         acc = fma(w[k], r.x, acc);
-        acc = fma(w[k + 1], r.y, acc);
+        if (k + 1 < N) acc = fma(w[k + 1 < N ? k + 1 : k], r.y, acc);
     }
     return acc;
 }
@@ -533,19 +545,24 @@ __device__ bool pairs_pd_shortcut(const T* __restrict__ A, T* __restrict__ B, in
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::min_blocks)
+__global__ void __launch_bounds__(ProjPairsCfg<T, N>::warps * 32, ProjPairsCfg<T, N>::min_blocks)
     k_project_pd_pairs(T* __restrict__ H, int64_t count, T eps, int mirroring, int* not_converged,
                        const int64_t* __restrict__ sel)
 {
-    static_assert(N % 6 == 0 && N <= 32, "N a multiple of 6 up to 30 (3 x 3 blocks, pairs, 16-byte rows)");
+    static_assert(N % 6 == 0 && N <= 30, "N a multiple of 6 up to 30 (3 x 3 blocks, pairs of indices)");
     using T2 = typename Pair2<T>::type;
-    constexpr int W = ProjPairsCfg<T>::warps;
-    constexpr int LD = N + 1, NP = N / 2, NR = N - 1, NOFF = NP * (NP - 1) / 2, SLOTS = (NOFF + 31) / 32, nb = N / 3;
-    __shared__ __align__(16) T sA[W][N * LD];
-    __shared__ __align__(16) T sB[W][N * LD];  // deflated copy for the positive-definiteness test
-    __shared__ __align__(16) T2 sCS[W][NP];  // (c, s) of the round's rotations
-    __shared__ uint2 sTab[NR][SLOTS][32];     // per round, slot and lane: 4 x 16-bit entry offsets
+    using Cfg = ProjPairsCfg<T, N>;
+    constexpr int W = Cfg::warps, LD = Cfg::LD, VS = Cfg::VS;
+    constexpr int NP = Cfg::NP, NR = Cfg::NR, NOFF = Cfg::NOFF, SLOTS = Cfg::SLOTS, nb = N / 3;
+    // dynamic shared memory (Cfg::smem_bytes): per warp A and a deflated copy B (the
+    // positive-definiteness test), (c, s) of the round's rotations, and per round, slot and
+    // lane the 4 x 16-bit entry offsets of an off-diagonal pair block
+    extern __shared__ __align__(16) unsigned char pairs_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T* sA = reinterpret_cast<T*>(pairs_smem) + (size_t)w * Cfg::mat_elems;
+    T* sB = reinterpret_cast<T*>(pairs_smem + Cfg::off_B) + (size_t)w * Cfg::mat_elems;
+    T2* sCS = reinterpret_cast<T2*>(pairs_smem + Cfg::off_CS) + (size_t)w * NP;
+    uint2* sTab = reinterpret_cast<uint2*>(pairs_smem + Cfg::off_tab);  // [NR][SLOTS][32]
 
     for (int e = threadIdx.x; e < NR * SLOTS * 32; e += blockDim.x) {
         const int r = e / (SLOTS * 32), j = (e / 32) % SLOTS, ln = e % 32, b = ln + 32 * j;
@@ -559,15 +576,15 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
             v.x = up(ak, al) | (up(ak, bl) << 16);
             v.y = up(bk, al) | (up(bk, bl) << 16);
         }
-        sTab[r][j][ln] = v;
+        sTab[(r * SLOTS + j) * 32 + ln] = v;
     }
     int bk[SLOTS], bl[SLOTS];
 #pragma unroll
     for (int j = 0; j < SLOTS; ++j) off_block<NP>(lane + 32 * j < NOFF ? lane + 32 * j : 0, bk[j], bl[j]);
     __syncthreads();
 
-    T* A = sA[w];
-    T2* CS = sCS[w];
+    T* A = sA;
+    T2* CS = sCS;
     int nc = 0;
     constexpr int max_sweeps = 2 * symxg_dev::JacobiTol<T>::max_double_sweeps;
     for (int64_t item = (int64_t)blockIdx.x * W + w; item < count; item += (int64_t)gridDim.x * W) {
@@ -581,7 +598,7 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
             f += v * v;
         }
         __syncwarp();
-        if (pairs_pd_shortcut<T, N>(A, sB[w], lane)) continue;  // H stays as it is
+        if (pairs_pd_shortcut<T, N>(A, sB, lane)) continue;  // H stays as it is
         T v[N];
 #pragma unroll
         for (int s = 0; s < N; ++s) v[s] = lane == slot_index<N>(s) ? T(1) : T(0);
@@ -618,7 +635,7 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
 #pragma unroll
                 for (int j = 0; j < SLOTS; ++j) {
                     if ((j + 1) * 32 <= NOFF || lane + 32 * j < NOFF) {
-                        const uint2 e = sTab[r][j][lane];
+                        const uint2 e = sTab[(r * SLOTS + j) * 32 + lane];
                         const T2 rk = CS[bk[j]], rl = CS[bl[j]];
                         const unsigned e00 = e.x & 0xffffu, e01 = e.x >> 16, e10 = e.y & 0xffffu, e11 = e.y >> 16;
                         const T b00 = A[e00], b01 = A[e01], b10 = A[e10], b11 = A[e11];
@@ -662,16 +679,17 @@ __global__ void __launch_bounds__(ProjPairsCfg<T>::warps * 32, ProjPairsCfg<T>::
         const bool changed = __any_sync(0xffffffffu, mine);
         if (changed) {
             __syncwarp();  // eigenvalues read before V overwrites A
+            // rows of V with stride VS (a multiple of 4) for 16-byte row reads
             if (lane < N) {
 #pragma unroll
-                for (int s = 0; s < N; ++s) A[lane * N + s] = v[s];
+                for (int s = 0; s < N; ++s) A[lane * VS + s] = v[s];
             }
 #pragma unroll
             for (int s = 0; s < N; ++s) v[s] *= __shfl_sync(0xffffffffu, lam, slot_index<N>(s));  // V diag(lambda)
             __syncwarp();
             if (lane < N) {
                 const int i = lane, bi = (i / 3) * nb, ri = (i % 3) * 3;
-                for (int j = 0; j < N; ++j) h[(bi + j / 3) * 9 + ri + j % 3] = row_dot<N>(v, A + j * N);
+                for (int j = 0; j < N; ++j) h[(bi + j / 3) * 9 + ri + j % 3] = row_dot<N>(v, A + j * VS);
             }
         }
         __syncwarp();  // the next matrix reuses this warp's shared memory
@@ -1148,6 +1166,24 @@ __host__ __device__ __forceinline__ size_t staged_stage_bytes(int cap, int stage
 // (kStagedPartSlots chunks in flight at most, with a count of the warps that stored theirs),
 // then the ring of stages.  The chunk slots and partials are used by the persistent kernel.
 constexpr int kStagedPartSlots = 2 * kStagedMaxStages;
+constexpr int kPcgGroupChunks = 16;  // chunks per FP64 group partial of the persistent PCG
+
+// B.partials of the persistent kernel with FP64 sums, in doubles: chunk partials, group
+// partials, r.r and r.z block partials, then the group counters (unsigned, zeroed at launch).
+struct PcgSumsLayout {
+    int n_groups, group, rr, rz, ctr, total;
+};
+__host__ __device__ __forceinline__ PcgSumsLayout pcg_sums_layout(int n_chunks, int grid)
+{
+    PcgSumsLayout L;
+    L.n_groups = (n_chunks + kPcgGroupChunks - 1) / kPcgGroupChunks;
+    L.group = n_chunks;
+    L.rr = L.group + L.n_groups;
+    L.rz = L.rr + grid;
+    L.ctr = L.rz + grid;
+    L.total = L.ctr + (L.n_groups + 1) / 2;
+    return L;
+}
 constexpr size_t kStagedHeaderBytes =
     (16 * kStagedMaxStages + 4 * kStagedMaxStages + 4 * kStagedPartSlots +
      8 * kStagedPartSlots * kStagedConsumerWarps + 127) / 128 * 128;
@@ -1377,11 +1413,38 @@ __device__ __forceinline__ void dyn_take(const PcgBuffers<float>& B, int n_chunk
         if (P.unit0 + k <= P.unit_end) P.rp[k] = __ldcg(B.staged.row_ptr_ext + (P.unit0 + k) * S);
 }
 
+// Where the product pass leaves p.q.  FF sums: one float-float partial per chunk (part_ff),
+// summed after the barrier in float-float.  FP64 sums: one FP64 partial per chunk (the
+// chunk's float-float sum converted exactly), and the last of the kPcgGroupChunks chunks of a
+// fixed group to publish adds the group's partials in chunk order in FP64 (group counters,
+// zero at launch, reset by that last publisher); after the barrier the group partials are
+// summed in FP64.  Both orders are fixed, so p.q does not depend on which block took which
+// chunk.
+// Both live in B.partials (pcg_sums_layout); their addresses are formed from the kernel
+// parameters where they are used, so the consumer loop holds no extra pointers.
+//
+// FP64 publication of chunk c's float-float sum (hi, lo), by one thread.
+__device__ __forceinline__ void publish_chunk_f64(double* partials, int n_chunks, int c, float hi, float lo)
+{
+    const PcgSumsLayout lay = pcg_sums_layout(n_chunks, (int)gridDim.x);
+    unsigned* group_ctr = reinterpret_cast<unsigned*>(partials + lay.ctr);
+    partials[c] = (double)hi + (double)lo;  // exact
+    const int grp = c / kPcgGroupChunks, g0 = grp * kPcgGroupChunks;
+    const unsigned members = (unsigned)min(kPcgGroupChunks, n_chunks - g0);
+    __threadfence();
+    if (atomicAdd(&group_ctr[grp], 1u) == members - 1) {
+        __threadfence();
+        double acc = 0.0;
+        for (unsigned i = 0; i < members; ++i) acc += __ldcg(partials + g0 + i);
+        partials[lay.group + grp] = acc;
+        group_ctr[grp] = 0u;  // the next pass starts after a grid barrier
+    }
+}
+template <bool kF64Sums>
 __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B, const StagedShared& ss, int li,
                                                      unsigned* ctr, int n_chunks, const float* __restrict__ p_old,
                                                      float* __restrict__ p_new, bool first, float beta, unsigned& seq,
-                                                     unsigned& issued, DynProducer& P, volatile int* abort_flag,
-                                                     float2* __restrict__ part)
+                                                     unsigned& issued, DynProducer& P, volatile int* abort_flag)
 {
     const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
     const size_t stage_bytes = staged_stage_bytes(CAP, S);
@@ -1491,8 +1554,12 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                     __threadfence_block();
                     FF sum{wp[0].x, wp[0].y};
                     for (int w = 1; w < kStagedConsumerWarps; ++w) sum = ff_add(sum, FF{wp[w].x, wp[w].y});
-                    part[pend_c] = make_float2(sum.hi, sum.lo);
                     ss.wcount[pend_ps] = 0;
+                    if constexpr (kF64Sums) {
+                        publish_chunk_f64(B.partials, n_chunks, pend_c, sum.hi, sum.lo);
+                    } else {
+                        reinterpret_cast<float2*>(B.partials)[pend_c] = make_float2(sum.hi, sum.lo);
+                    }
                 }
             }
             pend_c = -1;
@@ -1699,6 +1766,19 @@ __device__ double sum_chunk_partials(const float2* part, int n, double* sh)
     return result;
 }
 
+// Sum of n FP64 partials in one fixed order (the same in every block), returned to every
+// thread.
+__device__ double sum_partials_f64(const double* p, int n, double* sh)
+{
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a += __ldcg(p + i);
+    const double r = block_reduce<false>(a, sh);
+    __shared__ double result;
+    if (threadIdx.x == 0) result = r;
+    __syncthreads();
+    return result;
+}
+
 __global__ void __launch_bounds__(kStagedThreads, 1)
     k_pcg_spmv_staged(PcgBuffers<float> B, const float* __restrict__ p_old, float* __restrict__ p_new, int first)
 {
@@ -1849,6 +1929,8 @@ __host__ __device__ __forceinline__ int pcg_chunks(int n_blocks, int stage_rows)
     return (n_blocks + stage_rows - 1) / stage_rows;
 }
 
+
+template <bool kF64Sums>
 __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffers<float> B)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1869,9 +1951,11 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
     DynProducer P;
     const unsigned G = gridDim.x;
     const int n_chunks = pcg_chunks(B.n_blocks, B.staged.stage_rows);
-    float2* part_pq = reinterpret_cast<float2*>(B.partials);
-    float2* part_rr = reinterpret_cast<float2*>(B.partials + n_chunks);
+    const PcgSumsLayout lay = pcg_sums_layout(n_chunks, (int)G);
+    float2* part_rr = reinterpret_cast<float2*>(B.partials + n_chunks);  // FF sums
     float2* part_rz = part_rr + G;
+    double* part_rr64 = B.partials + lay.rr;  // FP64 sums
+    double* part_rz64 = B.partials + lay.rz;
     const int row_begin = (int)((int64_t)blockIdx.x * B.n_blocks / G);
     const int row_end = (int)((int64_t)(blockIdx.x + 1) * B.n_blocks / G);
     // a launch after a residual replacement continues the recurrence: beta from the state
@@ -1883,15 +1967,16 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         float* p_old = (iteration & 1) ? B.p : B.p2;
         float* p_new = (iteration & 1) ? B.p2 : B.p;
         const bool first = iteration == 0;
-        staged_spmv_pass_dyn(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : (float)beta, seq, issued, P,
-                             abort_flag, part_pq);
+        staged_spmv_pass_dyn<kF64Sums>(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : (float)beta, seq,
+                                       issued, P, abort_flag);
         if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls) || *abort_flag) {
             failed = true;
             break;
         }
         // no block claims from pass li - 1 any more, none from pass li + 2 before the next barrier
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ctr[(li + 2) % 3], 0u);
-        pAp = sum_chunk_partials(part_pq, n_chunks, sh);
+        pAp = kF64Sums ? sum_partials_f64(B.partials + lay.group, lay.n_groups, sh)
+                       : sum_chunk_partials(reinterpret_cast<const float2*>(B.partials), n_chunks, sh);
         if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
             indefinite = 1;
             iteration += 1;
@@ -1928,15 +2013,25 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         FF brr, brz;
         block_sum2_ff(rra.v, rza.v, sh, brr, brz);
         if (threadIdx.x == 0) {
-            part_rr[blockIdx.x] = make_float2(brr.hi, brr.lo);
-            part_rz[blockIdx.x] = make_float2(brz.hi, brz.lo);
+            if (kF64Sums) {
+                part_rr64[blockIdx.x] = (double)brr.hi + (double)brr.lo;
+                part_rz64[blockIdx.x] = (double)brz.hi + (double)brz.lo;
+            } else {
+                part_rr[blockIdx.x] = make_float2(brr.hi, brr.lo);
+                part_rz[blockIdx.x] = make_float2(brz.hi, brz.lo);
+            }
         }
         if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls)) {
             failed = true;
             break;
         }
         double rz_new;
-        sum_grid_partials2_ff(part_rr, part_rz, sh, rr, rz_new);
+        if (kF64Sums) {
+            rr = sum_partials_f64(part_rr64, (int)G, sh);
+            rz_new = sum_partials_f64(part_rz64, (int)G, sh);
+        } else {
+            sum_grid_partials2_ff(part_rr, part_rz, sh, rr, rz_new);
+        }
         iteration += 1;
         error = sqrt(rr / st0.bb);
         if (error < st0.abs_tol || error / st0.error0 < st0.rel_tol) {
@@ -2230,6 +2325,37 @@ void launch_dot_mixed(const T* a, const double* b, int64_t n, double* partials, 
     check_launch("dot");
 }
 
+// Warp-per-matrix projection (k_project_pd_pairs) of N x N matrices, N = 18, 24 or 30: a
+// persistent grid of the resident blocks, dynamic shared memory set up once per device.
+template <typename T, int N>
+void launch_project_pd_pairs(T* H, int64_t count, T eps, bool mirroring, int* not_converged, const int64_t* sel,
+                             cudaStream_t s)
+{
+    using Cfg = ProjPairsCfg<T, N>;
+    constexpr int threads = Cfg::warps * 32;
+    static std::mutex m;
+    static std::map<int, bool> configured;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lock(m);
+        if (!configured[dev]) {
+            const cudaError_t e = cudaFuncSetAttribute(k_project_pd_pairs<T, N>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::smem_bytes);
+            if (e != cudaSuccess)
+                throw std::runtime_error(std::string("symx_gb300: projection shared memory: ") + cudaGetErrorString(e));
+            configured[dev] = true;
+        }
+    }
+    int per_sm = 0, sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project_pd_pairs<T, N>, threads, Cfg::smem_bytes);
+    const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
+    const unsigned need = blocks_for(count, Cfg::warps);
+    k_project_pd_pairs<T, N><<<need < grid ? need : grid, threads, Cfg::smem_bytes, s>>>(H, count, eps, mirroring,
+                                                                                        not_converged, sel);
+}
+
 template <typename T>
 void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* not_converged, cudaStream_t s,
                        ProjectionScratch scratch, const int64_t* sel)
@@ -2269,14 +2395,9 @@ void launch_project_pd(T* H, int N, int64_t count, T eps, bool mirroring, int* n
         case 6: k_project_pd_unrolled<T, 6><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
         case 9: k_project_pd_unrolled<T, 9><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
         case 12: k_project_pd_unrolled<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, eps, mirroring, not_converged, sel); break;
-        case 24: {
-            constexpr int threads = ProjPairsCfg<T>::warps * 32;
-            const unsigned grid = resident_grid(k_project_pd_pairs<T, 24>, threads);
-            const unsigned need = blocks_for(count, ProjPairsCfg<T>::warps);
-            k_project_pd_pairs<T, 24><<<need < grid ? need : grid, threads, 0, s>>>(H, count, eps, mirroring,
-                                                                                   not_converged, sel);
-            break;
-        }
+        case 18: launch_project_pd_pairs<T, 18>(H, count, eps, mirroring, not_converged, sel, s); break;
+        case 24: launch_project_pd_pairs<T, 24>(H, count, eps, mirroring, not_converged, sel, s); break;
+        case 30: launch_project_pd_pairs<T, 30>(H, count, eps, mirroring, not_converged, sel, s); break;
         default:
             if (N > 30 || N % 3 != 0) throw std::runtime_error("symx_gb300: projection supports N = 3k <= 30");
             k_project_pd_generic<T><<<blocks_for(count, 64), 64, 0, s>>>(H, N, count, eps, mirroring, not_converged, sel);
@@ -2403,8 +2524,16 @@ void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s)
     PcgBuffers<float> arg = B;
     arg.staged.max_polls = wait_poll_limit();
     void* args[] = {&arg};
-    const cudaError_t l = cudaLaunchCooperativeKernel((const void*)k_pcg_solve_staged, dim3(B.staged.grid),
-                                                      dim3(kStagedThreads), args, B.staged.smem_bytes, s);
+    const void* fn = (const void*)k_pcg_solve_staged<false>;
+    if (B.staged.f64_sums) {
+        const PcgSumsLayout lay = pcg_sums_layout(pcg_chunks(B.n_blocks, B.staged.stage_rows), B.staged.grid);
+        const cudaError_t z =
+            cudaMemsetAsync(B.partials + lay.ctr, 0, sizeof(unsigned) * (size_t)lay.n_groups, s);  // group counters
+        if (z != cudaSuccess) throw std::runtime_error(std::string("symx_gb300: memset: ") + cudaGetErrorString(z));
+        fn = (const void*)k_pcg_solve_staged<true>;
+    }
+    const cudaError_t l = cudaLaunchCooperativeKernel(fn, dim3(B.staged.grid), dim3(kStagedThreads), args,
+                                                      B.staged.smem_bytes, s);
     if (l != cudaSuccess)
         throw std::runtime_error(std::string("symx_gb300: cooperative launch of the PCG failed: ") + cudaGetErrorString(l));
     check_launch("pcg_solve_staged");
@@ -2454,14 +2583,20 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
             continue;
         }
         // the persistent form needs every block resident at once (cooperative launch)
-        int coop = 0, resident_solve = 0;
+        int coop = 0, resident_ff = 0, resident_f64 = 0;
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         if (coop &&
-            cudaFuncSetAttribute(k_pcg_solve_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+            cudaFuncSetAttribute(k_pcg_solve_staged<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
                 cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_solve, k_pcg_solve_staged, kStagedThreads, smem) ==
+            cudaFuncSetAttribute(k_pcg_solve_staged<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
                 cudaSuccess &&
-            resident_solve >= per_sm && pcg_chunks(n, S) + 2 * grid <= 2 * kPcgMaxPartials)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_ff, k_pcg_solve_staged<false>, kStagedThreads,
+                                                          smem) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_f64, k_pcg_solve_staged<true>, kStagedThreads,
+                                                          smem) == cudaSuccess &&
+            resident_ff >= per_sm && resident_f64 >= per_sm &&
+            pcg_sums_layout(pcg_chunks(n, S), (int)grid).total <= 2 * kPcgMaxPartials &&
+            pcg_chunks(n, S) + 2 * grid <= 2 * kPcgMaxPartials)
             st.persistent = 1;
         cudaGetLastError();
         st.stages = stages;

@@ -149,6 +149,9 @@ struct PcgBuffers {
         size_t smem_bytes = 0;
         int persistent = 0;      // 1: the whole PCG loop can run as one cooperative launch
         long long max_polls = kDefaultWaitPolls;  // set from wait_poll_limit() at each launch
+        // one-launch PCG: chunk and block partials of p.Ap, r.r, r.z summed in FP64 (1) or in
+        // float-float (0); the per-thread and per-warp sums are float-float in both
+        int f64_sums = 1;
         const int32_t* row_ptr_ext = nullptr;  // row_ptr, then nnzb repeated to grid * rows_per_block + stage_rows + 8
         const int32_t* cols_ext = nullptr;     // cols, padded with zeros to a multiple of 4 plus 4
     } staged;

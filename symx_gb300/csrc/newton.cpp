@@ -1296,7 +1296,10 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     B.partials = I.partials.p;
     B.tickets = I.tickets.p;
     B.state = I.pcg_state.p;
-    if constexpr (std::is_same<T, float>::value) B.staged = I.staged;
+    if constexpr (std::is_same<T, float>::value) {
+        B.staged = I.staged;
+        B.staged.f64_sums = S.cg_fp64_partial_sums ? 1 : 0;
+    }
     T* du = V[0].p;
 
     if (S.linear_solver != LinearSolver::BDPCG) throw std::runtime_error("symx_gb300: only the BDPCG linear solver is implemented");

@@ -78,6 +78,10 @@ struct NewtonSettings {
     // replaced by the true residual b - A x accumulated in FP64 and the convergence test
     // is made on it (0: never; the FP64 PCG never replaces).
     int cg_residual_replacement = 0;
+    // One-launch FP32 PCG (Mixed): the chunk and block partials of its dot products (p.Ap,
+    // r.r, r.z) are accumulated in FP64 in a fixed order; false: in float-float.  Products
+    // and the per-thread and per-warp sums are float-float (exact products) in both.
+    bool cg_fp64_partial_sums = true;
 };
 
 struct Context {

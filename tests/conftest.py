@@ -46,3 +46,20 @@ def compiled_test(lib):
                     "-Wl,-rpath," + libdir, "-L" + os.path.join(cuda, "lib64"), "-lcudart",
                     "-Wl,-rpath," + os.path.join(cuda, "lib64")], check=True)
     return exe
+
+
+@pytest.fixture(scope="session")
+def gpu_api_test(lib):
+    """tests/cpp/test_gpu_api.cpp built against the library (the C++ drop-in API with user
+    potentials, NewtonsMethod on the GPU)."""
+    import subprocess
+
+    from symx_gb300.build import cuda_home
+
+    libdir = os.path.join(ROOT, "symx_gb300", "_build")
+    exe = os.path.join(libdir, "test_gpu_api")
+    cuda = cuda_home()
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(cuda, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "test_gpu_api.cpp"), "-o", exe, "-L" + libdir, "-lsymxg",
+                    "-Wl,-rpath," + libdir], check=True)
+    return exe

@@ -36,6 +36,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from symx_gb300 import problems  # noqa: E402
+sys.path.insert(0, HERE)
+from problem_io import contact_scene, write_problem, write_scene  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "symx_ref_harness")
 sys.path.insert(0, ROOT)
@@ -46,21 +48,6 @@ REF_DOC = os.path.join(reference_dir(), "docs", "source", "compilation.md")
 
 def run(*args):
     subprocess.run([HARNESS, *map(str, args)], check=True, stdout=subprocess.DEVNULL)
-
-
-def write_problem(path, p):
-    nv, ne, nn = p["X"].shape[0], p["conn"].shape[0], p["conn"].shape[1]
-    with open(path, "wb") as f:
-        np.array([nv, ne, p["bc_idx"].size, nn], dtype=np.int64).tofile(f)
-        np.array([p["dt"], *p["gravity"], p["k_bc"]], dtype=np.float64).tofile(f)
-        for k in ("X", "x0", "v0", "x_init"):
-            np.ascontiguousarray(p[k], dtype=np.float64).tofile(f)
-        np.ascontiguousarray(p["mass"], dtype=np.float64).tofile(f)
-        np.ascontiguousarray(p["conn"], dtype=np.int32).tofile(f)
-        np.ascontiguousarray(p["mu"], dtype=np.float64).tofile(f)
-        np.ascontiguousarray(p["lam"], dtype=np.float64).tofile(f)
-        np.ascontiguousarray(p["bc_idx"], dtype=np.int32).tofile(f)
-        np.ascontiguousarray(p["bc_target"], dtype=np.float64).tofile(f)
 
 
 def random_tets(seed, n):
@@ -186,6 +173,50 @@ def make_case(tmp, case, solve_iters=(1, -1), keep_triplets=True):
         sol[f"log_{tag}"] = open(os.path.join(sd, "log.txt")).read()
     np.savez_compressed(os.path.join(HERE, f"{case}_solve.npz"), **sol)
     return out, sol
+
+
+def make_mixed(tmp):
+    """d(dE/dx)/dmu and d(dE/dx)/dlambda of the NH Tet4 element through the reference's own
+    gradient() and Compiled<double>: on the seeded elements of elem_nh_tet4 and on every
+    element of tet4_6p at its initial state."""
+    rows_rand = random_tets(7, 64)
+    p = problems.step_problem("tet4_6p")
+    c = p["conn"]
+    rows_mesh = np.concatenate([p["x_init"][c].reshape(-1, 12), p["X"][c].reshape(-1, 12), p["mu"][:, None],
+                                p["lam"][:, None]], axis=1)
+    out = {}
+    for tag, rows in (("random", rows_rand), ("tet4_6p", rows_mesh)):
+        fin, fout = os.path.join(tmp, f"mixed_{tag}.in"), os.path.join(tmp, f"mixed_{tag}.out")
+        with open(fin, "wb") as f:
+            np.array([rows.shape[0]], dtype=np.int64).tofile(f)
+            rows.tofile(f)
+        run("mixed", fin, fout)
+        res = np.fromfile(fout).reshape(rows.shape[0], 24)
+        out[f"inputs_{tag}"] = rows
+        out[f"dg_dmu_{tag}"] = res[:, :12]
+        out[f"dg_dlam_{tag}"] = res[:, 12:]
+    np.savez_compressed(os.path.join(HERE, "mixed_nh_tet4.npz"), **out)
+    return out
+
+
+def make_contact(tmp, case="tet4_6p"):
+    """The step problem plus a conditional ground contact and a second DoF set (handles):
+    energy and gradient at the initial state and the solve, from the reference."""
+    p = problems.step_problem(case)
+    scene = contact_scene(p)
+    pfile, sfile = os.path.join(tmp, f"{case}_c.bin"), os.path.join(tmp, f"{case}_scene.bin")
+    write_problem(pfile, p)
+    write_scene(sfile, scene)
+    sd = os.path.join(tmp, f"{case}_contact")
+    os.makedirs(sd, exist_ok=True)
+    subprocess.run([HARNESS, "contact", pfile, sfile, sd, "1"], check=True, stdout=open(os.path.join(sd, "log.txt"), "w"))
+    rd = lambda name: np.fromfile(os.path.join(sd, name), dtype=np.float64)  # noqa: E731
+    stats = json.load(open(os.path.join(sd, "stats.json")))
+    out = dict(E=rd("E.bin")[0], grad=rd("grad.bin"), x_full=rd("x_final.bin").reshape(-1, 3),
+               h_full=rd("h_final.bin").reshape(-1, 3), **{k: stats[k] for k in stats},
+               log=open(os.path.join(sd, "log.txt")).read())
+    np.savez_compressed(os.path.join(HERE, f"{case}_contact.npz"), **out)
+    return out
 
 
 MODES = {0: "newton", 1: "projected", 2: "on_demand", 3: "progressive"}
@@ -320,6 +351,13 @@ def main():
             make_meshes(tmp)
             make_rcm(tmp)
             print(make_elem27(tmp)[:, :3])
+        return
+    if sys.argv[1:] == ["contact"]:  # conditional potential + second DoF set, and the mixed derivatives
+        with tempfile.TemporaryDirectory() as tmp:
+            out = make_contact(tmp)
+            print({k: out[k] for k in ("E", "return", "newton_iterations", "cg_iterations")})
+            mx = make_mixed(tmp)
+            print(mx["dg_dmu_random"][0, :3])
         return
     if sys.argv[1:] == ["modes"]:  # only the projection-mode fixture
         with tempfile.TemporaryDirectory() as tmp:

@@ -352,3 +352,18 @@ def test_cpp_hex27_element_matches_reference(cpp_test, golden, tmp_path):
     out = np.fromfile(fout).reshape(-1, 82)
     assert np.max(np.abs(out[:, 0] - ref[:, 0])) <= 1e-12 * np.max(np.abs(ref[:, 0]))
     assert np.max(np.abs(out[:, 1:] - ref[:, 1:])) <= 1e-12 * np.max(np.abs(ref[:, 1:]))
+
+
+def test_oracle_mixed_derivatives_match_reference_symbolic(golden):
+    """The oracle's adjoint uses dg/dmu = g(mu = 1, lambda = 0) and dg/dlambda = g(0, 1) (the
+    Neo-Hookean energy is linear in both); the reference's own gradient() of the element
+    gradient gives the same values (tests/golden/mixed_nh_tet4.npz)."""
+    d = golden("mixed_nh_tet4")
+    for tag in ("random", "tet4_6p"):
+        rows = d[f"inputs_{tag}"]
+        x, X = rows[:, :12].reshape(-1, 4, 3), rows[:, 12:24].reshape(-1, 4, 3)
+        one, zero = np.ones(rows.shape[0]), np.zeros(rows.shape[0])
+        _, g_mu, _ = O.nh_element_batch(x, X, one, zero, want_hess=False)
+        _, g_lam, _ = O.nh_element_batch(x, X, zero, one, want_hess=False)
+        for got, ref in ((g_mu, d[f"dg_dmu_{tag}"]), (g_lam, d[f"dg_dlam_{tag}"])):
+            assert np.max(np.abs(got.reshape(ref.shape) - ref)) <= 1e-12 * np.max(np.abs(ref))
