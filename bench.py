@@ -181,7 +181,7 @@ def run_ours(args):
 
     def device_solve(precision, **kw):
         solver.set_settings(precision=precision, **{"projection_fp64_refinement": 0, "cg_residual_replacement": 0,
-                                                    **kw})
+                                                    "cg_fp64_partial_sums": 1, **kw})
         solver.set_state(p["x_init"], p["x0"], p["v0"])
         solver.upload()
         torch.cuda.synchronize()
@@ -226,7 +226,8 @@ def run_ours(args):
     # every 50 PCG iterations; and the FP64 form with the same refined projection
     variants = {"mixed_fp64_projection_and_residual": ("mixed", dict(projection_fp64_refinement=1,
                                                                      cg_residual_replacement=50)),
-                "fp64_refined_projection": ("fp64", dict(projection_fp64_refinement=1))}
+                "fp64_refined_projection": ("fp64", dict(projection_fp64_refinement=1)),
+                "mixed_float_float_partial_sums": ("mixed", dict(cg_fp64_partial_sums=0))}
     variant_out, variant_x = {}, {}
     for name, (prec, kw) in variants.items():
         if args.no_variants:
