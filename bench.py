@@ -596,13 +596,17 @@ def measure_rollout(args):
            "n_elements": int(p["conn"].shape[0]), "steps": n_steps, "checkpoint_every": every,
            "loss": "0.5 |centroid(x_N) - target|^2; gradients wrt v0 and ln E"}
     grads = {}
+    lib = sg.load()
+    cur, peak = __import__("ctypes").c_int64(), __import__("ctypes").c_int64()
     for precision in ("fp64", "mixed"):
         free0, total = torch.cuda.mem_get_info()
+        lib.symxg_device_memory(None, None, 1)  # high-water mark from here
         s, info_f, xN, L = forward(p, precision)
         d = xN.mean(axis=0) - p["target"]
         dLdx = np.tile(d / xN.shape[0], (xN.shape[0], 1))
         g = s.rollout_backward(dLdx, rel_tol=1e-10)  # mixed: FP32 PCG inside FP64 defect correction
         free1, _ = torch.cuda.mem_get_info()
+        lib.symxg_device_memory(__import__("ctypes").byref(cur), __import__("ctypes").byref(peak), 0)
         grads[precision] = (g["dLdv0"], p["mu"] * g["dLdmu"] + p["lam"] * g["dLdlam"])
         out[precision] = {"forward_s": round(info_f["seconds_forward"], 3),
                           "backward_s": round(g["info"]["seconds_backward"], 3),
@@ -610,22 +614,38 @@ def measure_rollout(args):
                           "recomputed_steps": g["info"]["recomputed_steps"],
                           "armijo_polished_steps": info_f["armijo_polished_steps"] + g["info"]["armijo_polished_steps"],
                           "adjoint_pcg_iterations": g["info"]["adjoint_iterations"],
-                          "device_memory_held_mb": round((free0 - free1) / 2**20, 1), "loss": L}
+                          "device_memory_peak_mb": round(peak.value / 2**20, 1),
+                          "device_memory_peak_note": "high-water mark of the library's device buffers over the "
+                                                     "forward and backward rollout (symxg_device_memory)",
+                          "device_memory_held_after_mb": round((free0 - free1) / 2**20, 1), "loss": L}
         del s
     h = 1e-4
     dv = np.tile([1.0, 0.5, -0.3], (p["v0"].shape[0], 1)) + 0.1 * problems.normal(41, p["v0"].size).reshape(-1, 3)
     dp = 1.0 + 0.3 * problems.normal(42, p["logE"].size)
-    fd_v = (forward(dict(p, v0=p["v0"] + h * dv))[3] - forward(dict(p, v0=p["v0"] - h * dv))[3]) / (2 * h)
-    fd_p = []
-    for sgn in (1.0, -1.0):
-        mu, lam = problems.lame(np.exp(p["logE"] + sgn * h * dp), 0.3)
-        fd_p.append(forward(dict(p, mu=mu, lam=lam))[3])
-    fd_p = (fd_p[0] - fd_p[1]) / (2 * h)
+
+    def fd_v(hh):
+        return (forward(dict(p, v0=p["v0"] + hh * dv))[3] - forward(dict(p, v0=p["v0"] - hh * dv))[3]) / (2 * hh)
+
+    def fd_p(hh):
+        vals = []
+        for sgn in (1.0, -1.0):
+            mu, lam = problems.lame(np.exp(p["logE"] + sgn * hh * dp), 0.3)
+            vals.append(forward(dict(p, mu=mu, lam=lam))[3])
+        return (vals[0] - vals[1]) / (2 * hh)
+
+    # central differences at h and h/2; Richardson's (4 f(h/2) - f(h)) / 3 removes their O(h^2)
+    # truncation error
+    fv = [fd_v(h), fd_v(h / 2)]
+    fp = [fd_p(h), fd_p(h / 2)]
+    rv, rp = (4 * fv[1] - fv[0]) / 3, (4 * fp[1] - fp[0]) / 3
     for precision in ("fp64", "mixed"):
         gv, gp = grads[precision]
-        out[precision]["rel_err_dv0_direction"] = float(abs(gv @ dv.ravel() - fd_v) / abs(fd_v))
-        out[precision]["rel_err_dlnE_direction"] = float(abs(gp @ dp - fd_p) / abs(fd_p))
-    out["central_differences"] = {"h": h, "d_v0": fd_v, "d_lnE": fd_p}
+        out[precision]["rel_err_dv0_direction"] = float(abs(gv @ dv.ravel() - fv[0]) / abs(fv[0]))
+        out[precision]["rel_err_dlnE_direction"] = float(abs(gp @ dp - fp[0]) / abs(fp[0]))
+        out[precision]["rel_err_dv0_direction_richardson"] = float(abs(gv @ dv.ravel() - rv) / abs(rv))
+        out[precision]["rel_err_dlnE_direction_richardson"] = float(abs(gp @ dp - rp) / abs(rp))
+    out["central_differences"] = {"h": [h, h / 2], "d_v0": fv, "d_lnE": fp, "d_v0_richardson": rv,
+                                  "d_lnE_richardson": rp}
     return out
 
 

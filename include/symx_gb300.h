@@ -190,6 +190,12 @@ int symxg_generate_cuboid_mesh(int32_t element_type, const double size[3], const
 /* Number of CUDA kernels this library has launched since it was loaded (all handles). */
 int64_t symxg_launch_count(void);
 
+/* Device memory held by this library's own buffers (solver handles, Compiled<T> batches,
+ * stand-alone PCG workspaces; not the CUDA context, the loaded kernel images or the driver's
+ * local-memory reservation), and its high-water mark since the last reset (reset_peak != 0
+ * sets it to the current value after reading it).  Either pointer may be NULL. */
+void symxg_device_memory(int64_t* current, int64_t* peak, int32_t reset_peak);
+
 /* Bound on the waits inside the staged PCG kernels (no counterpart in the reference, whose
  * CPU solver never waits on another processor).  Every wait of those kernels on a
  * shared-memory stage or on the other blocks of the launch polls at most this many times;

@@ -30,6 +30,7 @@ EXPORTS = [
     "symxg_bcsr_pcg_f32", "symxg_bcsr_pcg_f64", "symxg_bcsr_pcg_f32_noalloc", "symxg_adjoint",
     "symxg_generate_cuboid_mesh",
     "symxg_rollout_forward", "symxg_rollout_backward", "symxg_set_wait_poll_limit", "symxg_wait_poll_limit",
+    "symxg_device_memory",
 ]
 
 
@@ -136,6 +137,7 @@ def load(path: str | None = None):
         "symxg_launch_count": ([], C.c_int64),
         "symxg_set_wait_poll_limit": ([C.c_int64], None),
         "symxg_wait_poll_limit": ([], C.c_int64),
+        "symxg_device_memory": ([C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int32], None),
         "symxg_default_settings": ([C.POINTER(NewtonSettings)], None),
         "symxg_elastic_create": ([C.POINTER(ElasticProblem), C.c_char_p, C.POINTER(P)], C.c_int),
         "symxg_destroy": ([P], C.c_int),

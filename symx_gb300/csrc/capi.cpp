@@ -124,11 +124,19 @@ static int pcg_impl(int32_t nb, const int32_t* rp, const int32_t* cols, const T*
         if (nb > 0) {
             const cudaError_t e = cudaMalloc(&ws, bytes);
             if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            symxg::note_device_alloc((int64_t)bytes);
         }
         struct Free {
             void* p;
-            ~Free() { if (p) cudaFree(p); }
-        } guard{ws};
+            size_t bytes;
+            ~Free()
+            {
+                if (p) {
+                    cudaFree(p);
+                    symxg::note_device_free((int64_t)bytes);
+                }
+            }
+        } guard{ws, bytes};
         const symxg::BcsrPcgResult r = symxg::run_bcsr_pcg<T>(nb, rp, cols, vals, vs, b, x, abs_tol, rel_tol, max_it, ws,
                                                                bytes, parts, (cudaStream_t)stream);
         info->converged = r.converged;
@@ -237,6 +245,12 @@ const char* symxg_last_error(void) { return g_last_error.c_str(); }
 int symxg_abi_version(void) { return SYMXG_ABI_VERSION; }
 int64_t symxg_launch_count(void) { return symxg::launch_count(); }
 void symxg_set_wait_poll_limit(int64_t polls) { symxg::set_wait_poll_limit((long long)polls); }
+void symxg_device_memory(int64_t* current, int64_t* peak, int32_t reset_peak)
+{
+    if (current) *current = symxg::device_bytes_current();
+    const int64_t p = symxg::device_bytes_peak(reset_peak != 0);
+    if (peak) *peak = p;
+}
 int64_t symxg_wait_poll_limit(void) { return (int64_t)symxg::wait_poll_limit(); }
 
 void symxg_default_settings(symxg_newton_settings* s)

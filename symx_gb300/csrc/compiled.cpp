@@ -2,6 +2,7 @@
 // run flow (symx/src/compile/Compilation.cpp:59-226, Compiled.cpp:1-200) with NVRTC and a
 // CUBIN in place of the system compiler and a shared object.
 #include "compiled.h"
+#include "kernels.cuh"
 
 #include <chrono>
 #include <cmath>
@@ -270,8 +271,14 @@ template <typename FLOAT>
 Compiled<FLOAT>::~Compiled()
 {
     // errors are ignored here: the context may already be gone at process exit
-    if (d_in_) cudaFree(d_in_);
-    if (d_out_) cudaFree(d_out_);
+    if (d_in_) {
+        cudaFree(d_in_);
+        symxg::note_device_free((int64_t)sizeof(FLOAT) * d_capacity_in_);
+    }
+    if (d_out_) {
+        cudaFree(d_out_);
+        symxg::note_device_free((int64_t)sizeof(FLOAT) * d_capacity_out_);
+    }
 }
 
 template <typename FLOAT>
@@ -324,17 +331,25 @@ void Compiled<FLOAT>::resize_buffers()
     if (!is_valid()) return;
     const int64_t need_in = (int64_t)n_threads_ * std::max(n_in, 1), need_out = (int64_t)n_threads_ * std::max(n_out, 1);
     if (need_in > d_capacity_in_) {
-        if (d_in_) cudaFree(d_in_);
+        if (d_in_) {
+            cudaFree(d_in_);
+            symxg::note_device_free((int64_t)sizeof(FLOAT) * d_capacity_in_);
+        }
         d_in_ = nullptr;
         d_capacity_in_ = 0;
         check_cuda(cudaMalloc(&d_in_, sizeof(FLOAT) * need_in), "cudaMalloc of Compiled inputs");
+        symxg::note_device_alloc((int64_t)sizeof(FLOAT) * need_in);
         d_capacity_in_ = need_in;
     }
     if (need_out > d_capacity_out_) {
-        if (d_out_) cudaFree(d_out_);
+        if (d_out_) {
+            cudaFree(d_out_);
+            symxg::note_device_free((int64_t)sizeof(FLOAT) * d_capacity_out_);
+        }
         d_out_ = nullptr;
         d_capacity_out_ = 0;
         check_cuda(cudaMalloc(&d_out_, sizeof(FLOAT) * need_out), "cudaMalloc of Compiled outputs");
+        symxg::note_device_alloc((int64_t)sizeof(FLOAT) * need_out);
         d_capacity_out_ = need_out;
     }
 }

@@ -2304,6 +2304,22 @@ std::atomic<long long> g_wait_polls{kDefaultWaitPolls};
 void set_wait_poll_limit(long long polls) { g_wait_polls.store(polls < 0 ? kDefaultWaitPolls : polls); }
 long long wait_poll_limit() { return g_wait_polls.load(); }
 void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+std::atomic<int64_t> g_dev_bytes{0}, g_dev_peak{0};
+void note_device_alloc(int64_t bytes)
+{
+    const int64_t now = g_dev_bytes.fetch_add(bytes) + bytes;
+    int64_t peak = g_dev_peak.load();
+    while (now > peak && !g_dev_peak.compare_exchange_weak(peak, now)) {
+    }
+}
+void note_device_free(int64_t bytes) { g_dev_bytes.fetch_sub(bytes); }
+int64_t device_bytes_current() { return g_dev_bytes.load(); }
+int64_t device_bytes_peak(bool reset)
+{
+    const int64_t p = g_dev_peak.load();
+    if (reset) g_dev_peak.store(g_dev_bytes.load());
+    return p;
+}
 
 void launch_sum(const double* x, int64_t n, double* partials, unsigned* ticket, double* out, cudaStream_t s)
 {

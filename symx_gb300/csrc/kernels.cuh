@@ -11,6 +11,13 @@ namespace symxg {
 int64_t launch_count();
 void count_launch(int64_t n = 1);
 
+// Device memory held by this library's own buffers (every cudaMalloc it makes for a solver,
+// a Compiled<T> or a stand-alone PCG workspace), and its high-water mark since the last reset.
+void note_device_alloc(int64_t bytes);
+void note_device_free(int64_t bytes);
+int64_t device_bytes_current();
+int64_t device_bytes_peak(bool reset);
+
 // Polls after which a bounded wait of the staged PCG kernels (a shared-memory stage's
 // mbarrier, the persistent kernel's grid barrier) gives up and flags the solve
 // (PcgState::wait_failed).  Process-wide, read at each launch; the default is

@@ -47,12 +47,18 @@ struct DevBuf {
     {
         if (count == n && p) return;
         release();
-        if (count) ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        if (count) {
+            ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+            symxg::note_device_alloc((int64_t)(count * sizeof(T)));
+        }
         n = count;
     }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaFree(p);
+            symxg::note_device_free((int64_t)(n * sizeof(T)));
+        }
         p = nullptr;
         n = 0;
     }
