@@ -181,7 +181,7 @@ def run_ours(args):
 
     def device_solve(precision, **kw):
         solver.set_settings(precision=precision, **{"projection_fp64_refinement": 0, "cg_residual_replacement": 0,
-                                                    "cg_fp64_partial_sums": 1, **kw})
+                                                    "cg_fp64_partial_sums": 0, **kw})
         solver.set_state(p["x_init"], p["x0"], p["v0"])
         solver.upload()
         torch.cuda.synchronize()
@@ -221,13 +221,14 @@ def run_ours(args):
     solver.download()
     x_fp64 = solver.get_positions()
 
-    # the split that keeps the projection's arithmetic and the PCG's residual in FP64: FP32
-    # Jacobi refined by one FP64 step (12 x 12 element Hessians), FP64 residual replacement
-    # every 50 PCG iterations; and the FP64 form with the same refined projection
-    variants = {"mixed_fp64_projection_and_residual": ("mixed", dict(projection_fp64_refinement=1,
-                                                                     cg_residual_replacement=50)),
-                "fp64_refined_projection": ("fp64", dict(projection_fp64_refinement=1)),
-                "mixed_float_float_partial_sums": ("mixed", dict(cg_fp64_partial_sums=0))}
+    # the split that keeps the projection's arithmetic, the PCG's residual and its dot-product
+    # accumulation in FP64: FP32 Jacobi refined by one FP64 step (12 x 12 element Hessians),
+    # FP64 residual replacement every 50 PCG iterations, FP64 sums of the dot partials; and the
+    # FP64 form with the same refined projection
+    variants = {"mixed_fp64_projection_residual_and_sums": ("mixed", dict(projection_fp64_refinement=1,
+                                                                          cg_residual_replacement=50,
+                                                                          cg_fp64_partial_sums=1)),
+                "fp64_refined_projection": ("fp64", dict(projection_fp64_refinement=1))}
     variant_out, variant_x = {}, {}
     for name, (prec, kw) in variants.items():
         if args.no_variants:

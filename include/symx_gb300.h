@@ -104,8 +104,8 @@ typedef struct symxg_newton_settings {
                                            refinement step, FP64 clamping correction), either precision */
     int32_t cg_residual_replacement; /* Mixed: every k PCG iterations replace the residual by b - A x
                                         accumulated in FP64 (0: never) */
-    int32_t cg_fp64_partial_sums;    /* Mixed: dot-product partials of the PCG summed in FP64 (1, default)
-                                        or float-float (0) */
+    int32_t cg_fp64_partial_sums;    /* Mixed: dot-product partials of the PCG summed in FP64 (1) or
+                                        float-float (0, default; faster) */
     int32_t pad;
 } symxg_newton_settings;
 

@@ -255,209 +255,6 @@ __global__ void __launch_bounds__(64) k_project_pd_refined_listed(S* __restrict_
     if (nc) *not_converged = 1;
 }
 
-// The same projection for translation-invariant matrices, with the FP64 matrix Q^T H Q and
-// the FP32 eigenvectors kept in shared memory (one column of kRefThreads entries per matrix
-// entry, so a warp's accesses are conflict-free) instead of spilled thread-local arrays: the
-// FP32 Jacobi runs in registers, then the refinement (Ogita-Aishima step, as
-// symxg_dev::refine_clamp_correction) makes one pass for lambda' and delta without storing
-// S or R, and a second pass per clamped eigenvalue that recomputes its column of S and R.
-constexpr int kRefThreads = 64;
-template <int M>
-struct RefinedSmem {
-    static constexpr int MT = M * (M + 1) / 2;
-    // A (FP64), dW (FP64), X (FP32), one column of kRefThreads entries per matrix entry
-    static constexpr size_t bytes =
-        2 * (size_t)MT * kRefThreads * sizeof(double) + (size_t)M * M * kRefThreads * sizeof(float);
-};
-
-// Helmert basis scale 1/sqrt(m (m + 1)) for m = 0..9 (entry 0 unused), read with runtime m.
-__constant__ double kHelmertScale[10] = {0.0,
-                                         0.70710678118654752440,
-                                         0.40824829046386301637,
-                                         0.28867513459481288225,
-                                         0.22360679774997896964,
-                                         0.18257418583505537115,
-                                         0.15430334996209191026,
-                                         0.13363062095621219234,
-                                         0.11785113019775792073,
-                                         0.10540925533894597774};
-
-template <typename S, int N>
-__global__ void __launch_bounds__(kRefThreads, 3) k_project_pd_refined_deflated(S* __restrict__ H, const int64_t* __restrict__ list,
-                                                                                 const unsigned long long* n_list, double eps,
-                                                                                 int mirroring, int* not_converged)
-{
-    using namespace symxg_dev;
-    constexpr int NB = N / 3, M = N - 3, MT = M * (M + 1) / 2;
-    static_assert(NB <= 10, "Helmert scale table");
-    extern __shared__ __align__(16) unsigned char ref_smem[];
-    double* sA = reinterpret_cast<double*>(ref_smem) + threadIdx.x;  // column-per-entry layout
-    double* sW = reinterpret_cast<double*>(ref_smem) + (size_t)MT * kRefThreads + threadIdx.x;
-    float* sX = reinterpret_cast<float*>(ref_smem + 2 * (size_t)MT * kRefThreads * sizeof(double)) + threadIdx.x;
-    // volatile: every use is a shared-memory load, so the compiler does not hoist the 45 + 81
-    // entries into registers across the passes (they would spill)
-    volatile double* vA = sA;
-    volatile double* vW = sW;
-    volatile float* vX = sX;
-    auto A = [&](int i, int j) -> volatile double& { return vA[tri<M>(i, j) * kRefThreads]; };
-    auto W = [&](int i, int j) -> volatile double& { return vW[tri<M>(i, j) * kRefThreads]; };
-    auto X = [&](int r, int c) -> volatile float& { return vX[(r * M + c) * kRefThreads]; };
-    const int64_t n = (int64_t)*n_list;
-    int nc = 0;
-    for (int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; item < n; item += (int64_t)gridDim.x * blockDim.x) {
-        S* __restrict__ h = H + list[item] * (N * N);
-        // b = Q^T H Q in FP64, one column q = (l, e) at a time: t = column q of H Q, then the
-        // Helmert combination of t's node blocks (prefix sums: B[i][m] = c_m for i < m, -m c_m for i = m)
-#pragma unroll 1
-        for (int q = 0; q < M; ++q) {
-            const int l = q / 3 + 1, e = q % 3;
-            const double cl = kHelmertScale[l];
-            double t[N];
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                const int ib = (i / 3) * NB, ir = (i % 3) * 3;  // block row of i, row inside the block
-                double s = 0.0;
-                for (int j = 0; j < l; ++j) s += (double)h[(ib + j) * 9 + ir + e];
-                t[i] = cl * (s - (double)l * (double)h[(ib + l) * 9 + ir + e]);
-            }
-#pragma unroll
-            for (int m = 1; m < NB; ++m)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const int p = 3 * (m - 1) + d;
-                    if (p > q) continue;
-                    double s = 0.0;
-#pragma unroll
-                    for (int i = 0; i < m; ++i) s += t[3 * i + d];
-                    A(p, q) = kHelmertScale[m] * (s - (double)m * t[3 * m + d]);
-                }
-        }
-        {
-            float a32[MT], v[M * M];
-#pragma unroll
-            for (int p = 0; p < M; ++p)
-#pragma unroll
-                for (int q = p; q < M; ++q) a32[tri<M>(p, q)] = (float)A(p, q);
-#pragma unroll
-            for (int i = 0; i < M; ++i)
-#pragma unroll
-                for (int j = 0; j < M; ++j) v[i * M + j] = (i == j) ? 1.0f : 0.0f;
-            if (!jacobi_eigen<float, M>(a32, v)) nc = 1;
-#pragma unroll
-            for (int i = 0; i < M * M; ++i) sX[i * kRefThreads] = v[i];
-        }
-        // pass 1: lambda'_j = s_jj / (1 - r_jj) and the norms of S - diag(lambda'), A and R
-        double lam[M], nsd = 0.0, nr = 0.0, na = 0.0;
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-#pragma unroll
-            for (int j = i; j < M; ++j) na = fma((i == j ? 1.0 : 2.0) * A(i, j), A(i, j), na);
-#pragma unroll 1
-        for (int j = 0; j < M; ++j) {
-            double y[M];
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                double tt = 0.0;
-#pragma unroll
-                for (int k2 = 0; k2 < M; ++k2) tt = fma(A(i, k2), (double)X(k2, j), tt);
-                y[i] = tt;
-            }
-            double sjj = 0.0, rjj = 0.0;
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                double s = 0.0, r = 0.0;
-#pragma unroll
-                for (int k2 = 0; k2 < M; ++k2) {
-                    const double xk = (double)X(k2, i);
-                    s = fma(xk, y[k2], s);
-                    r = fma(xk, (double)X(k2, j), r);
-                }
-                if (i == j) {
-                    sjj = s;
-                    rjj = 1.0 - r;
-                } else {
-                    nsd = fma(s, s, nsd);
-                    nr = fma(r, r, nr);
-                }
-            }
-            lam[j] = sjj / (1.0 - rjj);
-            nsd = fma(sjj - lam[j], sjj - lam[j], nsd);
-            nr = fma(rjj, rjj, nr);
-        }
-        const double delta = 2.0 * (sqrt(nsd) + sqrt(na) * sqrt(nr));
-        // pass 2: for each clamped eigenvalue, column k of S and R, x'_k, and the correction dW
-#pragma unroll
-        for (int k2 = 0; k2 < MT; ++k2) sW[k2 * kRefThreads] = 0.0;
-#pragma unroll 1
-        for (int k = 0; k < M; ++k) {
-            const double l = lam[k];
-            if (!(l < eps)) continue;
-            const double cc = (mirroring ? -l : eps) - l;
-            double y[M], x[M];
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                double tt = 0.0;
-#pragma unroll
-                for (int k2 = 0; k2 < M; ++k2) tt = fma(A(i, k2), (double)X(k2, k), tt);
-                y[i] = tt;
-                x[i] = (double)X(i, k);
-            }
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                double s = 0.0, r = 0.0;
-#pragma unroll
-                for (int k2 = 0; k2 < M; ++k2) {
-                    const double xk = (double)X(k2, i);
-                    s = fma(xk, y[k2], s);
-                    r = fma(xk, (double)X(k2, k), r);
-                }
-                r = (i == k ? 1.0 : 0.0) - r;
-                const double ei = (i == k) ? 0.5 * r
-                                           : (fabs(lam[i] - l) > delta ? (s + l * r) / (l - lam[i]) : 0.5 * r);
-#pragma unroll
-                for (int qq = 0; qq < M; ++qq) x[qq] = fma((double)X(qq, i), ei, x[qq]);
-            }
-#pragma unroll
-            for (int p = 0; p < M; ++p)
-#pragma unroll
-                for (int qq = p; qq < M; ++qq) W(p, qq) = fma(cc * x[p], x[qq], W(p, qq));
-        }
-        // H + Q dW Q^T + lam_t / NB (1 1^T (x) I3), the translation eigenvalues 0 -> eps; one
-        // column j = (jn, e) of H at a time: u = column (jn, e) of dW Q^T, then H(:, j) += Q u
-        const double diag_t = (mirroring ? 0.0 : eps) / (double)NB;
-#pragma unroll 1
-        for (int j = 0; j < N; ++j) {
-            const int jn = j / 3, e = j % 3;
-            double u[M];
-#pragma unroll
-            for (int p = 0; p < M; ++p) {
-                double s = 0.0;
-                for (int l = jn > 0 ? jn : 1; l < NB; ++l)  // B[jn][l] = c_l (l > jn), -jn c_jn (l = jn)
-                    s = fma(l == jn ? -(double)jn * kHelmertScale[l] : kHelmertScale[l], W(p, 3 * (l - 1) + e), s);
-                u[p] = s;
-            }
-            // rows i <= j only, each result stored at (i, j) and (j, i): the result stays exactly
-            // symmetric (the input is)
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                if (i > j) continue;
-                const int in = i / 3, d = i % 3;
-                double s = (d == e) ? diag_t : 0.0;
-#pragma unroll
-                for (int m = 1; m < NB; ++m) {
-                    if (m < in) continue;
-                    s = fma(m == in ? -(double)in * kHelmertScale[m] : kHelmertScale[m], u[3 * (m - 1) + d], s);
-                }
-                const int ij = (in * NB + jn) * 9 + d * 3 + e, ji = (jn * NB + in) * 9 + e * 3 + d;
-                const S out = (S)((double)h[ij] + s);
-                h[ij] = out;
-                h[ji] = out;
-            }
-        }
-    }
-    if (nc) *not_converged = 1;
-}
-
 // Progressive projection (NewtonsMethod.cpp:305-329): flag the element gradient blocks of
 // every DoF block whose gradient max-abs is at least thr (gflag zeroed before); counts the
 // other blocks in *n_inactive.
@@ -2617,33 +2414,10 @@ void launch_project_pd_refined12(T* H, int64_t count, double eps, bool mirroring
     k_project_pd_sort<T, 12><<<blocks_for(count, 128), 128, 0, s>>>(H, count, scratch.fallback, scratch.n_fallback, sel,
                                                                    scratch.pending, scratch.n_pending);
     check_launch("project_pd_sort");
-    {
-        constexpr size_t smem = RefinedSmem<9>::bytes;
-        static std::mutex m;
-        static std::map<int, unsigned> grids;  // per device: resident blocks (attribute set once)
-        int dev = 0;
-        cudaGetDevice(&dev);
-        unsigned grid = 0;
-        {
-            std::lock_guard<std::mutex> lock(m);
-            auto it = grids.find(dev);
-            if (it == grids.end()) {
-                const cudaError_t e = cudaFuncSetAttribute(k_project_pd_refined_deflated<T, 12>,
-                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (e != cudaSuccess)
-                    throw std::runtime_error(std::string("symx_gb300: projection shared memory: ") + cudaGetErrorString(e));
-                int sms = 0, per_sm = 0;
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project_pd_refined_deflated<T, 12>, kRefThreads,
-                                                              smem);
-                it = grids.emplace(dev, (unsigned)std::max(1, sms * std::max(1, per_sm))).first;
-            }
-            grid = it->second;
-        }
-        k_project_pd_refined_deflated<T, 12><<<grid, kRefThreads, smem, s>>>(H, scratch.pending, scratch.n_pending, eps,
-                                                                            mirroring, not_converged);
-        check_launch("project_pd_refined_deflated");
-    }
+    const unsigned pending_grid = resident_grid(k_project_pd_refined_listed<T, 12, true>, 64);
+    k_project_pd_refined_listed<T, 12, true><<<pending_grid, 64, 0, s>>>(H, scratch.pending, scratch.n_pending, eps,
+                                                                         mirroring, not_converged);
+    check_launch("project_pd_refined_listed");
     const unsigned fallback_grid = resident_grid(k_project_pd_refined_listed<T, 12, false>, 64);
     k_project_pd_refined_listed<T, 12, false><<<fallback_grid, 64, 0, s>>>(H, scratch.fallback, scratch.n_fallback, eps,
                                                                            mirroring, not_converged);

@@ -79,9 +79,11 @@ struct NewtonSettings {
     // is made on it (0: never; the FP64 PCG never replaces).
     int cg_residual_replacement = 0;
     // One-launch FP32 PCG (Mixed): the chunk and block partials of its dot products (p.Ap,
-    // r.r, r.z) are accumulated in FP64 in a fixed order; false: in float-float.  Products
-    // and the per-thread and per-warp sums are float-float (exact products) in both.
-    bool cg_fp64_partial_sums = true;
+    // r.r, r.z) are accumulated in FP64 in a fixed order; false (default): in float-float.
+    // Products and the per-thread and per-warp sums are float-float (exact products) in both.
+    // Every block forms the sums itself, so FP64 costs FP64-pipe time in every block
+    // (GB300's FP64 rate is 1/64 of FP32): about 8 us per iteration on the 64^3 Tet4 step.
+    bool cg_fp64_partial_sums = false;
 };
 
 struct Context {

@@ -97,9 +97,9 @@ def test_newton_fp64_refined_projection_matches_reference(sg, golden, case):
 
 @pytest.mark.parametrize("case", ["tet4_6p", "tet4_10"])
 def test_newton_mixed_fp64_split_matches_reference(sg, golden, case):
-    """Mixed precision with the FP64-accurate projection and an FP64 residual replacement
-    every 10 PCG iterations."""
-    p, s = make(sg, case, "mixed", projection_fp64_refinement=1, cg_residual_replacement=10)
+    """Mixed precision with the FP64-accurate projection, an FP64 residual replacement every 10
+    PCG iterations and FP64 sums of the PCG's dot-product partials."""
+    p, s = make(sg, case, "mixed", projection_fp64_refinement=1, cg_residual_replacement=10, cg_fp64_partial_sums=1)
     st = s.solve()
     sol = golden(f"{case}_solve")
     assert st["solver_return"] == 0 and st["final_residual"] < 1e-6
@@ -108,6 +108,15 @@ def test_newton_mixed_fp64_split_matches_reference(sg, golden, case):
     assert abs(st["cg_iterations"] - int(sol["cg_iterations_full"])) <= 2 + 0.05 * int(sol["cg_iterations_full"])
     x, xr = s.get_positions(), sol["x_full"]
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr - p["x0"]) < 1e-6
+
+
+def test_fp64_partial_sums_are_deterministic(sg):
+    p, s = make(sg, "tet4_10", "mixed", cg_fp64_partial_sums=1)
+    st1 = s.solve()
+    x1 = s.get_positions()
+    s.set_state(p["x_init"], p["x0"], p["v0"])
+    st2 = s.solve()
+    assert st1["cg_iterations"] == st2["cg_iterations"] and np.array_equal(x1, s.get_positions())
 
 
 def test_residual_replacement_keeps_the_iteration(sg):
