@@ -411,6 +411,8 @@ def run_profile(args):
     p = problems.step_problem(args.config)
     solver = sg.ElasticSolver(p)
     solver.set_settings(cg_rel_tolerance=1e-3, precision=args.profile_solve)
+    if args.profile_split:  # FP64-accurate projection, FP64 residual replacement and partial sums
+        solver.set_settings(projection_fp64_refinement=1, cg_residual_replacement=50, cg_fp64_partial_sums=1)
     out = None
     for i in range(2):
         solver.set_state(p["x_init"], p["x0"], p["v0"])
@@ -662,6 +664,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP64-projection / residual-replacement runs")
     ap.add_argument("--profile-solve", choices=["mixed", "fp64"], default=None)
+    ap.add_argument("--profile-split", action="store_true",
+                    help="with --profile-solve: the FP64 projection / residual / partial-sum settings")
     ap.add_argument("--measure", choices=["adjoint", "rollout"], default=None,
                     help="instead of the bench line: the adjoint (quasistatic) or rollout measurement")
     ap.add_argument("--rollout-steps", type=int, default=50)
