@@ -1377,7 +1377,7 @@ __device__ __forceinline__ void staged_drain(const PcgBuffers<float>& B, const S
 // and stores the chunk's float-float sum at part[chunk], and after the barrier every block
 // adds part[0 .. n_chunks) in one fixed order.  None of it depends on which block took which
 // chunk.
-constexpr int kClaimChunks = 2;
+constexpr int kClaimChunks = 1;
 struct DynProducer {
     int it = 0;         // pass of the next stage to issue
     int c = -1;         // its chunk, or -1: the end marker of pass `it`
