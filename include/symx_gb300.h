@@ -106,7 +106,8 @@ typedef struct symxg_newton_settings {
                                         accumulated in FP64 (0: never) */
     int32_t cg_fp64_partial_sums;    /* Mixed: dot-product partials of the PCG summed in FP64 (1) or
                                         float-float (0, default; faster) */
-    int32_t pad;
+    int32_t cg_lookahead;            /* Mixed: 1: the one-launch PCG with one grid barrier per
+                                        iteration (update folded into the next product pass); 0 (default): two */
 } symxg_newton_settings;
 
 typedef struct symxg_solve_stats {

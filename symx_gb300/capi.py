@@ -57,7 +57,7 @@ class NewtonSettings(C.Structure):
         ("bailout_residual", C.c_double), ("precision", C.c_int32), ("time_kernels", C.c_int32),
         ("project_on_demand_countdown", C.c_int32), ("ppn_tightening_factor", C.c_double),
         ("ppn_release_factor", C.c_double), ("projection_fp64_refinement", C.c_int32),
-        ("cg_residual_replacement", C.c_int32), ("cg_fp64_partial_sums", C.c_int32), ("pad", C.c_int32),
+        ("cg_residual_replacement", C.c_int32), ("cg_fp64_partial_sums", C.c_int32), ("cg_lookahead", C.c_int32),
     ]
 
 

@@ -281,7 +281,7 @@ void symxg_default_settings(symxg_newton_settings* s)
     s->projection_fp64_refinement = d.projection_fp64_refinement ? 1 : 0;
     s->cg_residual_replacement = d.cg_residual_replacement;
     s->cg_fp64_partial_sums = d.cg_fp64_partial_sums ? 1 : 0;
-    s->pad = 0;
+    s->cg_lookahead = d.cg_lookahead ? 1 : 0;
 }
 
 int symxg_elastic_create(const symxg_elastic_problem* p, const char* cache_dir, symxg_solver** out)
@@ -434,6 +434,7 @@ int symxg_set_settings(symxg_solver* s, const symxg_newton_settings* c)
         t.projection_fp64_refinement = c->projection_fp64_refinement != 0;
         t.cg_residual_replacement = c->cg_residual_replacement;
         t.cg_fp64_partial_sums = c->cg_fp64_partial_sums != 0;
+        t.cg_lookahead = c->cg_lookahead != 0;
         return SYMXG_OK;
     });
 }

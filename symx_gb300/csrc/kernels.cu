@@ -1419,6 +1419,85 @@ __device__ __forceinline__ void publish_chunk_f64(double* partials, int c, float
     partials[c] = (double)hi + (double)lo;
 }
 
+// Producer thread of a dynamically scheduled pass li (see above): claims chunks, copies each
+// into the next free ring slot and publishes its chunk index (-1: the pass's end marker).
+__device__ __forceinline__ void dyn_produce(const PcgBuffers<float>& B, const StagedShared& ss, int li, unsigned* ctr,
+                                            int n_chunks, unsigned& issued, DynProducer& P, volatile int* abort_flag)
+{
+    const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
+    const size_t stage_bytes = staged_stage_bytes(CAP, S);
+    const uint64_t pol = l2_evict_first_policy();
+    while (!*abort_flag) {
+        // once the end marker of pass li is out (in this pass or, running ahead, in the
+        // previous one), stop when every ring slot that pass li's consumers free is taken
+        if (P.end_it >= li) {
+            const unsigned e = P.end_it == li ? P.end_g : P.end_g_prev;
+            if (issued > e + (unsigned)NS) break;
+        }
+        if (!P.have) {  // nothing claimed ahead (launch start, or after a stop)
+            if (P.it > li + 1) break;
+            dyn_take(B, n_chunks, P.it, atomicAdd(&ctr[P.it % 3], (unsigned)kClaimChunks), P);
+        }
+        // claim the unit after this one now: its round trip overlaps the slot waits
+        if (!P.pending && (P.c < 0 || P.c == P.unit0)) {
+            const int nit = P.c < 0 ? P.it + 1 : P.it;
+            if (nit <= li + 1) {
+                P.next_it = nit;
+                P.next_v = atomicAdd(&ctr[nit % 3], (unsigned)kClaimChunks);
+                P.pending = true;
+            }
+        }
+        const unsigned g = issued, s = g % NS, use = g / NS;
+        if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1, B.staged.max_polls)) {
+            *abort_flag = 1;
+            break;
+        }
+        ss.chunk[s] = P.c;  // published to the consumers by the arrive's release
+        const uint32_t fb = smem_addr(&ss.full[s]);
+        if (P.c >= 0) {
+            const int r0 = P.c * S, j = P.c - P.unit0;
+            int kb = P.rp[0], ke = P.rp[1];  // constant indices only: P stays in registers
+#pragma unroll
+            for (int k = 1; k < kClaimChunks; ++k)
+                if (j == k) {
+                    kb = P.rp[k];
+                    ke = P.rp[k + 1];
+                }
+            const int kb4 = kb & ~3, ke4 = (ke + 3) & ~3;
+            const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
+            unsigned char* st = ss.stage0 + s * stage_bytes;
+            mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
+            if (span) {
+                for (int m = 0; m < 9; ++m)
+                    bulk_copy_g2s_stream(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4,
+                                         span, fb, pol);
+                bulk_copy_g2s_stream(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb,
+                                     pol);
+            }
+            bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0,
+                          (uint32_t)(S + 4) * 4u, fb);
+        } else {
+            mbar_arrive(fb);
+        }
+        issued = g + 1;
+        if (P.c < 0) {
+            P.end_it = P.it;
+            P.end_g_prev = P.end_g;
+            P.end_g = g;
+        }
+        // next stage: the unit's next chunk, else the claimed unit, else claim at the top
+        if (P.c >= 0 && P.c + 1 < P.unit_end) {
+            P.c += 1;
+        } else if (P.pending) {
+            P.pending = false;
+            dyn_take(B, n_chunks, P.next_it, P.next_v, P);
+        } else {
+            P.it = P.c < 0 ? P.it + 1 : P.it;
+            P.have = false;
+        }
+    }
+}
+
 template <bool kF64Sums>
 __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B, const StagedShared& ss, int li,
                                                      unsigned* ctr, int n_chunks, const float* __restrict__ p_old,
@@ -1429,78 +1508,7 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
     const size_t stage_bytes = staged_stage_bytes(CAP, S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
-        if (lane == 0) {
-            const uint64_t pol = l2_evict_first_policy();
-            while (!*abort_flag) {
-                // once the end marker of pass li is out (in this pass or, running ahead, in the
-                // previous one), stop when every ring slot that pass li's consumers free is taken
-                if (P.end_it >= li) {
-                    const unsigned e = P.end_it == li ? P.end_g : P.end_g_prev;
-                    if (issued > e + (unsigned)NS) break;
-                }
-                if (!P.have) {  // nothing claimed ahead (launch start, or after a stop)
-                    if (P.it > li + 1) break;
-                    dyn_take(B, n_chunks, P.it, atomicAdd(&ctr[P.it % 3], (unsigned)kClaimChunks), P);
-                }
-                // claim the unit after this one now: its round trip overlaps the slot waits
-                if (!P.pending && (P.c < 0 || P.c == P.unit0)) {
-                    const int nit = P.c < 0 ? P.it + 1 : P.it;
-                    if (nit <= li + 1) {
-                        P.next_it = nit;
-                        P.next_v = atomicAdd(&ctr[nit % 3], (unsigned)kClaimChunks);
-                        P.pending = true;
-                    }
-                }
-                const unsigned g = issued, s = g % NS, use = g / NS;
-                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1, B.staged.max_polls)) {
-                    *abort_flag = 1;
-                    break;
-                }
-                ss.chunk[s] = P.c;  // published to the consumers by the arrive's release
-                const uint32_t fb = smem_addr(&ss.full[s]);
-                if (P.c >= 0) {
-                    const int r0 = P.c * S, j = P.c - P.unit0;
-                    int kb = P.rp[0], ke = P.rp[1];  // constant indices only: P stays in registers
-#pragma unroll
-                    for (int k = 1; k < kClaimChunks; ++k)
-                        if (j == k) {
-                            kb = P.rp[k];
-                            ke = P.rp[k + 1];
-                        }
-                    const int kb4 = kb & ~3, ke4 = (ke + 3) & ~3;
-                    const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
-                    unsigned char* st = ss.stage0 + s * stage_bytes;
-                    mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
-                    if (span) {
-                        for (int m = 0; m < 9; ++m)
-                            bulk_copy_g2s_stream(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4,
-                                                 span, fb, pol);
-                        bulk_copy_g2s_stream(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb,
-                                             pol);
-                    }
-                    bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0,
-                                  (uint32_t)(S + 4) * 4u, fb);
-                } else {
-                    mbar_arrive(fb);
-                }
-                issued = g + 1;
-                if (P.c < 0) {
-                    P.end_it = P.it;
-                    P.end_g_prev = P.end_g;
-                    P.end_g = g;
-                }
-                // next stage: the unit's next chunk, else the claimed unit, else claim at the top
-                if (P.c >= 0 && P.c + 1 < P.unit_end) {
-                    P.c += 1;
-                } else if (P.pending) {
-                    P.pending = false;
-                    dyn_take(B, n_chunks, P.next_it, P.next_v, P);
-                } else {
-                    P.it = P.c < 0 ? P.it + 1 : P.it;
-                    P.have = false;
-                }
-            }
-        }
+        if (lane == 0) dyn_produce(B, ss, li, ctr, n_chunks, issued, P, abort_flag);
     } else {
         const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
         const int la = 4 * cw + half, lb = la + 2;
@@ -2042,6 +2050,430 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
     }
 }
 
+// ---------------------------------------------------------------- look-ahead PCG
+// The same iteration as k_pcg_solve_staged (the reference's block-Jacobi PCG, solve_pcg.h:82-232),
+// reorganised so that one grid barrier per iteration suffices: the update of x, r and z is
+// folded into the next product pass, and the pass forms the product of the next z directly.
+// With w_k = A z_k, mw_k = M^-1 w_k, mq_k = M^-1 q_k, iteration k of the pass computes, per
+// block row (the owning lane of each component):
+//     p_{k-1} = z_{k-1} + beta_{k-1} p_{k-2}        q_{k-1} = w_{k-1} + beta_{k-1} q_{k-2}
+//     mq_{k-1} = mw_{k-1} + beta_{k-1} mq_{k-2}     x_k = x_{k-1} + alpha_{k-1} p_{k-1}
+//     r_k = r_{k-1} - alpha_{k-1} q_{k-1}           z_k = z_{k-1} - alpha_{k-1} mq_{k-1}
+//     w_k = A z_k                                   mw_k = M^-1 w_k
+// where each gathered column c of A z_k is formed from (z_{k-1}, mw_{k-1}, mq_{k-2}) of row c
+// by the same two fused multiply-adds as its owner uses (the same bits).  The pass leaves
+// per-chunk partials of r.r, r.z, z.w, z.q + p.w and p.q; after the barrier every block
+// sums them in one fixed order and forms beta_k = rz_k / rz_{k-1} and
+//     p_k.A p_k = z.w + beta_k (z.q + p.w) + beta_k^2 p.q       (p_k = z_k + beta_k p_{k-1})
+// without any orthogonality assumption, so the iterates are those of the two-barrier form up
+// to rounding (the same iteration counts on the Tet4 systems of this path).  The convergence
+// test on r_k runs after the pass that formed x_k; a converged solve has done one product more
+// than the two-barrier form.  The first pass of a launch (entry) gathers z as it is (after
+// k_pcg_init or a residual replacement), forms w and mw and, when earlier iterations exist,
+// mq = M^-1 q of the last direction.  The gathered vectors (z, mw, mq) alternate between two
+// sets by pass parity, the per-chunk partials between two halves, so no pass writes what
+// another block may still read from the previous one.
+constexpr int kLaSums = 5;  // r.r, r.z, z.w, z.q + p.w, p.q
+// Shared-memory layout of a look-ahead block: full and empty barriers (one per stage), the
+// consumer warps' partials of stages + 1 chunks in flight (a warp publishes a chunk after
+// releasing its stage, so the warps are at most `stages` chunks apart), the chunk index of each
+// ring slot, the per-slot count of warps that published, then the ring of stages.
+__host__ __device__ __forceinline__ size_t la_header_bytes(int stages)
+{
+    return ((size_t)16 * stages + (size_t)8 * kLaSums * kStagedConsumerWarps * (stages + 1) + 4 * (size_t)stages +
+            4 * (size_t)(stages + 1) + 127) / 128 * 128;
+}
+__device__ __forceinline__ StagedShared la_shared(unsigned char* smem, int stages)
+{
+    StagedShared ss;
+    ss.full = reinterpret_cast<uint64_t*>(smem);
+    ss.empty = ss.full + stages;
+    ss.wpart = reinterpret_cast<float2*>(smem + 16 * stages);
+    unsigned char* tail = smem + 16 * stages + (size_t)8 * kLaSums * kStagedConsumerWarps * (stages + 1);
+    ss.chunk = reinterpret_cast<int*>(tail);
+    ss.wcount = reinterpret_cast<unsigned*>(tail + 4 * stages);
+    ss.stage0 = smem + la_header_bytes(stages);
+    return ss;
+}
+struct LaVectors {
+    const float* z;  // gathered set: z, mw, mq
+    const float* mw;
+    const float* mq;
+    float* zo;  // the set this pass writes
+    float* mwo;
+    float* mqo;
+    float* w;
+};
+__device__ __forceinline__ LaVectors la_vectors(const PcgBuffers<float>& B, int set_in)
+{
+    const int64_t vs = 4 * (int64_t)B.n_blocks;
+    float* z1 = B.la;
+    float* mw0 = B.la + vs;
+    float* mw1 = B.la + 2 * vs;
+    float* mq0 = B.la + 3 * vs;
+    float* mq1 = B.la + 4 * vs;
+    LaVectors v;
+    v.z = set_in ? z1 : B.z;
+    v.mw = set_in ? mw1 : mw0;
+    v.mq = set_in ? mq1 : mq0;
+    v.zo = set_in ? B.z : z1;
+    v.mwo = set_in ? mw0 : mw1;
+    v.mqo = set_in ? mq0 : mq1;
+    v.w = B.la + 5 * vs;
+    return v;
+}
+// z_k of one component from (z_{k-1}, mw_{k-1}, mq_{k-2}): the owner and every gather use this
+__device__ __forceinline__ float la_znext(float z, float mw, float mq, float alpha, float beta)
+{
+    return __fmaf_rn(-alpha, __fmaf_rn(beta, mq, mw), z);
+}
+
+// Chunk partial of the kLaSums float-float sums of one consumer warp: a fixed shuffle tree per
+// value, then the last of the 15 warps to finish the chunk adds the warp sums in a fixed tree
+// over 16 lanes and stores the chunk's partials (value-major: part[k * n_chunks + c]).
+template <bool kF64Sums>
+__device__ __forceinline__ void la_publish(FF (&v)[kLaSums], const StagedShared& ss, unsigned ps, int cw, int c,
+                                           int n_chunks, double* part)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) v[k] = ff_add(v[k], ff_shfl_down(v[k], o));
+    float2* wp = ss.wpart + (size_t)ps * kStagedConsumerWarps * kLaSums;
+    unsigned last = 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) wp[cw * kLaSums + k] = make_float2(v[k].hi, v[k].lo);
+        __threadfence_block();
+        last = atomicAdd(&ss.wcount[ps], 1u) == kStagedConsumerWarps - 1 ? 1u : 0u;
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) return;
+    __threadfence_block();
+    __syncwarp();
+    FF t[kLaSums];
+#pragma unroll
+    for (int k = 0; k < kLaSums; ++k) {
+        const volatile float* x = reinterpret_cast<volatile float*>(&wp[lane * kLaSums + k]);
+        t[k] = lane < kStagedConsumerWarps ? FF{x[0], x[1]} : FF{0.f, 0.f};
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
+    if (lane == 0) {
+        ss.wcount[ps] = 0;
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) {
+            if constexpr (kF64Sums) part[(size_t)k * n_chunks + c] = (double)t[k].hi + (double)t[k].lo;
+            else reinterpret_cast<float2*>(part)[(size_t)k * n_chunks + c] = make_float2(t[k].hi, t[k].lo);
+        }
+    }
+}
+
+// Consumer warps of one look-ahead pass (kEntry: the first pass of a launch).  Per stage a warp
+// takes four rows (two per half-warp), issues the owner's loads and the gathers together, then
+// reads the stage's values from shared memory and releases the stage (no global load is in
+// flight at the release), forms the products, the owners' updates and this chunk's partials.
+template <bool kF64Sums, bool kEntry>
+__device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const StagedShared& ss, const LaVectors& V,
+                                           int n_chunks, float alpha, float beta, bool first, double* part,
+                                           unsigned& seq, volatile int* abort_flag)
+{
+    const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
+    const size_t stage_bytes = staged_stage_bytes(CAP, S);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
+    const int la = 4 * cw + half, lb = la + 2;
+    const int idx = lane16 >> 1;                  // epilogue: 0..2 row A, 3..5 row B
+    const bool owner = !(lane16 & 1) && idx < 6;  // the lane that finishes one component
+    const int d = idx % 3;
+    const int wbase = (lane & 16) + (idx < 3 ? 0 : 6);  // lanes holding this row's w components
+    const int n = B.n_blocks;
+    auto gather = [&](int c) {
+        if constexpr (kEntry) {
+            return ld4cg(V.z + 4 * c);
+        } else {
+            const Row4<float> z = ld4cg(V.z + 4 * c), mw = ld4cg(V.mw + 4 * c), mq = ld4cg(V.mq + 4 * c);
+            return Row4<float>{la_znext(z.x, mw.x, mq.x, alpha, beta), la_znext(z.y, mw.y, mq.y, alpha, beta),
+                               la_znext(z.z, mw.z, mq.z, alpha, beta), 0.f};
+        }
+    };
+    for (;;) {
+        const unsigned g = seq, s = g % NS;
+        // one decision per warp: the product below shuffles over the full warp
+        const bool stop = __any_sync(
+            0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1, B.staged.max_polls));
+        if (stop) {
+            *abort_flag = 1;
+            break;
+        }
+        const int c = *(volatile int*)&ss.chunk[s];
+        seq = g + 1;
+        if (c < 0) {  // end of this pass
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+            break;
+        }
+        const int r0 = c * S;
+        const int rowA = r0 + la, rowB = r0 + lb;
+        const bool vA = rowA < n, vB = rowB < n;
+        const bool own = owner && (idx < 3 ? vA : vB);
+        const int orow = idx < 3 ? rowA : rowB;
+        const int64_t o = 4 * (int64_t)orow + d;
+        const unsigned char* st = ss.stage0 + s * stage_bytes;
+        const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
+        const int kb4 = rp[0] & ~3;
+        const int kbA = vA ? rp[la] - kb4 : 0, keA = vA ? rp[la + 1] - kb4 : 0;
+        const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
+        const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
+        const float* __restrict__ svals = reinterpret_cast<const float*>(st);
+        // the owner's row values (written by other blocks in the previous pass: L2 loads)
+        float zp = 0.f, mwp = 0.f, mqp = 0.f, po = 0.f, qo = 0.f, wo = 0.f, xo = 0.f, ro = 0.f;
+        Row4<float> dv{}, qrow{};
+        if (own) {
+            dv = ld4(B.Dinv + 12 * (int64_t)orow + 4 * d);
+            zp = __ldcg(V.z + o);
+            if constexpr (kEntry) {
+                if (!first) {
+                    po = __ldcg(B.p + o);
+                    qrow = ld4cg(B.q + 4 * (int64_t)orow);
+                }
+            } else {
+                mwp = __ldcg(V.mw + o);
+                mqp = __ldcg(V.mq + o);
+                po = __ldcg(B.p + o);
+                qo = __ldcg(B.q + o);
+                wo = __ldcg(V.w + o);
+                xo = __ldcg(B.x + o);
+                ro = __ldcg(B.r + o);
+            }
+        }
+        float a[3], b[3];
+        if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
+            // rows of at most 16 blocks: one block of each row per lane, both gathers in
+            // flight with the owner's loads; the values are read after they return
+            const int kA = kbA + lane16, kB = kbB + lane16;
+            const bool hA = kA < keA, hB = kB < keB;
+            const Row4<float> xA = hA ? gather(scols[kA]) : Row4<float>{};
+            const Row4<float> xB = hB ? gather(scols[kB]) : Row4<float>{};
+            a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = 0.f;
+            if (hA) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    a[r] = svals[(3 * r) * CAP + kA] * xA.x + svals[(3 * r + 1) * CAP + kA] * xA.y +
+                           svals[(3 * r + 2) * CAP + kA] * xA.z;
+            }
+            if (hB) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    b[r] = svals[(3 * r) * CAP + kB] * xB.x + svals[(3 * r + 1) * CAP + kB] * xB.y +
+                           svals[(3 * r + 2) * CAP + kB] * xB.z;
+            }
+        } else {
+            two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, gather, a, b);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+        const float wd = half_warp_transpose_sum<float>(a, b, lane16);
+        const float w0 = __shfl_sync(0xffffffffu, wd, wbase), w1 = __shfl_sync(0xffffffffu, wd, wbase + 2),
+                    w2 = __shfl_sync(0xffffffffu, wd, wbase + 4);
+        FF t[kLaSums];
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) t[k] = FF{0.f, 0.f};
+        if (own) {
+            const float mwd = dv.x * w0 + dv.y * w1 + dv.z * w2;
+            if constexpr (kEntry) {
+                const float mqd = first ? 0.f : dv.x * qrow.x + dv.y * qrow.y + dv.z * qrow.z;
+                const float qd = first ? 0.f : (d == 0 ? qrow.x : d == 1 ? qrow.y : qrow.z);
+                V.zo[o] = zp;
+                V.mwo[o] = mwd;
+                V.mqo[o] = mqd;
+                V.w[o] = wd;
+                if (first) {  // no earlier direction: p = q = 0 for the first update
+                    B.p[o] = 0.f;
+                    B.q[o] = 0.f;
+                }
+                t[2] = ff_prod(zp, wd);
+                t[3] = ff_add(ff_prod(zp, qd), ff_prod(po, wd));
+                t[4] = ff_prod(po, qd);
+            } else {
+                const float pd = __fmaf_rn(beta, po, zp);
+                const float qd = __fmaf_rn(beta, qo, wo);
+                const float mqd = __fmaf_rn(beta, mqp, mwp);
+                const float xd = __fmaf_rn(alpha, pd, xo);
+                const float rd = __fmaf_rn(-alpha, qd, ro);
+                const float zd = __fmaf_rn(-alpha, mqd, zp);  // la_znext's bits
+                V.zo[o] = zd;
+                V.mwo[o] = mwd;
+                V.mqo[o] = mqd;
+                V.w[o] = wd;
+                B.p[o] = pd;
+                B.q[o] = qd;
+                B.x[o] = xd;
+                B.r[o] = rd;
+                t[0] = ff_prod(rd, rd);
+                t[1] = ff_prod(rd, zd);
+                t[2] = ff_prod(zd, wd);
+                t[3] = ff_add(ff_prod(zd, qd), ff_prod(pd, wd));
+                t[4] = ff_prod(pd, qd);
+            }
+        }
+        la_publish<kF64Sums>(t, ss, g % (unsigned)(NS + 1), cw, c, n_chunks, part);
+    }
+}
+
+// Fixed-order sums of the kLaSums chunk partial arrays (value-major, n each), returned to every
+// thread.  sh: kLaSums * 2 floats per warp.
+template <bool kF64Sums>
+__device__ void la_sum_partials(const double* part, int n, double* sh, double (&out)[kLaSums])
+{
+    __shared__ double result[kLaSums];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if constexpr (kF64Sums) {
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) {
+            double a = 0.0;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) a += __ldcg(part + (size_t)k * n + i);
+            const double r = block_reduce<false>(a, sh);
+            if (threadIdx.x == 0) result[k] = r;
+        }
+    } else {
+        const float2* p2 = reinterpret_cast<const float2*>(part);
+        FF a[kLaSums];
+#pragma unroll
+        for (int k = 0; k < kLaSums; ++k) a[k] = FF{0.f, 0.f};
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            float2 v[kLaSums];
+#pragma unroll
+            for (int k = 0; k < kLaSums; ++k) v[k] = __ldcg(p2 + (size_t)k * n + i);
+#pragma unroll
+            for (int k = 0; k < kLaSums; ++k) a[k] = ff_add(a[k], FF{v[k].x, v[k].y});
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < kLaSums; ++k) a[k] = ff_add(a[k], ff_shfl_down(a[k], o));
+        float* shf = reinterpret_cast<float*>(sh);
+        __syncthreads();
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < kLaSums; ++k) {
+                shf[(warp * kLaSums + k) * 2] = a[k].hi;
+                shf[(warp * kLaSums + k) * 2 + 1] = a[k].lo;
+            }
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int k = 0; k < kLaSums; ++k)
+                a[k] = lane < nw ? FF{shf[(lane * kLaSums + k) * 2], shf[(lane * kLaSums + k) * 2 + 1]} : FF{0.f, 0.f};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < kLaSums; ++k) a[k] = ff_add(a[k], ff_shfl_down(a[k], o));
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < kLaSums; ++k) result[k] = (double)a[k].hi + (double)a[k].lo;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kLaSums; ++k) out[k] = result[k];
+}
+
+template <bool kF64Sums>
+__global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<float> B)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ double sh[kLaSums * (kStagedThreads / 32)];  // la_sum_partials: 2 floats per value and warp
+    __shared__ int aborted, barrier_ok;
+    __shared__ PcgState st0;  // as k_pcg_init or the residual replacement left it
+    if (threadIdx.x == 0) st0 = *B.state;
+    __syncthreads();
+    if (st0.done) return;
+    const int NS = B.staged.stages;
+    const StagedShared ss = la_shared(smem, NS);
+    if (threadIdx.x == 0) aborted = 0;
+    if (threadIdx.x <= NS) ss.wcount[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(smem_addr(&ss.full[s]), 1);
+            mbar_init(smem_addr(&ss.empty[s]), kStagedConsumerWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    volatile int* abort_flag = &aborted;
+    unsigned* bar = B.tickets + 6;
+    unsigned* ctr = B.tickets + 8;  // chunk counters of three consecutive passes
+    unsigned generation = 0, seq = 0, issued = 0;
+    DynProducer P;
+    const int n_chunks = pcg_chunks(B.n_blocks, B.staged.stage_rows);
+    const bool first = st0.iteration == 0;
+    // after a residual replacement the state holds the new r.z and beta (k_pcg_replace_residual)
+    double rz = st0.rz, alpha = 0.0, beta = first ? 0.0 : st0.beta, pAp = 0.0, rr = 0.0, error = st0.error;
+    int iteration = st0.iteration, converged = 0, indefinite = 0, paused = 0;
+    bool failed = false;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int li = 0;; ++li) {
+        // no block claims from pass li - 1 any more, none from pass li + 2 before the barrier
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ctr[(li + 2) % 3], 0u);
+        const LaVectors V = la_vectors(B, li & 1);
+        double* part = B.partials + (size_t)(li & 1) * kLaSums * n_chunks;
+        if (warp == 0) {
+            if (lane == 0) dyn_produce(B, ss, li, ctr, n_chunks, issued, P, abort_flag);
+        } else if (li == 0) {
+            la_consume<kF64Sums, true>(B, ss, V, n_chunks, 0.f, 0.f, first, part, seq, abort_flag);
+        } else {
+            la_consume<kF64Sums, false>(B, ss, V, n_chunks, (float)alpha, (float)beta, false, part, seq, abort_flag);
+        }
+        if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls) || *abort_flag) {
+            failed = true;
+            break;
+        }
+        double sums[kLaSums];
+        la_sum_partials<kF64Sums>(part, n_chunks, sh, sums);
+        if (li > 0) {  // the pass formed x_k and r_k: the reference's test after its update
+            iteration += 1;
+            rr = sums[0];
+            error = sqrt(rr / st0.bb);
+            if (error < st0.abs_tol || error / st0.error0 < st0.rel_tol) {
+                converged = 1;
+                break;
+            }
+            if (iteration >= st0.max_iterations) break;
+            if (st0.replace_every > 0 && iteration % st0.replace_every == 0) {
+                paused = 1;  // rz stays that of the last iterate: the replacement forms beta
+                break;
+            }
+            beta = sums[1] / rz;
+            rz = sums[1];
+        }
+        pAp = sums[2] + beta * sums[3] + beta * beta * sums[4];
+        if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
+            indefinite = 1;
+            iteration += 1;
+            break;
+        }
+        alpha = rz / pAp;
+    }
+    staged_drain(B, ss, issued);  // stages copied ahead for a pass that will not run
+    if (failed && threadIdx.x == 0) atomicExch(&B.state->wait_failed, 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !failed) {
+        PcgState* st = B.state;
+        st->iteration = iteration;
+        st->converged = converged;
+        st->indefinite = indefinite;
+        st->done = paused ? 0 : 1;
+        st->pAp = pAp;
+        st->alpha = alpha;
+        st->beta = beta;
+        st->rz = rz;
+        st->rr = rr;
+        st->error = error;
+    }
+}
+
 // Residual replacement (see launch_pcg_replace_residual): one half-warp per block row,
 // lane-strided over the row's blocks, products and sums in FP64.
 __global__ void __launch_bounds__(256) k_pcg_replace_residual(PcgBuffers<float> B, const double* __restrict__ grad)
@@ -2519,9 +2951,12 @@ void launch_pcg_solve_persistent(const PcgBuffers<float>& B, cudaStream_t s)
     PcgBuffers<float> arg = B;
     arg.staged.max_polls = wait_poll_limit();
     void* args[] = {&arg};
-    const void* fn = B.staged.f64_sums ? (const void*)k_pcg_solve_staged<true> : (const void*)k_pcg_solve_staged<false>;
+    const bool la = B.staged.lookahead && B.la;
+    const void* fn = la ? (B.staged.f64_sums ? (const void*)k_pcg_solve_la<true> : (const void*)k_pcg_solve_la<false>)
+                        : (B.staged.f64_sums ? (const void*)k_pcg_solve_staged<true>
+                                             : (const void*)k_pcg_solve_staged<false>);
     const cudaError_t l = cudaLaunchCooperativeKernel(fn, dim3(B.staged.grid), dim3(kStagedThreads), args,
-                                                      B.staged.smem_bytes, s);
+                                                      la ? B.staged.la_smem_bytes : B.staged.smem_bytes, s);
     if (l != cudaSuccess)
         throw std::runtime_error(std::string("symx_gb300: cooperative launch of the PCG failed: ") + cudaGetErrorString(l));
     check_launch("pcg_solve_staged");
@@ -2586,6 +3021,25 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
             pcg_sums_layout(pcg_chunks(n, S), (int)grid).total <= 2 * kPcgMaxPartials &&
             pcg_chunks(n, S) + 2 * grid <= 2 * kPcgMaxPartials)
             st.persistent = 1;
+        cudaGetLastError();
+        // the look-ahead form: its own header, the same ring; partials of two passes
+        const size_t la_smem = la_header_bytes(stages) + (size_t)stages * stage_bytes;
+        const int64_t la_budget = std::min<int64_t>(optin, per_sm_bytes / per_sm - 1024) - 1024;  // static smem
+        int resident_la0 = 0, resident_la1 = 0;
+        if (st.persistent && (int64_t)la_smem <= la_budget &&
+            cudaFuncSetAttribute(k_pcg_solve_la<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)la_smem) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k_pcg_solve_la<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)la_smem) ==
+                cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_la0, k_pcg_solve_la<false>, kStagedThreads,
+                                                          la_smem) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_la1, k_pcg_solve_la<true>, kStagedThreads,
+                                                          la_smem) == cudaSuccess &&
+            resident_la0 >= per_sm && resident_la1 >= per_sm &&
+            (int64_t)2 * kLaSums * pcg_chunks(n, S) <= 2 * (int64_t)kPcgMaxPartials) {
+            st.lookahead = 1;
+            st.la_smem_bytes = la_smem;
+        }
         cudaGetLastError();
         st.stages = stages;
         st.stage_rows = S;

@@ -142,6 +142,10 @@ struct PcgBuffers {
     T* p;               // search directions, ping-pong between p and p2 across iterations
     T* p2;
     T* q;
+    // Look-ahead PCG (float, k_pcg_solve_la; null: not used): six more vectors of 4 * n_blocks
+    // values each, one after the other: z of the second gather set, mw = M^-1 A z of both
+    // sets, mq = M^-1 q of both sets, w = A z.  z of the first set is `z` above.
+    T* la = nullptr;
     double* partials;   // kPcgPartials doubles x 2
     unsigned* tickets;  // counters: 16 for the persistent kernel, 8 otherwise
     PcgState* state;
@@ -155,6 +159,8 @@ struct PcgBuffers {
         int grid = 0;
         size_t smem_bytes = 0;
         int persistent = 0;      // 1: the whole PCG loop can run as one cooperative launch
+        int lookahead = 0;       // 1: ... also as the look-ahead form (k_pcg_solve_la), used when `la` is set
+        size_t la_smem_bytes = 0;  // dynamic shared memory of the look-ahead form
         long long max_polls = kDefaultWaitPolls;  // set from wait_poll_limit() at each launch
         // one-launch PCG: chunk and block partials of p.Ap, r.r, r.z summed in FP64 (1) or in
         // float-float (0); the per-thread and per-warp sums are float-float in both

@@ -586,6 +586,7 @@ struct SolverImpl {
     DevBuf<float> vals32, Dinv32;
     DevBuf<double> vals64, Dinv64;
     DevBuf<float> v32[6];
+    DevBuf<float> la32;  // look-ahead PCG: six more vectors (PcgBuffers::la)
     DevBuf<double> v64[6];
     DevBuf<double> partials, scalars;
     DevBuf<unsigned> tickets;
@@ -639,6 +640,10 @@ struct SolverImpl {
             for (auto& v : v32) {
                 v.alloc(n);
                 ck(cudaMemset(v.p, 0, sizeof(float) * n), "memset");
+            }
+            if (staged.lookahead) {
+                la32.alloc(6 * n);
+                ck(cudaMemset(la32.p, 0, sizeof(float) * 6 * n), "memset");
             }
         } else {
             H64.alloc((size_t)n_hblocks * 9);
@@ -1305,6 +1310,7 @@ SolverReturn solve_t(SolverImpl& I, const NewtonSettings& S, SolveStats& st, int
     if constexpr (std::is_same<T, float>::value) {
         B.staged = I.staged;
         B.staged.f64_sums = S.cg_fp64_partial_sums ? 1 : 0;
+        B.la = S.cg_lookahead && I.staged.lookahead ? I.la32.p : nullptr;
     }
     T* du = V[0].p;
 
@@ -1608,7 +1614,10 @@ AdjointInfo adjoint_pcg_t(SolverImpl& I, const double* rhs, double* lambda, doub
     B.partials = I.partials.p;
     B.tickets = I.tickets.p;
     B.state = I.pcg_state.p;
-    if constexpr (std::is_same<T, float>::value) B.staged = I.staged;
+    if constexpr (std::is_same<T, float>::value) {
+        B.staged = I.staged;
+        B.la = I.staged.lookahead ? I.la32.p : nullptr;
+    }
     PcgState init{};
     init.abs_tol = 0.0;
     init.rel_tol = rel_tol;

@@ -84,6 +84,10 @@ struct NewtonSettings {
     // Every block forms the sums itself, so FP64 costs FP64-pipe time in every block
     // (GB300's FP64 rate is 1/64 of FP32): about 8 us per iteration on the 64^3 Tet4 step.
     bool cg_fp64_partial_sums = false;
+    // One-launch FP32 PCG (Mixed): one grid barrier per iteration, the update of x, r and z folded
+    // into the next product pass (k_pcg_solve_la); false: the two-barrier form (product pass,
+    // barrier, update, barrier).  Same iterates up to rounding.
+    bool cg_lookahead = false;
 };
 
 struct Context {
