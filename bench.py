@@ -413,6 +413,8 @@ def run_profile(args):
     solver.set_settings(cg_rel_tolerance=1e-3, precision=args.profile_solve)
     if args.profile_split:  # FP64-accurate projection, FP64 residual replacement and partial sums
         solver.set_settings(projection_fp64_refinement=1, cg_residual_replacement=50, cg_fp64_partial_sums=1)
+    if args.pcg_two_barrier:
+        solver.set_settings(cg_lookahead=0)
     out = None
     for i in range(2):
         solver.set_state(p["x_init"], p["x0"], p["v0"])
@@ -664,6 +666,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP64-projection / residual-replacement runs")
     ap.add_argument("--profile-solve", choices=["mixed", "fp64"], default=None)
+    ap.add_argument("--pcg-two-barrier", action="store_true",
+                    help="with --profile-solve: the two-barrier one-launch PCG instead of the look-ahead form")
     ap.add_argument("--profile-split", action="store_true",
                     help="with --profile-solve: the FP64 projection / residual / partial-sum settings")
     ap.add_argument("--measure", choices=["adjoint", "rollout"], default=None,

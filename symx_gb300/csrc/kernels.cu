@@ -965,7 +965,8 @@ struct DotAcc<float> {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) a = ff_add(a, ff_shfl_down(a, o));
         }
-        return (double)a.hi + (double)a.lo;
+        // FP64 only where the result is used (GB300's FP64 rate is 1/64 of FP32)
+        return threadIdx.x == 0 ? (double)a.hi + (double)a.lo : 0.0;
     }
 };
 template <>
@@ -1910,6 +1911,19 @@ __device__ bool grid_barrier(unsigned* bar, unsigned& generation, volatile int* 
     return *ok_flag != 0;
 }
 
+// Per-iteration decisions of a persistent PCG block, taken by thread 0 alone and read by the
+// others after a __syncthreads: the scalar recurrence runs in FP64, and on GB300 (FP64 at
+// 1/64 of the FP32 rate) every thread of every block repeating its divisions and square root
+// would cost more than the rest of an iteration's arithmetic.
+struct PcgCtl {
+    float alpha, beta;  // the coefficients the next pass / update use
+    int stop;           // 1: leave the iteration loop
+    // thread 0's FP64 recurrence and outcome (in shared memory, so the other threads hold no
+    // registers for it)
+    double rz, alpha64, beta64, pAp, rr, error;
+    int iteration, converged, indefinite, paused;
+};
+
 // Chunks of the persistent kernel's product pass (one stage of rows each).
 __host__ __device__ __forceinline__ int pcg_chunks(int n_blocks, int stage_rows)
 {
@@ -1946,15 +1960,27 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
     const int row_begin = (int)((int64_t)blockIdx.x * B.n_blocks / G);
     const int row_end = (int)((int64_t)(blockIdx.x + 1) * B.n_blocks / G);
     // a launch after a residual replacement continues the recurrence: beta from the state
-    double rz = st0.rz, alpha = 0.0, beta = st0.iteration > 0 ? st0.beta : 0.0, pAp = 0.0, rr = 0.0,
-           error = st0.error;
-    int iteration = st0.iteration, converged = 0, indefinite = 0, paused = 0;
+    // the FP64 recurrence is thread 0's (PcgCtl); every thread counts the iterations
+    __shared__ PcgCtl ctl;
+    if (threadIdx.x == 0) {
+        ctl.rz = st0.rz;
+        ctl.alpha64 = 0.0;
+        ctl.beta64 = st0.iteration > 0 ? st0.beta : 0.0;
+        ctl.pAp = ctl.rr = 0.0;
+        ctl.error = st0.error;
+        ctl.iteration = st0.iteration;
+        ctl.converged = ctl.indefinite = ctl.paused = 0;
+        ctl.beta = (float)ctl.beta64;
+    }
+    __syncthreads();
+    int iteration = st0.iteration;
     bool failed = false;
+    float beta_f = ctl.beta;
     for (int li = 0;; ++li) {
         float* p_old = (iteration & 1) ? B.p : B.p2;
         float* p_new = (iteration & 1) ? B.p2 : B.p;
         const bool first = iteration == 0;
-        staged_spmv_pass_dyn<kF64Sums>(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : (float)beta, seq,
+        staged_spmv_pass_dyn<kF64Sums>(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : beta_f, seq,
                                        issued, P, abort_flag);
         if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls) || *abort_flag) {
             failed = true;
@@ -1962,15 +1988,23 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         }
         // no block claims from pass li - 1 any more, none from pass li + 2 before the next barrier
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ctr[(li + 2) % 3], 0u);
-        pAp = kF64Sums ? sum_partials_f64(B.partials, n_chunks, sh)
-                       : sum_chunk_partials(reinterpret_cast<const float2*>(B.partials), n_chunks, sh);
-        if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
-            indefinite = 1;
-            iteration += 1;
-            break;
+        const double pAp = kF64Sums ? sum_partials_f64(B.partials, n_chunks, sh)
+                                    : sum_chunk_partials(reinterpret_cast<const float2*>(B.partials), n_chunks, sh);
+        if (threadIdx.x == 0) {
+            ctl.stop = 0;
+            ctl.pAp = pAp;
+            if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
+                ctl.indefinite = 1;
+                ctl.iteration = iteration + 1;
+                ctl.stop = 1;
+            } else {
+                ctl.alpha64 = ctl.rz / pAp;
+                ctl.alpha = (float)ctl.alpha64;
+            }
         }
-        alpha = rz / pAp;
-        const float a = (float)alpha;
+        __syncthreads();
+        if (ctl.stop) break;
+        const float a = ctl.alpha;
         DotAcc<float> rra, rza;
         // one row per thread and pass, all its loads (preconditioner block included) issued
         // before its math
@@ -2012,7 +2046,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
             failed = true;
             break;
         }
-        double rz_new;
+        double rr, rz_new;
         if (kF64Sums) {
             rr = sum_partials_f64(part_rr64, (int)G, sh);
             rz_new = sum_partials_f64(part_rz64, (int)G, sh);
@@ -2020,33 +2054,41 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
             sum_grid_partials2_ff(part_rr, part_rz, sh, rr, rz_new);
         }
         iteration += 1;
-        error = sqrt(rr / st0.bb);
-        if (error < st0.abs_tol || error / st0.error0 < st0.rel_tol) {
-            converged = 1;
-            break;
+        if (threadIdx.x == 0) {
+            ctl.stop = 1;
+            ctl.iteration = iteration;
+            ctl.rr = rr;
+            ctl.error = sqrt(rr / st0.bb);
+            if (ctl.error < st0.abs_tol || ctl.error / st0.error0 < st0.rel_tol) {
+                ctl.converged = 1;
+            } else if (iteration >= st0.max_iterations) {
+            } else if (st0.replace_every > 0 && iteration % st0.replace_every == 0) {
+                ctl.paused = 1;  // rz stays that of the last iterate: the replacement forms beta
+            } else {
+                ctl.beta64 = rz_new / ctl.rz;
+                ctl.rz = rz_new;
+                ctl.beta = (float)ctl.beta64;
+                ctl.stop = 0;
+            }
         }
-        if (iteration >= st0.max_iterations) break;
-        if (st0.replace_every > 0 && iteration % st0.replace_every == 0) {
-            paused = 1;  // rz stays that of the last iterate: the replacement forms beta
-            break;
-        }
-        beta = rz_new / rz;
-        rz = rz_new;
+        __syncthreads();
+        if (ctl.stop) break;
+        beta_f = ctl.beta;
     }
     staged_drain(B, ss, issued);  // stages copied ahead for a pass that will not run
     if (failed && threadIdx.x == 0) atomicExch(&B.state->wait_failed, 1);
     if (blockIdx.x == 0 && threadIdx.x == 0 && !failed) {
         PcgState* st = B.state;
-        st->iteration = iteration;
-        st->converged = converged;
-        st->indefinite = indefinite;
-        st->done = paused ? 0 : 1;
-        st->pAp = pAp;
-        st->alpha = alpha;
-        st->beta = beta;
-        st->rz = rz;
-        st->rr = rr;
-        st->error = error;
+        st->iteration = ctl.iteration;
+        st->converged = ctl.converged;
+        st->indefinite = ctl.indefinite;
+        st->done = ctl.paused ? 0 : 1;
+        st->pAp = ctl.pAp;
+        st->alpha = ctl.alpha64;
+        st->beta = ctl.beta64;
+        st->rz = ctl.rz;
+        st->rr = ctl.rr;
+        st->error = ctl.error;
     }
 }
 
@@ -2057,11 +2099,14 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
 // With w_k = A z_k, mw_k = M^-1 w_k, mq_k = M^-1 q_k, iteration k of the pass computes, per
 // block row (the owning lane of each component):
 //     p_{k-1} = z_{k-1} + beta_{k-1} p_{k-2}        q_{k-1} = w_{k-1} + beta_{k-1} q_{k-2}
-//     mq_{k-1} = mw_{k-1} + beta_{k-1} mq_{k-2}     x_k = x_{k-1} + alpha_{k-1} p_{k-1}
-//     r_k = r_{k-1} - alpha_{k-1} q_{k-1}           z_k = z_{k-1} - alpha_{k-1} mq_{k-1}
-//     w_k = A z_k                                   mw_k = M^-1 w_k
-// where each gathered column c of A z_k is formed from (z_{k-1}, mw_{k-1}, mq_{k-2}) of row c
-// by the same two fused multiply-adds as its owner uses (the same bits).  The pass leaves
+//     x_k = x_{k-1} + alpha_{k-1} p_{k-1}           r_k = r_{k-1} - alpha_{k-1} q_{k-1}
+//     z_k = M^-1 r_k      mq_{k-1} = M^-1 q_{k-1}   w_k = A z_k      mw_k = M^-1 w_k
+// where each gathered column c of z_k is formed from (z_{k-1}, mw_{k-1}, mq_{k-2}) of row c as
+// z_{k-1} - alpha_{k-1} (mw_{k-1} + beta_{k-1} mq_{k-2}), equal to M^-1 r_k up to the rounding
+// of that one step: the stored z and mq are formed from r and q in every pass, so no rounding
+// accumulates in them (a recursively updated z loses its agreement with r once r falls below
+// the FP32 resolution of its first value, and the residual then stops decreasing).  The pass
+// leaves
 // per-chunk partials of r.r, r.z, z.w, z.q + p.w and p.q; after the barrier every block
 // sums them in one fixed order and forms beta_k = rz_k / rz_{k-1} and
 //     p_k.A p_k = z.w + beta_k (z.q + p.w) + beta_k^2 p.q       (p_k = z_k + beta_k p_{k-1})
@@ -2128,46 +2173,73 @@ __device__ __forceinline__ float la_znext(float z, float mw, float mq, float alp
     return __fmaf_rn(-alpha, __fmaf_rn(beta, mq, mw), z);
 }
 
-// Chunk partial of the kLaSums float-float sums of one consumer warp: a fixed shuffle tree per
-// value, then the last of the 15 warps to finish the chunk adds the warp sums in a fixed tree
-// over 16 lanes and stores the chunk's partials (value-major: part[k * n_chunks + c]).
+// Sums of eight float-float values over groups of W lanes (W = 32 or 16) in a fixed tree that
+// transposes as it goes: at each of the first three levels a lane keeps half of its values and
+// sends the other half, so each lane ends with one value, the total of value j in lane
+// j * W / 8 of its group (the other lanes hold partial or repeated sums).  Each total is the
+// same fixed sequence of float-float additions on every run.
+__device__ __forceinline__ FF ff_shfl_xor(FF a, int o)
+{
+    return FF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+}
+template <int W>
+__device__ __forceinline__ FF ff_transpose_sum8(const FF (&v)[8], int lane)
+{
+    constexpr int h = W / 2;
+    FF w[4], u[2];
+    const bool b2 = (lane & h) != 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = ff_add(b2 ? v[i + 4] : v[i], ff_shfl_xor(b2 ? v[i] : v[i + 4], h));
+    const bool b1 = (lane & (h / 2)) != 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) u[i] = ff_add(b1 ? w[i + 2] : w[i], ff_shfl_xor(b1 ? w[i] : w[i + 2], h / 2));
+    const bool b0 = (lane & (h / 4)) != 0;
+    FF t = ff_add(b0 ? u[1] : u[0], ff_shfl_xor(b0 ? u[0] : u[1], h / 4));
+#pragma unroll
+    for (int o = h / 8; o > 0; o >>= 1) t = ff_add(t, ff_shfl_xor(t, o));
+    return t;
+}
+
+// Chunk partial of the kLaSums float-float sums of one consumer warp: a fixed transposing
+// tree over the warp, then the last of the 15 warps to finish the chunk adds the 15 warp sums
+// in a fixed tree over 16 lanes and stores the chunk's partials (value-major:
+// part[k * n_chunks + c]).
 template <bool kF64Sums>
-__device__ __forceinline__ void la_publish(FF (&v)[kLaSums], const StagedShared& ss, unsigned ps, int cw, int c,
+__device__ __forceinline__ void la_publish(const FF (&v)[kLaSums], const StagedShared& ss, unsigned ps, int cw, int c,
                                            int n_chunks, double* part)
 {
     const int lane = threadIdx.x & 31;
+    FF v8[8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-        for (int k = 0; k < kLaSums; ++k) v[k] = ff_add(v[k], ff_shfl_down(v[k], o));
+    for (int k = 0; k < 8; ++k) v8[k] = k < kLaSums ? v[k] : FF{0.f, 0.f};
+    const FF t = ff_transpose_sum8<32>(v8, lane);  // value lane / 4 in lanes 0, 4, ..., 16
     float2* wp = ss.wpart + (size_t)ps * kStagedConsumerWarps * kLaSums;
+    if ((lane & 3) == 0 && lane < 4 * kLaSums) wp[cw * kLaSums + (lane >> 2)] = make_float2(t.hi, t.lo);
+    __syncwarp();
     unsigned last = 0;
     if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < kLaSums; ++k) wp[cw * kLaSums + k] = make_float2(v[k].hi, v[k].lo);
         __threadfence_block();
         last = atomicAdd(&ss.wcount[ps], 1u) == kStagedConsumerWarps - 1 ? 1u : 0u;
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) return;
     __threadfence_block();
     __syncwarp();
-    FF t[kLaSums];
+    FF s8[8];
 #pragma unroll
-    for (int k = 0; k < kLaSums; ++k) {
-        const volatile float* x = reinterpret_cast<volatile float*>(&wp[lane * kLaSums + k]);
-        t[k] = lane < kStagedConsumerWarps ? FF{x[0], x[1]} : FF{0.f, 0.f};
-    }
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1)
-#pragma unroll
-        for (int k = 0; k < kLaSums; ++k) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
-    if (lane == 0) {
-        ss.wcount[ps] = 0;
-#pragma unroll
-        for (int k = 0; k < kLaSums; ++k) {
-            if constexpr (kF64Sums) part[(size_t)k * n_chunks + c] = (double)t[k].hi + (double)t[k].lo;
-            else reinterpret_cast<float2*>(part)[(size_t)k * n_chunks + c] = make_float2(t[k].hi, t[k].lo);
+    for (int k = 0; k < 8; ++k) {
+        if (k < kLaSums && lane < kStagedConsumerWarps) {
+            const volatile float* x = reinterpret_cast<volatile float*>(&wp[lane * kLaSums + k]);
+            s8[k] = FF{x[0], x[1]};
+        } else {
+            s8[k] = FF{0.f, 0.f};
         }
+    }
+    const FF s = ff_transpose_sum8<16>(s8, lane);  // value lane / 2 in lanes 0, 2, ..., 8
+    if (lane == 0) ss.wcount[ps] = 0;
+    if ((lane & 1) == 0 && lane < 2 * kLaSums) {
+        const int k = lane >> 1;
+        if constexpr (kF64Sums) part[(size_t)k * n_chunks + c] = (double)s.hi + (double)s.lo;
+        else reinterpret_cast<float2*>(part)[(size_t)k * n_chunks + c] = make_float2(s.hi, s.lo);
     }
 }
 
@@ -2229,7 +2301,7 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
         const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
         const float* __restrict__ svals = reinterpret_cast<const float*>(st);
         // the owner's row values (written by other blocks in the previous pass: L2 loads)
-        float zp = 0.f, mwp = 0.f, mqp = 0.f, po = 0.f, qo = 0.f, wo = 0.f, xo = 0.f, ro = 0.f;
+        float zp = 0.f, po = 0.f, qo = 0.f, wo = 0.f, xo = 0.f, ro = 0.f;
         Row4<float> dv{}, qrow{};
         if (own) {
             dv = ld4(B.Dinv + 12 * (int64_t)orow + 4 * d);
@@ -2240,8 +2312,6 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
                     qrow = ld4cg(B.q + 4 * (int64_t)orow);
                 }
             } else {
-                mwp = __ldcg(V.mw + o);
-                mqp = __ldcg(V.mq + o);
                 po = __ldcg(B.p + o);
                 qo = __ldcg(B.q + o);
                 wo = __ldcg(V.w + o);
@@ -2281,9 +2351,9 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
         FF t[kLaSums];
 #pragma unroll
         for (int k = 0; k < kLaSums; ++k) t[k] = FF{0.f, 0.f};
-        if (own) {
-            const float mwd = dv.x * w0 + dv.y * w1 + dv.z * w2;
-            if constexpr (kEntry) {
+        if constexpr (kEntry) {
+            if (own) {
+                const float mwd = dv.x * w0 + dv.y * w1 + dv.z * w2;
                 const float mqd = first ? 0.f : dv.x * qrow.x + dv.y * qrow.y + dv.z * qrow.z;
                 const float qd = first ? 0.f : (d == 0 ? qrow.x : d == 1 ? qrow.y : qrow.z);
                 V.zo[o] = zp;
@@ -2297,13 +2367,22 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
                 t[2] = ff_prod(zp, wd);
                 t[3] = ff_add(ff_prod(zp, qd), ff_prod(po, wd));
                 t[4] = ff_prod(po, qd);
-            } else {
-                const float pd = __fmaf_rn(beta, po, zp);
-                const float qd = __fmaf_rn(beta, qo, wo);
-                const float mqd = __fmaf_rn(beta, mqp, mwp);
-                const float xd = __fmaf_rn(alpha, pd, xo);
-                const float rd = __fmaf_rn(-alpha, qd, ro);
-                const float zd = __fmaf_rn(-alpha, mqd, zp);  // la_znext's bits
+            }
+        }
+        if constexpr (!kEntry) {
+            // every lane takes part in the shuffles (non-owners carry zeros)
+            const float pd = __fmaf_rn(beta, po, zp);
+            const float qd = __fmaf_rn(beta, qo, wo);
+            const float xd = __fmaf_rn(alpha, pd, xo);
+            const float rd = __fmaf_rn(-alpha, qd, ro);
+            const float r0 = __shfl_sync(0xffffffffu, rd, wbase), r1 = __shfl_sync(0xffffffffu, rd, wbase + 2),
+                        r2 = __shfl_sync(0xffffffffu, rd, wbase + 4);
+            const float q0 = __shfl_sync(0xffffffffu, qd, wbase), q1 = __shfl_sync(0xffffffffu, qd, wbase + 2),
+                        q2 = __shfl_sync(0xffffffffu, qd, wbase + 4);
+            if (own) {
+                const float mwd = dv.x * w0 + dv.y * w1 + dv.z * w2;
+                const float zd = dv.x * r0 + dv.y * r1 + dv.z * r2;
+                const float mqd = dv.x * q0 + dv.y * q1 + dv.z * q2;
                 V.zo[o] = zd;
                 V.mwo[o] = mwd;
                 V.mqo[o] = mqd;
@@ -2410,9 +2489,18 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<f
     DynProducer P;
     const int n_chunks = pcg_chunks(B.n_blocks, B.staged.stage_rows);
     const bool first = st0.iteration == 0;
-    // after a residual replacement the state holds the new r.z and beta (k_pcg_replace_residual)
-    double rz = st0.rz, alpha = 0.0, beta = first ? 0.0 : st0.beta, pAp = 0.0, rr = 0.0, error = st0.error;
-    int iteration = st0.iteration, converged = 0, indefinite = 0, paused = 0;
+    // after a residual replacement the state holds the new r.z and beta (k_pcg_replace_residual);
+    // the FP64 recurrence is thread 0's (PcgCtl)
+    __shared__ PcgCtl ctl;
+    if (threadIdx.x == 0) {
+        ctl.rz = st0.rz;
+        ctl.alpha64 = 0.0;
+        ctl.beta64 = first ? 0.0 : st0.beta;
+        ctl.pAp = ctl.rr = 0.0;
+        ctl.error = st0.error;
+        ctl.iteration = st0.iteration;
+        ctl.converged = ctl.indefinite = ctl.paused = 0;
+    }
     bool failed = false;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int li = 0;; ++li) {
@@ -2425,7 +2513,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<f
         } else if (li == 0) {
             la_consume<kF64Sums, true>(B, ss, V, n_chunks, 0.f, 0.f, first, part, seq, abort_flag);
         } else {
-            la_consume<kF64Sums, false>(B, ss, V, n_chunks, (float)alpha, (float)beta, false, part, seq, abort_flag);
+            la_consume<kF64Sums, false>(B, ss, V, n_chunks, ctl.alpha, ctl.beta, false, part, seq, abort_flag);
         }
         if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls) || *abort_flag) {
             failed = true;
@@ -2433,44 +2521,57 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<f
         }
         double sums[kLaSums];
         la_sum_partials<kF64Sums>(part, n_chunks, sh, sums);
-        if (li > 0) {  // the pass formed x_k and r_k: the reference's test after its update
-            iteration += 1;
-            rr = sums[0];
-            error = sqrt(rr / st0.bb);
-            if (error < st0.abs_tol || error / st0.error0 < st0.rel_tol) {
-                converged = 1;
-                break;
+        if (threadIdx.x == 0) {
+            ctl.stop = 1;
+            bool go = true;
+            if (li > 0) {  // the pass formed x_k and r_k: the reference's test after its update
+                ctl.iteration += 1;
+                ctl.rr = sums[0];
+                ctl.error = sqrt(ctl.rr / st0.bb);
+                if (ctl.error < st0.abs_tol || ctl.error / st0.error0 < st0.rel_tol) {
+                    ctl.converged = 1;
+                    go = false;
+                } else if (ctl.iteration >= st0.max_iterations) {
+                    go = false;
+                } else if (st0.replace_every > 0 && ctl.iteration % st0.replace_every == 0) {
+                    ctl.paused = 1;  // rz stays that of the last iterate: the replacement forms beta
+                    go = false;
+                } else {
+                    ctl.beta64 = sums[1] / ctl.rz;
+                    ctl.rz = sums[1];
+                }
             }
-            if (iteration >= st0.max_iterations) break;
-            if (st0.replace_every > 0 && iteration % st0.replace_every == 0) {
-                paused = 1;  // rz stays that of the last iterate: the replacement forms beta
-                break;
+            if (go) {
+                const double beta = ctl.beta64;
+                ctl.pAp = sums[2] + beta * sums[3] + beta * beta * sums[4];
+                if (!(ctl.pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
+                    ctl.indefinite = 1;
+                    ctl.iteration += 1;
+                } else {
+                    ctl.alpha64 = ctl.rz / ctl.pAp;
+                    ctl.alpha = (float)ctl.alpha64;
+                    ctl.beta = (float)beta;
+                    ctl.stop = 0;
+                }
             }
-            beta = sums[1] / rz;
-            rz = sums[1];
         }
-        pAp = sums[2] + beta * sums[3] + beta * beta * sums[4];
-        if (!(pAp > 0.0)) {  // indefinite (or NaN): stop as the reference does
-            indefinite = 1;
-            iteration += 1;
-            break;
-        }
-        alpha = rz / pAp;
+        __syncthreads();
+        if (ctl.stop) break;
     }
     staged_drain(B, ss, issued);  // stages copied ahead for a pass that will not run
     if (failed && threadIdx.x == 0) atomicExch(&B.state->wait_failed, 1);
     if (blockIdx.x == 0 && threadIdx.x == 0 && !failed) {
         PcgState* st = B.state;
-        st->iteration = iteration;
-        st->converged = converged;
-        st->indefinite = indefinite;
-        st->done = paused ? 0 : 1;
-        st->pAp = pAp;
-        st->alpha = alpha;
-        st->beta = beta;
-        st->rz = rz;
-        st->rr = rr;
-        st->error = error;
+        st->iteration = ctl.iteration;
+        st->converged = ctl.converged;
+        st->indefinite = ctl.indefinite;
+        st->done = ctl.paused ? 0 : 1;
+        st->pAp = ctl.pAp;
+        st->alpha = ctl.alpha64;
+        st->beta = ctl.beta64;
+        st->rz = ctl.rz;
+        st->rr = ctl.rr;
+        st->error = ctl.error;
     }
 }
 
