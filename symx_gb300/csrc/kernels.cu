@@ -1020,6 +1020,16 @@ __device__ __forceinline__ Row4<float> ld4cg(const float* p)
     const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
     return Row4<float>{v.x, v.y, v.z, v.w};
 }
+// The same cached in L1: the gathers of a product pass.  Neighbouring block rows share most of
+// their columns, so a chunk of rows gathers a few thousand bytes many times over, and L1 serves
+// the repeats instead of L2.  Valid for vectors written by other blocks before the last grid
+// barrier: its GPU-scope acquire (grid_barrier) invalidates the SM's L1, and nothing writes the
+// gathered vector during the pass.
+__device__ __forceinline__ Row4<float> ld4ca(const float* p)
+{
+    const float4 v = __ldca(reinterpret_cast<const float4*>(p));
+    return Row4<float>{v.x, v.y, v.z, v.w};
+}
 __device__ __forceinline__ Row4<float> direction_cg(const float* z, const float* p_old, float beta, bool first, int i)
 {
     const Row4<float> zz = ld4cg(z + 4 * i);
@@ -1092,9 +1102,10 @@ __global__ void __launch_bounds__(kSpmvThreads, SpmvMinBlocks<T>::value)
 // bounded: a wait that gives up marks the block aborted, the block stops issuing and
 // consuming, waits (bounded) for the copies it issued, and the solve is flagged in
 // PcgState::error.
-constexpr int kStagedConsumerWarps = 15;
+constexpr int kStagedConsumerWarps = 7;
 constexpr int kStagedThreads = 32 * (kStagedConsumerWarps + 1);  // warp 0: producer
-constexpr int kStagedRows = 4 * kStagedConsumerWarps;
+constexpr int kStagedRowsPerWarp = 8;                             // one block row per quad of lanes
+constexpr int kStagedRows = kStagedRowsPerWarp * kStagedConsumerWarps;
 constexpr int kStagedMaxStages = 8;
 // Bound of the drain waits (copies in flight before a block exits); the data waits use
 // B.staged.max_polls (wait_poll_limit()).
@@ -1215,6 +1226,59 @@ __device__ __forceinline__ void staged_init_barriers(const StagedShared& ss, int
     }
 }
 
+// Consumer side of the staged passes: the four lanes of a quad (q = lane & 3) take one block
+// row of a stage.  Lane q multiplies blocks q, q + 4, ... of the row (its range [kb, ke) of
+// the stage's value and column slots), four at a time with the four gathers in flight
+// together, and a transposing sum over the quad leaves component q of the row's product in
+// lane q (q < 3; lane 3 holds 0).  Per row this is a handful of warp instructions, where a
+// half-warp per row spent most of its instructions on the 16-lane sum and per-stage
+// bookkeeping.  Every lane of the warp must call it (the loop bound and the shuffles are
+// warp-wide); rows without blocks pass kb == ke.  The sum of component j is taken in one
+// fixed order.
+template <typename XV>
+__device__ __forceinline__ float quad_row_product(int kb, int ke, int q, const int32_t* __restrict__ scols,
+                                                  const float* __restrict__ svals, int CAP, XV xv)
+{
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    for (int base = kb + q; __any_sync(0xffffffffu, base < ke); base += 16) {
+        Row4<float> x[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) x[i] = base + 4 * i < ke ? xv(scols[base + 4 * i]) : Row4<float>{};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int k = base + 4 * i;
+            if (k < ke) {
+                a0 += svals[k] * x[i].x + svals[CAP + k] * x[i].y + svals[2 * CAP + k] * x[i].z;
+                a1 += svals[3 * CAP + k] * x[i].x + svals[4 * CAP + k] * x[i].y + svals[5 * CAP + k] * x[i].z;
+                a2 += svals[6 * CAP + k] * x[i].x + svals[7 * CAP + k] * x[i].y + svals[8 * CAP + k] * x[i].z;
+            }
+        }
+    }
+    const bool b2 = (q & 2) != 0, b1 = (q & 1) != 0;
+    const float w0 = (b2 ? a2 : a0) + __shfl_xor_sync(0xffffffffu, b2 ? a0 : a2, 2);
+    const float w1 = (b2 ? 0.f : a1) + __shfl_xor_sync(0xffffffffu, b2 ? a1 : 0.f, 2);
+    return (b1 ? w1 : w0) + __shfl_xor_sync(0xffffffffu, b1 ? w0 : w1, 1);
+}
+
+// Position of a consumer in the ring: stage number g, its slot and the parity of the slot's
+// phase, advanced without dividing by the stage count.
+struct RingCursor {
+    unsigned g, slot, parity;
+    __device__ __forceinline__ RingCursor(unsigned g0, int stages) : g(g0)
+    {
+        slot = g0 % (unsigned)stages;
+        parity = (g0 / (unsigned)stages) & 1u;
+    }
+    __device__ __forceinline__ void advance(int stages)
+    {
+        ++g;
+        if (++slot == (unsigned)stages) {
+            slot = 0;
+            parity ^= 1u;
+        }
+    }
+};
+
 // One pass of the staged product over this block's rows: p = z + beta p_old (fused into
 // the gathers; the owning lane stores p_new), q = A p, and this thread's share of p.q.
 // Stages are numbered over the whole launch (pass after pass; the matrix does not change):
@@ -1275,74 +1339,46 @@ __device__ __forceinline__ void staged_spmv_pass(const PcgBuffers<float>& B, con
             }
         }
     } else {
-        const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
+        const int cw = warp - 1, q = lane & 3, lr = kStagedRowsPerWarp * cw + (lane >> 2);
         const float* __restrict__ z = B.z;
         auto pv = [z, p_old, beta, first](int c) {
             return kCg ? direction_cg(z, p_old, beta, first, c) : direction(z, p_old, beta, first, c);
         };
+        RingCursor rc(seq, NS);
         for (int j = 0; j < n_stages; ++j) {
-            const unsigned g = seq + j, s = g % NS;
             // one decision per warp: the product below shuffles over the full warp
             const bool stop = __any_sync(
-                0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1, B.staged.max_polls));
+                0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[rc.slot]), rc.parity, B.staged.max_polls));
             if (stop) {
                 *abort_flag = 1;
                 break;
             }
-            const unsigned char* st = ss.stage0 + s * stage_bytes;
+            const unsigned char* st = ss.stage0 + rc.slot * stage_bytes;
             const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
             const int kb4 = rp[0] & ~3;
-            const int r0 = row_begin + j * S;
-            const int la = 4 * cw + half, lb = la + 2;
-            const int rowA = r0 + la, rowB = r0 + lb;
-            const bool vA = rowA < row_end, vB = rowB < row_end;
-            float a[3], b[3];
-            const int kbA = vA ? rp[la] - kb4 : 0, keA = vA ? rp[la + 1] - kb4 : 0;
-            const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
+            const int row = row_begin + j * S + lr;
+            const bool valid = row < row_end;
+            const int kb = valid ? rp[lr] - kb4 : 0, ke = valid ? rp[lr + 1] - kb4 : 0;
             const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
             const float* __restrict__ svals = reinterpret_cast<const float*>(st);
-            if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
-                // rows of at most 16 blocks: each lane takes at most one block of each row into
-                // registers and the stage is released before the gathers are issued (the
-                // arrive's release semantics would wait for them), so the ring slot is refilled
-                // while this warp waits on L2
-                const int kA = kbA + lane16, kB = kbB + lane16;
-                const bool hA = kA < keA, hB = kB < keB;
-                const int cA = hA ? scols[kA] : 0, cB = hB ? scols[kB] : 0;
-                float mA[9], mB[9];
-#pragma unroll
-                for (int m = 0; m < 9; ++m) {
-                    mA[m] = hA ? svals[m * CAP + kA] : 0.0f;
-                    mB[m] = hB ? svals[m * CAP + kB] : 0.0f;
-                }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
-                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
-                a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
-                a[1] = mA[3] * xA.x + mA[4] * xA.y + mA[5] * xA.z;
-                a[2] = mA[6] * xA.x + mA[7] * xA.y + mA[8] * xA.z;
-                b[0] = mB[0] * xB.x + mB[1] * xB.y + mB[2] * xB.z;
-                b[1] = mB[3] * xB.x + mB[4] * xB.y + mB[5] * xB.z;
-                b[2] = mB[6] * xB.x + mB[7] * xB.y + mB[8] * xB.z;
-            } else {
-                two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, pv, a, b);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+            const bool own = valid && q < 3;  // the lane that finishes component q of the row
+            const int64_t o = 4 * (int64_t)row + q;
+            float zo = 0.f, po = 0.f;
+            if (own) {
+                zo = kCg ? __ldcg(z + o) : z[o];
+                po = first ? 0.0f : (kCg ? __ldcg(p_old + o) : p_old[o]);
             }
-            const float qd = half_warp_transpose_sum<float>(a, b, lane16);
-            const int idx = lane16 >> 1;  // 0..2 row A, 3..5 row B
-            if (!(lane16 & 1) && idx < 6) {
-                const int row = idx < 3 ? rowA : rowB, d = idx % 3;
-                if (idx < 3 ? vA : vB) {
-                    const int64_t o = 4 * (int64_t)row + d;
-                    const float zo = kCg ? __ldcg(z + o) : z[o];
-                    const float po = first ? 0.0f : (kCg ? __ldcg(p_old + o) : p_old[o]);
-                    const float pd = first ? zo : fmaf(beta, po, zo);  // direction()'s bits
-                    p_new[o] = pd;
-                    B.q[o] = qd;
-                    pq.add_prod(pd, qd);
-                }
+            // the stage is released after its values are read, when its loads have returned
+            const float qd = quad_row_product(kb, ke, q, scols, svals, CAP, pv);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
+            if (own) {
+                const float pd = first ? zo : fmaf(beta, po, zo);  // direction()'s bits
+                p_new[o] = pd;
+                B.q[o] = qd;
+                pq.add_prod(pd, qd);
             }
+            rc.advance(NS);
         }
     }
     seq += n_stages;
@@ -1511,24 +1547,35 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
     if (warp == 0) {
         if (lane == 0) dyn_produce(B, ss, li, ctr, n_chunks, issued, P, abort_flag);
     } else {
-        const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
-        const int la = 4 * cw + half, lb = la + 2;
-        const int idx = lane16 >> 1;                 // epilogue: 0..2 row A, 3..5 row B
-        const bool owner = !(lane16 & 1) && idx < 6;  // the lane that finishes one component
+        const int cw = warp - 1, q = lane & 3, lr = kStagedRowsPerWarp * cw + (lane >> 2);
         const float* __restrict__ z = B.z;
         // The pass gathers z only and forms w = A z; the owning lane then sets
         // p = z + beta p_old and q = w + beta q_old (A p_old = q_old), half the gathered bytes
         // of forming A (z + beta p_old) directly.  Equal in exact arithmetic; in float the
         // recursive q differs from A p by rounding carried over iterations, which the outer
         // Newton loop's FP64 residual corrects like the rest of the FP32 solve's error.
-        auto pv = [z](int c) { return ld4cg(z + 4 * c); };
+        auto pv = [z](int c) { return ld4ca(z + 4 * c); };
         const int n = B.n_blocks;
-        // p.q of the last chunk, published during the next stage: warp sum in a fixed tree,
-        // then the last warp of the block to publish a chunk adds the 15 warp sums in warp
-        // order and stores the chunk's partial
+        // p.q of the last chunk, published at the start of the next stage (before its global
+        // loads, so the block-scope fence waits for no load): warp sum in a fixed tree, then
+        // the last warp of the block to publish a chunk adds the warp sums in warp order and
+        // stores the chunk's partial
         FF pend{0.f, 0.f};
         int pend_c = -1;
         unsigned pend_ps = 0;
+        // the last stage's p and q components, stored after its partial is published: the
+        // publication's block-scope fence then finds no store of this thread in flight (stores
+        // issued just before it would hold the warp for their L2 round trip)
+        bool pend_own = false;
+        int64_t pend_o = 0;
+        float pend_pd = 0.f, pend_qd = 0.f;
+        auto store_pending = [&]() {
+            if (pend_own) {
+                p_new[pend_o] = pend_pd;
+                B.q[pend_o] = pend_qd;  // only this lane reads and writes component o of q in a pass
+            }
+            pend_own = false;
+        };
         auto publish = [&]() {
             FF t = pend;
 #pragma unroll
@@ -1552,125 +1599,62 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
             }
             pend_c = -1;
         };
+        RingCursor rc(seq, NS);
         for (;;) {
-            const unsigned g = seq, s = g % NS;
             // one decision per warp: the product below shuffles over the full warp
             const bool stop = __any_sync(
-                0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1, B.staged.max_polls));
+                0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[rc.slot]), rc.parity, B.staged.max_polls));
             if (stop) {
                 *abort_flag = 1;
                 break;
             }
-            const int c = *(volatile int*)&ss.chunk[s];
-            seq = g + 1;
+            const int c = *(volatile int*)&ss.chunk[rc.slot];
             if (c < 0) {  // end of this pass
                 __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
                 if (pend_c >= 0) publish();
+                store_pending();
+                rc.advance(NS);
                 break;
             }
-            const int r0 = c * S;
-            const int rowA = r0 + la, rowB = r0 + lb;
-            const bool vA = rowA < n, vB = rowB < n;
-            const bool own = owner && (idx < 3 ? vA : vB);
-            const int64_t o = 4 * (int64_t)(idx < 3 ? rowA : rowB) + idx % 3;
-            const unsigned char* st = ss.stage0 + s * stage_bytes;
+            if (pend_c >= 0) publish();
+            store_pending();
+            const unsigned char* st = ss.stage0 + rc.slot * stage_bytes;
             const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
             const int kb4 = rp[0] & ~3;
-            float a[3], b[3];
-            const int kbA = vA ? rp[la] - kb4 : 0, keA = vA ? rp[la + 1] - kb4 : 0;
-            const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
+            const int row = c * S + lr;
+            const bool valid = row < n;
+            const int kb = valid ? rp[lr] - kb4 : 0, ke = valid ? rp[lr + 1] - kb4 : 0;
             const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
             const float* __restrict__ svals = reinterpret_cast<const float*>(st);
-            // The slot release (an mbarrier arrive, release semantics) and the partial's
-            // publication (a block-scope fence) wait for this thread's outstanding memory
-            // operations, so both go before any global load of this stage is issued.
+            const bool own = valid && q < 3;  // the lane that finishes component q of the row
+            const int64_t o = 4 * (int64_t)row + q;
             float zo = 0.f, po = 0.f, qo = 0.f;
-            if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
-                // rows of at most 16 blocks: each lane takes at most one block of each row into
-                // registers, releases the stage, then gathers
-                const int kA = kbA + lane16, kB = kbB + lane16;
-                const bool hA = kA < keA, hB = kB < keB;
-                const int cA = hA ? scols[kA] : 0, cB = hB ? scols[kB] : 0;
-                float mA[9], mB[9];
-#pragma unroll
-                for (int m = 0; m < 9; ++m) {
-                    mA[m] = hA ? svals[m * CAP + kA] : 0.0f;
-                    mB[m] = hB ? svals[m * CAP + kB] : 0.0f;
-                }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
-                if (pend_c >= 0) publish();
-                if (own) {
-                    zo = __ldcg(z + o);
-                    if (!first) {
-                        po = __ldcg(p_old + o);
-                        qo = __ldcg(B.q + o);
-                    }
-                }
-                const Row4<float> xA = hA ? pv(cA) : Row4<float>{}, xB = hB ? pv(cB) : Row4<float>{};
-                a[0] = mA[0] * xA.x + mA[1] * xA.y + mA[2] * xA.z;
-                a[1] = mA[3] * xA.x + mA[4] * xA.y + mA[5] * xA.z;
-                a[2] = mA[6] * xA.x + mA[7] * xA.y + mA[8] * xA.z;
-                b[0] = mB[0] * xB.x + mB[1] * xB.y + mB[2] * xB.z;
-                b[1] = mB[3] * xB.x + mB[4] * xB.y + mB[5] * xB.z;
-                b[2] = mB[6] * xB.x + mB[7] * xB.y + mB[8] * xB.z;
-            } else if (__all_sync(0xffffffffu, keA - kbA <= 32 && keB - kbB <= 32)) {
-                // rows of at most 32 blocks (Hex8: 27): two blocks of each row per lane, the four
-                // gathers issued together, values read from the stage after they arrive (the
-                // stage is released after the products)
-                if (pend_c >= 0) publish();
-                const int kA0 = kbA + lane16, kA1 = kA0 + 16, kB0 = kbB + lane16, kB1 = kB0 + 16;
-                const bool hA0 = kA0 < keA, hA1 = kA1 < keA, hB0 = kB0 < keB, hB1 = kB1 < keB;
-                const Row4<float> xA0 = hA0 ? pv(scols[kA0]) : Row4<float>{}, xA1 = hA1 ? pv(scols[kA1]) : Row4<float>{};
-                const Row4<float> xB0 = hB0 ? pv(scols[kB0]) : Row4<float>{}, xB1 = hB1 ? pv(scols[kB1]) : Row4<float>{};
-                auto prod = [&](int k, bool h, const Row4<float>& x, float (&acc)[3]) {
-                    if (!h) return;
-#pragma unroll
-                    for (int r = 0; r < 3; ++r)
-                        acc[r] += svals[(3 * r) * CAP + k] * x.x + svals[(3 * r + 1) * CAP + k] * x.y +
-                                  svals[(3 * r + 2) * CAP + k] * x.z;
-                };
-                a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = 0.0f;
-                prod(kA0, hA0, xA0, a);
-                prod(kA1, hA1, xA1, a);
-                prod(kB0, hB0, xB0, b);
-                prod(kB1, hB1, xB1, b);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
-                if (own) {
-                    zo = __ldcg(z + o);
-                    if (!first) {
-                        po = __ldcg(p_old + o);
-                        qo = __ldcg(B.q + o);
-                    }
-                }
-            } else {
-                if (pend_c >= 0) publish();
-                two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, pv, a, b);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
-                if (own) {
-                    zo = __ldcg(z + o);
-                    if (!first) {
-                        po = __ldcg(p_old + o);
-                        qo = __ldcg(B.q + o);
-                    }
+            if (own) {
+                zo = __ldcg(z + o);
+                if (!first) {
+                    po = __ldcg(p_old + o);
+                    qo = __ldcg(B.q + o);
                 }
             }
-            const float wd = half_warp_transpose_sum<float>(a, b, lane16);
+            // the stage is released after its values are read, when its loads have returned
+            const float wd = quad_row_product(kb, ke, q, scols, svals, CAP, pv);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
             FF t{0.f, 0.f};
             if (own) {
-                const float pd = first ? zo : fmaf(beta, po, zo);
-                const float qd = first ? wd : fmaf(beta, qo, wd);
-                p_new[o] = pd;
-                B.q[o] = qd;  // only this lane reads and writes component o of q in a pass
-                t = ff_prod(pd, qd);
+                pend_pd = first ? zo : fmaf(beta, po, zo);
+                pend_qd = first ? wd : fmaf(beta, qo, wd);
+                pend_o = o;
+                t = ff_prod(pend_pd, pend_qd);
             }
+            pend_own = own;
             pend = t;
             pend_c = c;
-            pend_ps = g % kStagedPartSlots;
+            pend_ps = rc.g % kStagedPartSlots;
+            rc.advance(NS);
         }
+        seq = rc.g;
     }
 }
 
@@ -1733,13 +1717,13 @@ __device__ double sum_chunk_partials(const float2* part, int n, double* sh)
 {
     FF a{0.f, 0.f};
     int i = threadIdx.x;
-    for (; i + 3 * (int)blockDim.x < n; i += 4 * blockDim.x) {
-        const float2 v0 = __ldcg(part + i), v1 = __ldcg(part + i + blockDim.x), v2 = __ldcg(part + i + 2 * blockDim.x),
-                     v3 = __ldcg(part + i + 3 * blockDim.x);
-        a = ff_add(a, FF{v0.x, v0.y});
-        a = ff_add(a, FF{v1.x, v1.y});
-        a = ff_add(a, FF{v2.x, v2.y});
-        a = ff_add(a, FF{v3.x, v3.y});
+    constexpr int U = 8;  // loads in flight per thread
+    for (; i + (U - 1) * (int)blockDim.x < n; i += U * blockDim.x) {
+        float2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = __ldcg(part + i + u * blockDim.x);
+#pragma unroll
+        for (int u = 0; u < U; ++u) a = ff_add(a, FF{v[u].x, v[u].y});
     }
     for (; i < n; i += blockDim.x) {
         const float2 v = __ldcg(part + i);
@@ -1921,7 +1905,9 @@ struct PcgCtl {
     // thread 0's FP64 recurrence and outcome (in shared memory, so the other threads hold no
     // registers for it)
     double rz, alpha64, beta64, pAp, rr, error;
+    double thr_abs, thr_rel;  // the convergence test on r.r (no square root per iteration)
     int iteration, converged, indefinite, paused;
+    int have_rr;  // rr holds a residual of this launch
 };
 
 // Chunks of the persistent kernel's product pass (one stage of rows each).
@@ -1969,8 +1955,11 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         ctl.pAp = ctl.rr = 0.0;
         ctl.error = st0.error;
         ctl.iteration = st0.iteration;
-        ctl.converged = ctl.indefinite = ctl.paused = 0;
+        ctl.converged = ctl.indefinite = ctl.paused = ctl.have_rr = 0;
         ctl.beta = (float)ctl.beta64;
+        // sqrt(rr / bb) < abs_tol  and  sqrt(rr / bb) / error0 < rel_tol, as comparisons of rr
+        ctl.thr_abs = st0.abs_tol * st0.abs_tol * st0.bb;
+        ctl.thr_rel = st0.rel_tol * st0.error0 * st0.rel_tol * st0.error0 * st0.bb;
     }
     __syncthreads();
     int iteration = st0.iteration;
@@ -2006,30 +1995,49 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         if (ctl.stop) break;
         const float a = ctl.alpha;
         DotAcc<float> rra, rza;
-        // one row per thread and pass, all its loads (preconditioner block included) issued
-        // before its math
-        for (int i = row_begin + (int)threadIdx.x; i < row_end; i += blockDim.x) {
-            Row4<float> x = ld4(B.x + 4 * i), r = ld4(B.r + 4 * i);
-            const Row4<float> pp = ld4(p_new + 4 * i), q = ld4(B.q + 4 * i);
-            const Row4<float> m0 = ld4(B.Dinv + 12 * (int64_t)i), m1 = ld4(B.Dinv + 12 * (int64_t)i + 4),
-                              m2 = ld4(B.Dinv + 12 * (int64_t)i + 8);
-            x.x = fmaf(a, pp.x, x.x);
-            x.y = fmaf(a, pp.y, x.y);
-            x.z = fmaf(a, pp.z, x.z);
-            r.x = fmaf(-a, q.x, r.x);
-            r.y = fmaf(-a, q.y, r.y);
-            r.z = fmaf(-a, q.z, r.z);
-            const Row4<float> z{m0.x * r.x + m0.y * r.y + m0.z * r.z, m1.x * r.x + m1.y * r.y + m1.z * r.z,
-                                m2.x * r.x + m2.y * r.y + m2.z * r.z, 0.0f};
-            st4(B.x + 4 * i, x);
-            st4(B.r + 4 * i, r);
-            st4(B.z + 4 * i, z);
-            rra.add_prod(r.x, r.x);
-            rra.add_prod(r.y, r.y);
-            rra.add_prod(r.z, r.z);
-            rza.add_prod(r.x, z.x);
-            rza.add_prod(r.y, z.y);
-            rza.add_prod(r.z, z.z);
+        // two rows per thread and pass (rows i and i + blockDim.x, summed in that order, as a
+        // row-by-row loop would), all their loads (preconditioner blocks included) issued
+        // before their math
+        for (int i = row_begin + (int)threadIdx.x; i < row_end; i += 2 * blockDim.x) {
+            const int i2 = i + (int)blockDim.x;
+            const bool h2 = i2 < row_end;
+            Row4<float> x[2], r[2], pp[2], q[2], m0[2], m1[2], m2[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int k = u ? i2 : i;
+                if (u == 0 || h2) {
+                    x[u] = ld4(B.x + 4 * k);
+                    r[u] = ld4(B.r + 4 * k);
+                    pp[u] = ld4(p_new + 4 * k);
+                    q[u] = ld4(B.q + 4 * k);
+                    m0[u] = ld4(B.Dinv + 12 * (int64_t)k);
+                    m1[u] = ld4(B.Dinv + 12 * (int64_t)k + 4);
+                    m2[u] = ld4(B.Dinv + 12 * (int64_t)k + 8);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (u == 1 && !h2) break;
+                const int k = u ? i2 : i;
+                x[u].x = fmaf(a, pp[u].x, x[u].x);
+                x[u].y = fmaf(a, pp[u].y, x[u].y);
+                x[u].z = fmaf(a, pp[u].z, x[u].z);
+                r[u].x = fmaf(-a, q[u].x, r[u].x);
+                r[u].y = fmaf(-a, q[u].y, r[u].y);
+                r[u].z = fmaf(-a, q[u].z, r[u].z);
+                const Row4<float> z{m0[u].x * r[u].x + m0[u].y * r[u].y + m0[u].z * r[u].z,
+                                    m1[u].x * r[u].x + m1[u].y * r[u].y + m1[u].z * r[u].z,
+                                    m2[u].x * r[u].x + m2[u].y * r[u].y + m2[u].z * r[u].z, 0.0f};
+                st4(B.x + 4 * k, x[u]);
+                st4(B.r + 4 * k, r[u]);
+                st4(B.z + 4 * k, z);
+                rra.add_prod(r[u].x, r[u].x);
+                rra.add_prod(r[u].y, r[u].y);
+                rra.add_prod(r[u].z, r[u].z);
+                rza.add_prod(r[u].x, z.x);
+                rza.add_prod(r[u].y, z.y);
+                rza.add_prod(r[u].z, z.z);
+            }
         }
         FF brr, brz;
         block_sum2_ff(rra.v, rza.v, sh, brr, brz);
@@ -2058,8 +2066,8 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
             ctl.stop = 1;
             ctl.iteration = iteration;
             ctl.rr = rr;
-            ctl.error = sqrt(rr / st0.bb);
-            if (ctl.error < st0.abs_tol || ctl.error / st0.error0 < st0.rel_tol) {
+            ctl.have_rr = 1;
+            if (rr < ctl.thr_abs || rr < ctl.thr_rel) {
                 ctl.converged = 1;
             } else if (iteration >= st0.max_iterations) {
             } else if (st0.replace_every > 0 && iteration % st0.replace_every == 0) {
@@ -2088,7 +2096,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         st->beta = ctl.beta64;
         st->rz = ctl.rz;
         st->rr = ctl.rr;
-        st->error = ctl.error;
+        st->error = ctl.have_rr ? sqrt(ctl.rr / st0.bb) : st0.error;
     }
 }
 
@@ -2255,61 +2263,54 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
     const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
     const size_t stage_bytes = staged_stage_bytes(CAP, S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int cw = warp - 1, lane16 = lane & 15, half = (lane >> 4) & 1;
-    const int la = 4 * cw + half, lb = la + 2;
-    const int idx = lane16 >> 1;                  // epilogue: 0..2 row A, 3..5 row B
-    const bool owner = !(lane16 & 1) && idx < 6;  // the lane that finishes one component
-    const int d = idx % 3;
-    const int wbase = (lane & 16) + (idx < 3 ? 0 : 6);  // lanes holding this row's w components
+    const int cw = warp - 1, q = lane & 3, lr = kStagedRowsPerWarp * cw + (lane >> 2);
+    const int qb = lane & ~3;  // first lane of this quad: components 0..2 of its row in qb .. qb + 2
     const int n = B.n_blocks;
     auto gather = [&](int c) {
         if constexpr (kEntry) {
-            return ld4cg(V.z + 4 * c);
+            return ld4ca(V.z + 4 * c);
         } else {
-            const Row4<float> z = ld4cg(V.z + 4 * c), mw = ld4cg(V.mw + 4 * c), mq = ld4cg(V.mq + 4 * c);
+            const Row4<float> z = ld4ca(V.z + 4 * c), mw = ld4ca(V.mw + 4 * c), mq = ld4ca(V.mq + 4 * c);
             return Row4<float>{la_znext(z.x, mw.x, mq.x, alpha, beta), la_znext(z.y, mw.y, mq.y, alpha, beta),
                                la_znext(z.z, mw.z, mq.z, alpha, beta), 0.f};
         }
     };
+    RingCursor rc(seq, NS);
     for (;;) {
-        const unsigned g = seq, s = g % NS;
         // one decision per warp: the product below shuffles over the full warp
         const bool stop = __any_sync(
-            0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[s]), (g / NS) & 1, B.staged.max_polls));
+            0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[rc.slot]), rc.parity, B.staged.max_polls));
         if (stop) {
             *abort_flag = 1;
             break;
         }
-        const int c = *(volatile int*)&ss.chunk[s];
-        seq = g + 1;
+        const int c = *(volatile int*)&ss.chunk[rc.slot];
         if (c < 0) {  // end of this pass
             __syncwarp();
-            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
+            if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
+            rc.advance(NS);
             break;
         }
-        const int r0 = c * S;
-        const int rowA = r0 + la, rowB = r0 + lb;
-        const bool vA = rowA < n, vB = rowB < n;
-        const bool own = owner && (idx < 3 ? vA : vB);
-        const int orow = idx < 3 ? rowA : rowB;
-        const int64_t o = 4 * (int64_t)orow + d;
-        const unsigned char* st = ss.stage0 + s * stage_bytes;
+        const int row = c * S + lr;
+        const bool valid = row < n;
+        const bool own = valid && q < 3;  // the lane that finishes component q of the row
+        const int64_t o = 4 * (int64_t)row + q;
+        const unsigned char* st = ss.stage0 + rc.slot * stage_bytes;
         const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
         const int kb4 = rp[0] & ~3;
-        const int kbA = vA ? rp[la] - kb4 : 0, keA = vA ? rp[la + 1] - kb4 : 0;
-        const int kbB = vB ? rp[lb] - kb4 : 0, keB = vB ? rp[lb + 1] - kb4 : 0;
+        const int kb = valid ? rp[lr] - kb4 : 0, ke = valid ? rp[lr + 1] - kb4 : 0;
         const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
         const float* __restrict__ svals = reinterpret_cast<const float*>(st);
         // the owner's row values (written by other blocks in the previous pass: L2 loads)
         float zp = 0.f, po = 0.f, qo = 0.f, wo = 0.f, xo = 0.f, ro = 0.f;
         Row4<float> dv{}, qrow{};
         if (own) {
-            dv = ld4(B.Dinv + 12 * (int64_t)orow + 4 * d);
+            dv = ld4(B.Dinv + 12 * (int64_t)row + 4 * q);
             zp = __ldcg(V.z + o);
             if constexpr (kEntry) {
                 if (!first) {
                     po = __ldcg(B.p + o);
-                    qrow = ld4cg(B.q + 4 * (int64_t)orow);
+                    qrow = ld4cg(B.q + 4 * (int64_t)row);
                 }
             } else {
                 po = __ldcg(B.p + o);
@@ -2319,78 +2320,49 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
                 ro = __ldcg(B.r + o);
             }
         }
-        float a[3], b[3];
-        if (__all_sync(0xffffffffu, keA - kbA <= 16 && keB - kbB <= 16)) {
-            // rows of at most 16 blocks: one block of each row per lane, both gathers in
-            // flight with the owner's loads; the values are read after they return
-            const int kA = kbA + lane16, kB = kbB + lane16;
-            const bool hA = kA < keA, hB = kB < keB;
-            const Row4<float> xA = hA ? gather(scols[kA]) : Row4<float>{};
-            const Row4<float> xB = hB ? gather(scols[kB]) : Row4<float>{};
-            a[0] = a[1] = a[2] = b[0] = b[1] = b[2] = 0.f;
-            if (hA) {
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    a[r] = svals[(3 * r) * CAP + kA] * xA.x + svals[(3 * r + 1) * CAP + kA] * xA.y +
-                           svals[(3 * r + 2) * CAP + kA] * xA.z;
-            }
-            if (hB) {
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    b[r] = svals[(3 * r) * CAP + kB] * xB.x + svals[(3 * r + 1) * CAP + kB] * xB.y +
-                           svals[(3 * r + 2) * CAP + kB] * xB.z;
-            }
-        } else {
-            two_range_products<float>(kbA, keA, kbB, keB, lane16, scols, svals, StridedBcsr{CAP}, gather, a, b);
-        }
+        // the stage is released after its values are read, when its loads have returned
+        const float wd = quad_row_product(kb, ke, q, scols, svals, CAP, gather);
         __syncwarp();
-        if (lane == 0) mbar_arrive(smem_addr(&ss.empty[s]));
-        const float wd = half_warp_transpose_sum<float>(a, b, lane16);
-        const float w0 = __shfl_sync(0xffffffffu, wd, wbase), w1 = __shfl_sync(0xffffffffu, wd, wbase + 2),
-                    w2 = __shfl_sync(0xffffffffu, wd, wbase + 4);
+        if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
+        const float w0 = __shfl_sync(0xffffffffu, wd, qb), w1 = __shfl_sync(0xffffffffu, wd, qb + 1),
+                    w2 = __shfl_sync(0xffffffffu, wd, qb + 2);
         FF t[kLaSums];
 #pragma unroll
         for (int k = 0; k < kLaSums; ++k) t[k] = FF{0.f, 0.f};
+        float sv[7];  // the owner's stores, issued after the partials are published
         if constexpr (kEntry) {
             if (own) {
                 const float mwd = dv.x * w0 + dv.y * w1 + dv.z * w2;
                 const float mqd = first ? 0.f : dv.x * qrow.x + dv.y * qrow.y + dv.z * qrow.z;
-                const float qd = first ? 0.f : (d == 0 ? qrow.x : d == 1 ? qrow.y : qrow.z);
-                V.zo[o] = zp;
-                V.mwo[o] = mwd;
-                V.mqo[o] = mqd;
-                V.w[o] = wd;
-                if (first) {  // no earlier direction: p = q = 0 for the first update
-                    B.p[o] = 0.f;
-                    B.q[o] = 0.f;
-                }
+                const float qd = first ? 0.f : (q == 0 ? qrow.x : q == 1 ? qrow.y : qrow.z);
                 t[2] = ff_prod(zp, wd);
                 t[3] = ff_add(ff_prod(zp, qd), ff_prod(po, wd));
                 t[4] = ff_prod(po, qd);
+                sv[0] = zp;
+                sv[1] = mwd;
+                sv[2] = mqd;
             }
-        }
-        if constexpr (!kEntry) {
+        } else {
             // every lane takes part in the shuffles (non-owners carry zeros)
             const float pd = __fmaf_rn(beta, po, zp);
             const float qd = __fmaf_rn(beta, qo, wo);
             const float xd = __fmaf_rn(alpha, pd, xo);
             const float rd = __fmaf_rn(-alpha, qd, ro);
-            const float r0 = __shfl_sync(0xffffffffu, rd, wbase), r1 = __shfl_sync(0xffffffffu, rd, wbase + 2),
-                        r2 = __shfl_sync(0xffffffffu, rd, wbase + 4);
-            const float q0 = __shfl_sync(0xffffffffu, qd, wbase), q1 = __shfl_sync(0xffffffffu, qd, wbase + 2),
-                        q2 = __shfl_sync(0xffffffffu, qd, wbase + 4);
+            const float r0 = __shfl_sync(0xffffffffu, rd, qb), r1 = __shfl_sync(0xffffffffu, rd, qb + 1),
+                        r2 = __shfl_sync(0xffffffffu, rd, qb + 2);
+            const float q0 = __shfl_sync(0xffffffffu, qd, qb), q1 = __shfl_sync(0xffffffffu, qd, qb + 1),
+                        q2 = __shfl_sync(0xffffffffu, qd, qb + 2);
             if (own) {
                 const float mwd = dv.x * w0 + dv.y * w1 + dv.z * w2;
                 const float zd = dv.x * r0 + dv.y * r1 + dv.z * r2;
                 const float mqd = dv.x * q0 + dv.y * q1 + dv.z * q2;
-                V.zo[o] = zd;
-                V.mwo[o] = mwd;
-                V.mqo[o] = mqd;
-                V.w[o] = wd;
-                B.p[o] = pd;
-                B.q[o] = qd;
-                B.x[o] = xd;
-                B.r[o] = rd;
+                sv[0] = zd;
+                sv[1] = mwd;
+                sv[2] = mqd;
+                sv[3] = pd;
+                sv[4] = qd;
+                sv[5] = xd;
+                sv[6] = rd;
                 t[0] = ff_prod(rd, rd);
                 t[1] = ff_prod(rd, zd);
                 t[2] = ff_prod(zd, wd);
@@ -2398,8 +2370,28 @@ __device__ __forceinline__ void la_consume(const PcgBuffers<float>& B, const Sta
                 t[4] = ff_prod(pd, qd);
             }
         }
-        la_publish<kF64Sums>(t, ss, g % (unsigned)(NS + 1), cw, c, n_chunks, part);
+        // publish first: its block-scope fence then waits for no store of this stage
+        la_publish<kF64Sums>(t, ss, rc.g % (unsigned)(NS + 1), cw, c, n_chunks, part);
+        if (own) {
+            V.zo[o] = sv[0];
+            V.mwo[o] = sv[1];
+            V.mqo[o] = sv[2];
+            V.w[o] = wd;
+            if constexpr (kEntry) {
+                if (first) {  // no earlier direction: p = q = 0 for the first update
+                    B.p[o] = 0.f;
+                    B.q[o] = 0.f;
+                }
+            } else {
+                B.p[o] = sv[3];
+                B.q[o] = sv[4];
+                B.x[o] = sv[5];
+                B.r[o] = sv[6];
+            }
+        }
+        rc.advance(NS);
     }
+    seq = rc.g;
 }
 
 // Fixed-order sums of the kLaSums chunk partial arrays (value-major, n each), returned to every
@@ -2422,7 +2414,20 @@ __device__ void la_sum_partials(const double* part, int n, double* sh, double (&
         FF a[kLaSums];
 #pragma unroll
         for (int k = 0; k < kLaSums; ++k) a[k] = FF{0.f, 0.f};
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int i = threadIdx.x;
+        constexpr int U = 4;  // chunks per thread in flight (kLaSums loads each)
+        for (; i + (U - 1) * (int)blockDim.x < n; i += U * blockDim.x) {
+            float2 v[U][kLaSums];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int k = 0; k < kLaSums; ++k) v[u][k] = __ldcg(p2 + (size_t)k * n + i + u * blockDim.x);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int k = 0; k < kLaSums; ++k) a[k] = ff_add(a[k], FF{v[u][k].x, v[u][k].y});
+        }
+        for (; i < n; i += blockDim.x) {
             float2 v[kLaSums];
 #pragma unroll
             for (int k = 0; k < kLaSums; ++k) v[k] = __ldcg(p2 + (size_t)k * n + i);
@@ -2499,7 +2504,9 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<f
         ctl.pAp = ctl.rr = 0.0;
         ctl.error = st0.error;
         ctl.iteration = st0.iteration;
-        ctl.converged = ctl.indefinite = ctl.paused = 0;
+        ctl.converged = ctl.indefinite = ctl.paused = ctl.have_rr = 0;
+        ctl.thr_abs = st0.abs_tol * st0.abs_tol * st0.bb;
+        ctl.thr_rel = st0.rel_tol * st0.error0 * st0.rel_tol * st0.error0 * st0.bb;
     }
     bool failed = false;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2527,8 +2534,8 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<f
             if (li > 0) {  // the pass formed x_k and r_k: the reference's test after its update
                 ctl.iteration += 1;
                 ctl.rr = sums[0];
-                ctl.error = sqrt(ctl.rr / st0.bb);
-                if (ctl.error < st0.abs_tol || ctl.error / st0.error0 < st0.rel_tol) {
+                ctl.have_rr = 1;
+                if (ctl.rr < ctl.thr_abs || ctl.rr < ctl.thr_rel) {
                     ctl.converged = 1;
                     go = false;
                 } else if (ctl.iteration >= st0.max_iterations) {
@@ -2571,7 +2578,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_la(PcgBuffers<f
         st->beta = ctl.beta64;
         st->rz = ctl.rz;
         st->rr = ctl.rr;
-        st->error = ctl.error;
+        st->error = ctl.have_rr ? sqrt(ctl.rr / st0.bb) : st0.error;
     }
 }
 
