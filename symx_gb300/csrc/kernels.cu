@@ -1179,19 +1179,6 @@ __host__ __device__ __forceinline__ size_t staged_stage_bytes(int cap, int stage
 // then the ring of stages.  The chunk slots and partials are used by the persistent kernel.
 constexpr int kStagedPartSlots = 2 * kStagedMaxStages;
 
-// B.partials of the persistent kernel with FP64 sums, in doubles: chunk partials of p.Ap, then
-// the r.r and r.z block partials.
-struct PcgSumsLayout {
-    int rr, rz, total;
-};
-__host__ __device__ __forceinline__ PcgSumsLayout pcg_sums_layout(int n_chunks, int grid)
-{
-    PcgSumsLayout L;
-    L.rr = n_chunks;
-    L.rz = L.rr + grid;
-    L.total = L.rz + grid;
-    return L;
-}
 constexpr size_t kStagedHeaderBytes =
     (16 * kStagedMaxStages + 4 * kStagedMaxStages + 4 * kStagedPartSlots +
      8 * kStagedPartSlots * kStagedConsumerWarps + 127) / 128 * 128;
@@ -1396,7 +1383,7 @@ __device__ __forceinline__ void staged_drain(const PcgBuffers<float>& B, const S
         mbar_wait(smem_addr(&ss.full[g % NS]), (g / NS) & 1);
 }
 
-// ---- dynamic schedule of the persistent kernel's product pass
+// ---- dynamic schedule of the look-ahead kernel's product pass
 // The rows are cut into chunks of stage_rows rows (one stage each).  In every pass the
 // blocks claim chunks, kClaimChunks at a time, from a counter of that pass (atomicAdd; a
 // value past the last chunk ends the block's pass), so a block on a slower SM simply takes
@@ -1405,15 +1392,13 @@ __device__ __forceinline__ void staged_drain(const PcgBuffers<float>& B, const S
 // claim's round trip, and the load of the next unit's row range after it, overlap the waits
 // for ring slots.  After the end marker of pass li it runs on into pass li + 1 until the
 // ring is full; it never claims from a pass beyond li + 1.  Three counters rotate (pass k
-// uses ctr[k % 3]); ctr[(li + 2) % 3] is cleared by block 0 between the two grid barriers of
-// pass li, when no block can still claim from pass li - 1 and none can claim from pass
-// li + 2 yet.
+// uses ctr[k % 3]); ctr[(li + 2) % 3] is cleared by block 0 during pass li, when no block can
+// still claim from pass li - 1 and none can claim from pass li + 2 yet.
 //
-// p.q stays bitwise reproducible: each consumer warp sums its products of a chunk in a fixed
-// shuffle tree, the last of the 15 warps to finish a chunk adds the warp sums in warp order
-// and stores the chunk's float-float sum at part[chunk], and after the barrier every block
-// adds part[0 .. n_chunks) in one fixed order.  None of it depends on which block took which
-// chunk.
+// The sums stay bitwise reproducible: each consumer warp sums its products of a chunk in a
+// fixed shuffle tree, the last warp to finish a chunk adds the warp sums in a fixed order and
+// stores the chunk's partials, and after the barrier every block adds them in chunk order.
+// None of it depends on which block took which chunk.
 constexpr int kClaimChunks = 1;
 struct DynProducer {
     int it = 0;         // pass of the next stage to issue
@@ -1444,16 +1429,6 @@ __device__ __forceinline__ void dyn_take(const PcgBuffers<float>& B, int n_chunk
 #pragma unroll
     for (int k = 0; k <= kClaimChunks; ++k)
         if (P.unit0 + k <= P.unit_end) P.rp[k] = __ldcg(B.staged.row_ptr_ext + (P.unit0 + k) * S);
-}
-
-// Where the product pass leaves p.q: one partial per chunk in B.partials (pcg_sums_layout),
-// summed after the barrier by every block in chunk order, so p.q does not depend on which
-// block took which chunk.  FF sums: the partials are float-float and are summed in
-// float-float.  FP64 sums: each chunk's float-float sum is converted to double (exactly) and
-// the partials are summed in FP64.
-__device__ __forceinline__ void publish_chunk_f64(double* partials, int c, float hi, float lo)
-{
-    partials[c] = (double)hi + (double)lo;
 }
 
 // Producer thread of a dynamically scheduled pass li (see above): claims chunks, copies each
@@ -1535,72 +1510,70 @@ __device__ __forceinline__ void dyn_produce(const PcgBuffers<float>& B, const St
     }
 }
 
-template <bool kF64Sums>
-__device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B, const StagedShared& ss, int li,
-                                                     unsigned* ctr, int n_chunks, const float* __restrict__ p_old,
-                                                     float* __restrict__ p_new, bool first, float beta, unsigned& seq,
-                                                     unsigned& issued, DynProducer& P, volatile int* abort_flag)
+// One pass of the persistent kernel's product over this block's own rows [row_begin,
+// row_end) (an even split; stages of S rows, the last one shorter), z gathered alone: the
+// owning lane forms p = z + beta p_old and q = A z + beta q_old (A p_old = q_old), half the
+// gathered bytes of forming A (z + beta p_old) directly.  Equal in exact arithmetic; in float
+// the recursive q differs from A p by rounding carried over iterations, which the outer Newton
+// loop's FP64 residual corrects like the rest of the FP32 solve's error.  The producer runs
+// on into the next pass's stages (the same rows: the matrix does not change) until the ring is
+// full, so a pass starts on stages already in shared memory.  Contiguous rows per block keep
+// the z rows gathered by consecutive stages overlapping, so many gathers hit L1.  Each thread
+// accumulates its share of p.q; nothing is published per stage, so the loop holds no fence.
+__device__ __forceinline__ void staged_pass_rows(const PcgBuffers<float>& B, const StagedShared& ss, int row_begin,
+                                                 int row_end, const float* __restrict__ p_old,
+                                                 float* __restrict__ p_new, bool first, float beta, unsigned& seq,
+                                                 unsigned& issued, volatile int* abort_flag, DotAcc<float>& pq)
 {
     const int S = B.staged.stage_rows, CAP = B.staged.stage_cap, NS = B.staged.stages;
     const size_t stage_bytes = staged_stage_bytes(CAP, S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_stages = (row_end - row_begin + S - 1) / S;
+    if (n_stages <= 0) return;
     if (warp == 0) {
-        if (lane == 0) dyn_produce(B, ss, li, ctr, n_chunks, issued, P, abort_flag);
+        if (lane == 0) {
+            const unsigned last = seq + n_stages + NS;  // one past the last stage to copy now
+            auto range = [&](unsigned g, int& r0, int& kb, int& ke) {
+                r0 = row_begin + (int)(g % (unsigned)n_stages) * S;
+                kb = B.staged.row_ptr_ext[r0];
+                ke = B.staged.row_ptr_ext[min(r0 + S, row_end)];
+            };
+            const uint64_t pol = l2_evict_first_policy();
+            int next_r0 = 0, next_kb = 0, next_ke = 0;
+            if (issued < last) range(issued, next_r0, next_kb, next_ke);
+            for (unsigned g = issued; g < last && !*abort_flag; ++g) {
+                const unsigned s = g % NS, use = g / NS;
+                const int r0 = next_r0, kb = next_kb, ke = next_ke;
+                if (g + 1 < last) range(g + 1, next_r0, next_kb, next_ke);  // overlaps the slot wait
+                if (r0 & 3) {  // row_ptr copies need a 16-byte aligned start (pcg_block_rows)
+                    *abort_flag = 1;
+                    break;
+                }
+                if (use > 0 && !mbar_wait(smem_addr(&ss.empty[s]), (use - 1) & 1, B.staged.max_polls)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                const int kb4 = kb & ~3, ke4 = (ke + 3) & ~3;
+                const uint32_t span = (uint32_t)(ke4 - kb4) * 4u;
+                unsigned char* st = ss.stage0 + s * stage_bytes;
+                const uint32_t fb = smem_addr(&ss.full[s]);
+                mbar_arrive_expect_tx(fb, 10u * span + (uint32_t)(S + 4) * 4u);
+                if (span) {
+                    for (int m = 0; m < 9; ++m)
+                        bulk_copy_g2s_stream(smem_addr(st + (size_t)m * CAP * 4), B.vals + m * B.vals_stride + kb4,
+                                             span, fb, pol);
+                    bulk_copy_g2s_stream(smem_addr(st + (size_t)9 * CAP * 4), B.staged.cols_ext + kb4, span, fb, pol);
+                }
+                bulk_copy_g2s(smem_addr(st + (size_t)10 * CAP * 4), B.staged.row_ptr_ext + r0, (uint32_t)(S + 4) * 4u, fb);
+                issued = g + 1;
+            }
+        }
     } else {
         const int cw = warp - 1, q = lane & 3, lr = kStagedRowsPerWarp * cw + (lane >> 2);
         const float* __restrict__ z = B.z;
-        // The pass gathers z only and forms w = A z; the owning lane then sets
-        // p = z + beta p_old and q = w + beta q_old (A p_old = q_old), half the gathered bytes
-        // of forming A (z + beta p_old) directly.  Equal in exact arithmetic; in float the
-        // recursive q differs from A p by rounding carried over iterations, which the outer
-        // Newton loop's FP64 residual corrects like the rest of the FP32 solve's error.
         auto pv = [z](int c) { return ld4ca(z + 4 * c); };
-        const int n = B.n_blocks;
-        // p.q of the last chunk, published at the start of the next stage (before its global
-        // loads, so the block-scope fence waits for no load): warp sum in a fixed tree, then
-        // the last warp of the block to publish a chunk adds the warp sums in warp order and
-        // stores the chunk's partial
-        FF pend{0.f, 0.f};
-        int pend_c = -1;
-        unsigned pend_ps = 0;
-        // the last stage's p and q components, stored after its partial is published: the
-        // publication's block-scope fence then finds no store of this thread in flight (stores
-        // issued just before it would hold the warp for their L2 round trip)
-        bool pend_own = false;
-        int64_t pend_o = 0;
-        float pend_pd = 0.f, pend_qd = 0.f;
-        auto store_pending = [&]() {
-            if (pend_own) {
-                p_new[pend_o] = pend_pd;
-                B.q[pend_o] = pend_qd;  // only this lane reads and writes component o of q in a pass
-            }
-            pend_own = false;
-        };
-        auto publish = [&]() {
-            FF t = pend;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_down(t, o));
-            if (lane == 0) {
-                volatile float2* wp = ss.wpart + pend_ps * kStagedConsumerWarps;
-                wp[cw].x = t.hi;
-                wp[cw].y = t.lo;
-                __threadfence_block();
-                if (atomicAdd(&ss.wcount[pend_ps], 1u) == kStagedConsumerWarps - 1) {
-                    __threadfence_block();
-                    FF sum{wp[0].x, wp[0].y};
-                    for (int w = 1; w < kStagedConsumerWarps; ++w) sum = ff_add(sum, FF{wp[w].x, wp[w].y});
-                    ss.wcount[pend_ps] = 0;
-                    if constexpr (kF64Sums) {
-                        publish_chunk_f64(B.partials, pend_c, sum.hi, sum.lo);
-                    } else {
-                        reinterpret_cast<float2*>(B.partials)[pend_c] = make_float2(sum.hi, sum.lo);
-                    }
-                }
-            }
-            pend_c = -1;
-        };
         RingCursor rc(seq, NS);
-        for (;;) {
+        for (int j = 0; j < n_stages; ++j) {
             // one decision per warp: the product below shuffles over the full warp
             const bool stop = __any_sync(
                 0xffffffffu, *abort_flag || !mbar_wait(smem_addr(&ss.full[rc.slot]), rc.parity, B.staged.max_polls));
@@ -1608,22 +1581,11 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
                 *abort_flag = 1;
                 break;
             }
-            const int c = *(volatile int*)&ss.chunk[rc.slot];
-            if (c < 0) {  // end of this pass
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
-                if (pend_c >= 0) publish();
-                store_pending();
-                rc.advance(NS);
-                break;
-            }
-            if (pend_c >= 0) publish();
-            store_pending();
             const unsigned char* st = ss.stage0 + rc.slot * stage_bytes;
             const int32_t* rp = reinterpret_cast<const int32_t*>(st + (size_t)10 * CAP * 4);
             const int kb4 = rp[0] & ~3;
-            const int row = c * S + lr;
-            const bool valid = row < n;
+            const int row = row_begin + j * S + lr;
+            const bool valid = row < row_end && lr < S;
             const int kb = valid ? rp[lr] - kb4 : 0, ke = valid ? rp[lr + 1] - kb4 : 0;
             const int32_t* __restrict__ scols = reinterpret_cast<const int32_t*>(st + (size_t)9 * CAP * 4);
             const float* __restrict__ svals = reinterpret_cast<const float*>(st);
@@ -1641,21 +1603,17 @@ __device__ __forceinline__ void staged_spmv_pass_dyn(const PcgBuffers<float>& B,
             const float wd = quad_row_product(kb, ke, q, scols, svals, CAP, pv);
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_addr(&ss.empty[rc.slot]));
-            FF t{0.f, 0.f};
             if (own) {
-                pend_pd = first ? zo : fmaf(beta, po, zo);
-                pend_qd = first ? wd : fmaf(beta, qo, wd);
-                pend_o = o;
-                t = ff_prod(pend_pd, pend_qd);
+                const float pd = first ? zo : fmaf(beta, po, zo);
+                const float qd = first ? wd : fmaf(beta, qo, wd);
+                p_new[o] = pd;
+                B.q[o] = qd;  // only this lane reads and writes component o of q in a pass
+                pq.add_prod(pd, qd);
             }
-            pend_own = own;
-            pend = t;
-            pend_c = c;
-            pend_ps = rc.g % kStagedPartSlots;
             rc.advance(NS);
         }
-        seq = rc.g;
     }
+    seq += n_stages;  // every thread, producer included: the next pass's first stage
 }
 
 // Block-wide float-float sums of two values per thread in a fixed tree; valid in thread 0.
@@ -1851,11 +1809,11 @@ __global__ void __launch_bounds__(256) k_pcg_update(PcgBuffers<T> B, const T* __
 
 // ---------------------------------------------------------------- persistent PCG
 // The whole PCG loop in one cooperative launch (all blocks resident): per iteration the
-// staged product pass over dynamically claimed chunks (staged_spmv_pass_dyn), a grid
-// barrier, p.Ap from the chunk partials (every block sums them itself in one fixed order,
-// so all blocks hold the same alpha), the update of the block's own rows (x, r, z, r.r, r.z;
-// rows split evenly over the blocks), a second grid barrier, and the convergence test and
-// beta, computed identically in every block.  The iteration and its stopping rules are those
+// staged product pass over the block's own rows (staged_pass_rows; an even split in units of
+// four rows), a grid barrier, p.Ap from the block partials (every block sums them itself in
+// one fixed order, so all blocks hold the same alpha), the update of the same rows (x, r, z,
+// r.r, r.z), a second grid barrier, and the convergence test and beta, computed identically
+// in every block.  The iteration and its stopping rules are those
 // of k_pcg_spmv + k_pcg_update.  Plain (L1-cached) loads are safe across iterations: the
 // barrier's acquire at GPU scope, ordered before every thread of the block by __syncthreads,
 // makes the other blocks' writes visible to them (the guarantee a grid synchronization
@@ -1910,6 +1868,17 @@ struct PcgCtl {
     int have_rr;  // rr holds a residual of this launch
 };
 
+// Rows [row_begin, row_end) of block b of G in the persistent kernel: an even split in units of
+// four rows, so every stage of S rows (S a multiple of four) starts on a 16-byte boundary of
+// row_ptr, as its bulk copy requires.
+__host__ __device__ __forceinline__ void pcg_block_rows(int64_t b, int64_t G, int64_t n, int& row_begin, int& row_end)
+{
+    const int64_t units = (n + 3) / 4;
+    const int64_t rb = 4 * (b * units / G), re = 4 * ((b + 1) * units / G);
+    row_begin = (int)(rb < n ? rb : n);
+    row_end = (int)(re < n ? re : n);
+}
+
 // Chunks of the persistent kernel's product pass (one stage of rows each).
 __host__ __device__ __forceinline__ int pcg_chunks(int n_blocks, int stage_rows)
 {
@@ -1933,18 +1902,17 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
     __syncthreads();
     volatile int* abort_flag = &aborted;
     unsigned* bar = B.tickets + 6;
-    unsigned* ctr = B.tickets + 8;  // chunk counters of three consecutive passes
     unsigned generation = 0, seq = 0, issued = 0;
-    DynProducer P;
     const unsigned G = gridDim.x;
-    const int n_chunks = pcg_chunks(B.n_blocks, B.staged.stage_rows);
-    const PcgSumsLayout lay = pcg_sums_layout(n_chunks, (int)G);
-    float2* part_rr = reinterpret_cast<float2*>(B.partials + n_chunks);  // FF sums
+    // block partials (FF sums: float2, FP64 sums: double; 8 bytes each): p.Ap, r.r, r.z
+    float2* part_pq = reinterpret_cast<float2*>(B.partials);
+    float2* part_rr = part_pq + G;
     float2* part_rz = part_rr + G;
-    double* part_rr64 = B.partials + lay.rr;  // FP64 sums
-    double* part_rz64 = B.partials + lay.rz;
-    const int row_begin = (int)((int64_t)blockIdx.x * B.n_blocks / G);
-    const int row_end = (int)((int64_t)(blockIdx.x + 1) * B.n_blocks / G);
+    double* part_pq64 = B.partials;
+    double* part_rr64 = B.partials + G;
+    double* part_rz64 = B.partials + 2 * G;
+    int row_begin, row_end;
+    pcg_block_rows(blockIdx.x, G, B.n_blocks, row_begin, row_end);
     // a launch after a residual replacement continues the recurrence: beta from the state
     // the FP64 recurrence is thread 0's (PcgCtl); every thread counts the iterations
     __shared__ PcgCtl ctl;
@@ -1969,16 +1937,22 @@ __global__ void __launch_bounds__(kStagedThreads, 2) k_pcg_solve_staged(PcgBuffe
         float* p_old = (iteration & 1) ? B.p : B.p2;
         float* p_new = (iteration & 1) ? B.p2 : B.p;
         const bool first = iteration == 0;
-        staged_spmv_pass_dyn<kF64Sums>(B, ss, li, ctr, n_chunks, p_old, p_new, first, first ? 0.f : beta_f, seq,
-                                       issued, P, abort_flag);
+        DotAcc<float> pqa;
+        staged_pass_rows(B, ss, row_begin, row_end, p_old, p_new, first, first ? 0.f : beta_f, seq, issued, abort_flag,
+                         pqa);
+        {
+            FF bpq, unused;
+            block_sum2_ff(pqa.v, FF{0.f, 0.f}, sh, bpq, unused);  // valid in thread 0
+            if (threadIdx.x == 0) {
+                if (kF64Sums) part_pq64[blockIdx.x] = (double)bpq.hi + (double)bpq.lo;
+                else part_pq[blockIdx.x] = make_float2(bpq.hi, bpq.lo);
+            }
+        }
         if (!grid_barrier(bar, generation, &barrier_ok, B.staged.max_polls) || *abort_flag) {
             failed = true;
             break;
         }
-        // no block claims from pass li - 1 any more, none from pass li + 2 before the next barrier
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ctr[(li + 2) % 3], 0u);
-        const double pAp = kF64Sums ? sum_partials_f64(B.partials, n_chunks, sh)
-                                    : sum_chunk_partials(reinterpret_cast<const float2*>(B.partials), n_chunks, sh);
+        const double pAp = kF64Sums ? sum_partials_f64(part_pq64, (int)G, sh) : sum_chunk_partials(part_pq, (int)G, sh);
         if (threadIdx.x == 0) {
             ctl.stop = 0;
             ctl.pAp = pAp;
@@ -3092,9 +3066,17 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
         const int64_t grid = (int64_t)sms * per_sm;
         const int64_t rows = ((n + grid - 1) / grid + S - 1) / S * S;
         int64_t cap = 4;
-        for (int64_t r0 = 0; r0 < grid * rows; r0 += S) {
+        for (int64_t r0 = 0; r0 < grid * rows; r0 += S) {  // chunks (dynamic schedule, fixed ranges)
             const int64_t kb = rp[std::min<int64_t>(r0, n)], ke = rp[std::min<int64_t>(r0 + S, n)];
             cap = std::max<int64_t>(cap, ((ke + 3) & ~int64_t(3)) - (kb & ~int64_t(3)));
+        }
+        for (int64_t b = 0; b < grid; ++b) {  // stages of the even row split (persistent kernel)
+            int rb, re;
+            pcg_block_rows(b, grid, n, rb, re);
+            for (int64_t r0 = rb; r0 < re; r0 += S) {
+                const int64_t kb = rp[r0], ke = rp[std::min<int64_t>(r0 + S, re)];
+                cap = std::max<int64_t>(cap, ((ke + 3) & ~int64_t(3)) - (kb & ~int64_t(3)));
+            }
         }
         const size_t stage_bytes = staged_stage_bytes((int)cap, S);
         const int64_t budget =
@@ -3126,8 +3108,7 @@ StagedSizes plan_staged_spmv(int n, const int32_t* rp, PcgBuffers<float>::Staged
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident_f64, k_pcg_solve_staged<true>, kStagedThreads,
                                                           smem) == cudaSuccess &&
             resident_ff >= per_sm && resident_f64 >= per_sm &&
-            pcg_sums_layout(pcg_chunks(n, S), (int)grid).total <= 2 * kPcgMaxPartials &&
-            pcg_chunks(n, S) + 2 * grid <= 2 * kPcgMaxPartials)
+            3 * grid <= 2 * kPcgMaxPartials)
             st.persistent = 1;
         cudaGetLastError();
         // the look-ahead form: its own header, the same ring; partials of two passes
