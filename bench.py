@@ -249,8 +249,10 @@ def run_ours(args):
             "stage_seconds": {k: round(vst[k], 6) for k in vst if k.startswith("t_")},
             "vs_fp64_step_speedup": round(statistics.mean(fp64_ms) / statistics.mean(vms), 3)}
 
-    # end to end through the C ABI with host arrays
-    solver.set_settings(precision="mixed")
+    # end to end through the C ABI with host arrays, with the headline's settings (the variants
+    # above changed the projection, residual and partial-sum settings)
+    solver.set_settings(precision="mixed", projection_fp64_refinement=0, cg_residual_replacement=0,
+                        cg_fp64_partial_sums=0)
     e2e_ms, e2e_st = [], None
     for i in range(args.steps + 1):
         torch.cuda.synchronize()
